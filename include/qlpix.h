@@ -1,0 +1,198 @@
+/*
+ * qlpix.h -- C ABI of the GB300 pixel-image likelihood library (libqlpix.so).
+ *
+ * The library evaluates QLens's pixel-level log-evidence for a Cartesian
+ * pixellated source: it ray-shoots the masked, split image pixels through the
+ * lens model, builds the lensing matrix L on the source grid, convolves L with
+ * the PSF, assembles F = L^T C^-1 L + lambda R, solves for the source
+ * amplitudes and returns chi^2 plus the regularised log-evidence terms.
+ *
+ * Drop-in boundary: one call of qlp_eval() replaces one call of
+ *   double QLens::invert_image_surface_brightness_map(double &chisq0,
+ *                                                     bool verbal, int ranchisq_i)
+ *   (qlens.h:944, lens.cpp:12293-13195; Cartesian branch lens.cpp:12431-12624,
+ *    chi^2 loop lens.cpp:12950-13016)
+ * for source_fit_mode=cartesian, ray_tracing_method=interpolate,
+ * inversion_method=dense, regularization curvature (or none).  The return
+ * value m2logev of qlp_result is that function's return value, chisq0 is what
+ * it writes into its reference argument.
+ *
+ * Conventions
+ *  - Plain C types only; caller-owned input and output buffers; every call
+ *    returns an int status (QLP_OK = 0).  No exceptions cross the ABI.
+ *  - Image arrays are indexed [i*npixels_y + j] with i along x and j along y,
+ *    the layout of QLens's ImagePixelData::surface_brightness[i][j].
+ *  - Lens parameters follow the QLens 'lens' command order (see qlp_lens).
+ *  - One context per host thread; a context owns one CUDA stream on one GPU.
+ *  - Failures the reference reports with sentinels keep those sentinels in
+ *    qlp_result.m2logev (2e30 for an unusable source grid, -1e30 for missing
+ *    data) and also set a distinct status code.
+ */
+#ifndef QLPIX_H
+#define QLPIX_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define QLP_OK                   0
+#define QLP_ERR_ARG              1  /* bad argument or size */
+#define QLP_ERR_CUDA             2  /* CUDA runtime error (message in qlp_last_error) */
+#define QLP_ERR_NOT_SPD          3  /* F or R not positive definite (reference: die) */
+#define QLP_ERR_NO_SOURCE_PIXELS 4  /* no active source cell (reference: return 2e30) */
+#define QLP_ERR_GRID_TOO_SMALL   5  /* source grid < 2 cells a side (reference: return 2e30) */
+#define QLP_ERR_NO_DATA          6  /* no image data (reference: return -1e30) */
+#define QLP_ERR_NOMEM            7  /* device allocation failed */
+#define QLP_ERR_TIMEOUT          8  /* a bounded device wait ran out */
+#define QLP_ERR_NO_DEVICE        9  /* no CUDA device / library built without GPU support */
+
+/* ---- lens models ---- */
+#define QLP_LENS_SPLE  0  /* p = b, alpha, s, q, theta_deg, xc, yc        (models.cpp SPLE_Lens) */
+#define QLP_LENS_SHEAR 1  /* p = shear, theta_deg, xc, yc                 (models.cpp Shear) */
+#define QLP_LENS_NFW   2  /* p = ks, rs, q, theta_deg, xc, yc             (models.cpp NFW) */
+#define QLP_MAX_LENSES 8
+#define QLP_MAX_PLANES 4
+#define QLP_MAX_PARAMS 8
+
+/* ---- precision modes ---- */
+#define QLP_FP64  0  /* plain FP64 everywhere */
+#define QLP_MIXED 1  /* FP32-class tensor-core SYRK + Cholesky, FP64 refinement/logdet/sums */
+
+typedef struct qlp_ctx qlp_ctx;
+
+typedef struct {
+    int type;                    /* QLP_LENS_* */
+    int plane;                   /* index into qlp_planes (0 for single-plane lensing) */
+    double p[QLP_MAX_PARAMS];    /* default parameters, QLens order */
+} qlp_lens;
+
+/* Multi-plane redshift factors (QLens::deflection, lenscalc.cpp:41-80):
+ * zfac[i] scales plane i's deflection; beta[i-1][j] couples plane j into
+ * plane i.  n_planes = 1 with zfac[0] = 1 is ordinary single-plane lensing. */
+typedef struct {
+    int n_planes;
+    double zfac[QLP_MAX_PLANES];
+    double beta[QLP_MAX_PLANES][QLP_MAX_PLANES];
+} qlp_planes;
+
+typedef struct {
+    int npixels_x, npixels_y;
+    const double* xvals;               /* npixels_x+1 pixel-corner x (ImagePixelData::xvals) */
+    const double* yvals;               /* npixels_y+1 pixel-corner y */
+    const double* surface_brightness;  /* data, [i*npixels_y + j] */
+    const double* covinv_map;          /* 1/sigma^2 per pixel, or NULL for a uniform noise */
+    double background_pixel_noise;     /* used when covinv_map == NULL */
+    const unsigned char* in_mask;      /* 1 = pixel is fitted */
+} qlp_image;
+
+typedef struct {
+    int nx, ny;                        /* odd sizes; psf[i*ny + j] like QLens psf_matrix[i][j] */
+    const double* matrix;
+} qlp_psf;
+
+typedef struct {
+    int nsplit;                        /* default_imgpixel_nsplit (split_imgpixels on) */
+    int npixels_x, npixels_y;          /* source-grid cells (src_npixels) */
+    int auto_sourcegrid;               /* 1: bounds from ray-traced sub-pixels (find_optimal_sourcegrid) */
+    double xmin, xmax, ymin, ymax;     /* fixed bounds when auto_sourcegrid == 0 */
+    double limit_xmin, limit_xmax, limit_ymin, limit_ymax;  /* sourcegrid_limit_* (default +-1e30) */
+    double noise_threshold;            /* QLens noise_threshold (default 0 = off) */
+    double size_scale;                 /* srcgrid_size_scale (default 0 = off) */
+    int regularization;                /* 0 none, 1 curvature */
+    double regparam;                   /* lambda */
+} qlp_srcgrid_opts;
+
+typedef struct {
+    double m2logev;       /* -2 log(evidence) (no priors): chisq0 + regterms + logdet_F */
+    double chisq0;
+    double logdet_F;
+    double logdet_R;
+    double Es_times_two;  /* s^T R s */
+    double regterms;      /* lambda*Es_times_two - M*ln(lambda) - logdet_R */
+    int n_active_pixels;  /* image_npixels */
+    int n_active_src;     /* source_npixels (M) */
+    long long L_nnz;      /* nonzeros of the pre-PSF L */
+    int status;
+    int refine_iters;     /* FP64 refinement sweeps used (mixed precision) */
+} qlp_result;
+
+/* Per-instance description for batched evaluation (uneven masks / grids). */
+typedef struct {
+    int mask_id;          /* index into the masks given to qlp_set_instance_masks, or -1 = image mask */
+    int src_npixels_x;    /* source-grid size for this instance */
+    int src_npixels_y;
+} qlp_instance;
+
+/* Defaults for a qlp_srcgrid_opts (QLens constructor defaults, lens.cpp:185-560). */
+void qlp_srcgrid_defaults(qlp_srcgrid_opts* opts);
+
+/* Create a context: uploads the image, mask, noise and PSF to `device`.
+ * Replaces QLens's ImagePixelData/ImagePixelGrid set-up
+ * (pixelgrid.cpp:9622-9700, 9940-10099, set_nsplits 10898-10938). */
+qlp_ctx* qlp_create(const qlp_image* image, const qlp_psf* psf,
+                    const qlp_srcgrid_opts* opts, int device, int* status);
+
+/* Lens list (QLens lens_list + lens redshift planes).  The p[] of each lens
+ * are the defaults used by qlp_eval when lens_params is NULL. */
+int qlp_set_lens_model(qlp_ctx* ctx, const qlp_lens* lenses, int nlens, const qlp_planes* planes);
+
+/* QLP_FP64 or QLP_MIXED. */
+int qlp_set_precision(qlp_ctx* ctx, int mode);
+
+/* Attach the context to an existing CUDA stream (cudaStream_t as void*);
+ * NULL restores the context's own stream. */
+int qlp_set_stream(qlp_ctx* ctx, void* stream);
+
+/* One likelihood evaluation.  lens_params: the concatenated p[] of every lens
+ * (count given by qlp_n_params), or NULL for the model defaults.
+ * regparam <= 0 uses opts->regparam.  Replaces
+ * QLens::invert_image_surface_brightness_map (lens.cpp:12293). */
+int qlp_eval(qlp_ctx* ctx, const double* lens_params, double regparam, qlp_result* out);
+
+/* Number of doubles in one lens-parameter vector for the current model. */
+int qlp_n_params(const qlp_ctx* ctx);
+
+/* Extra masks for batched evaluation ([n_masks][npixels_x*npixels_y]). */
+int qlp_set_instance_masks(qlp_ctx* ctx, const unsigned char* masks, int n_masks);
+
+/* Batched evaluation of n parameter vectors (nested-sampling live points,
+ * T-Walk proposals): params is [n][qlp_n_params], regparams [n] (or NULL),
+ * inst [n] (or NULL = image mask and opts grid for all).  Results in out[n].
+ * Generalises the per-group evaluation of UCMC::MonoSample / TWalk
+ * (mcmchdr.cpp:2901-3087, 820) to one device launch sequence. */
+int qlp_eval_batch(qlp_ctx* ctx, const double* params, const double* regparams,
+                   const qlp_instance* inst, int n, qlp_result* out);
+
+/* Parity hooks: copy intermediates of the last qlp_eval to host buffers
+ * (any pointer may be NULL; sizes are in elements and must be large enough,
+ * query them with the matching n_* fields of qlp_result).
+ *  srcpt_xy   [2*N_sub]  sub-pixel source points, masked pixels in j-outer /
+ *                        i-inner order, sub-cells in QLens order
+ *  L_rowptr   [N_pix+1], L_index [nnz], L_value [nnz]  pre-PSF L (CSR)
+ *  active_index [src_nx*src_ny]  active index per cell ([j*src_nx+i]) or -1
+ *  D [M], s [M], model [N_pix] */
+int qlp_dump(qlp_ctx* ctx, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value,
+             int* active_index, double* D, double* s, double* model);
+
+/* Copy the first `rows` rows of the PSF-convolved dense L (row-major, M
+ * columns) of the last qlp_eval. */
+int qlp_dump_Lpsf(qlp_ctx* ctx, int rows, double* out);
+
+/* Milliseconds of device time per stage of the last qlp_eval (CUDA events):
+ * [0] ray shooting, [1] grid+mapping, [2] L+PSF, [3] F/D assembly,
+ * [4] factorisations+solve, [5] model+chi^2.  n >= 6. */
+int qlp_stage_times(qlp_ctx* ctx, float* ms, int n);
+
+/* Number of kernel launches issued by the last qlp_eval / qlp_eval_batch. */
+long long qlp_last_launch_count(const qlp_ctx* ctx);
+
+/* Message of the last error on this thread ("" if none). */
+const char* qlp_last_error(void);
+
+void qlp_destroy(qlp_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QLPIX_H */

@@ -1,0 +1,85 @@
+"""Python loader for the C oracle (oracle/qlpix_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py as the checker.  The product never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from qlens_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libqlpix_oracle.so")
+SOURCES = [os.path.join(HERE, "qlpix_oracle.c"), os.path.join(HERE, "nfw_oracle.c")]
+
+
+def build(force=False):
+    """Compile the oracle with gcc (OpenMP, no fused multiply-adds)."""
+    deps = SOURCES + [os.path.join(HERE, "qlpix_oracle.h"),
+                      os.path.join(os.path.dirname(HERE), "include", "qlpix.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           "-Wall", "-Wno-unknown-pragmas"] + SOURCES + ["-o", tmp, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.oracle_eval.restype = C.c_int
+        _lib.oracle_eval.argtypes = [C.POINTER(abi.qlp_image), C.POINTER(abi.qlp_psf),
+                                     C.POINTER(abi.qlp_srcgrid_opts), C.POINTER(abi.qlp_lens), C.c_int,
+                                     C.POINTER(abi.qlp_planes), C.POINTER(C.c_double), C.c_double,
+                                     C.POINTER(abi.qlp_result)]
+        _lib.oracle_get.restype = C.c_long
+        _lib.oracle_get.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
+        _lib.oracle_threads.restype = C.c_int
+    return _lib
+
+
+_DT = {"srcpt": np.float64, "L_rowptr": np.int32, "L_index": np.int32, "L_value": np.float64,
+       "active_index": np.int32, "Lpsf": np.float64, "D": np.float64, "s": np.float64,
+       "model": np.float64, "F_diag": np.float64, "grid": np.float64}
+
+
+def get(name):
+    L = lib()
+    n = L.oracle_get(name.encode(), None, 0)
+    if n < 0:
+        raise KeyError(name)
+    out = np.empty(max(n, 0), dtype=_DT[name])
+    if n > 0:
+        L.oracle_get(name.encode(), out.ctypes.data_as(C.c_void_p), n)
+    return out
+
+
+def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.0, planes=None):
+    """Run the oracle; returns the qlp_result as a dict."""
+    L = lib()
+    lenses = abi.make_lenses(lens_spec)
+    pl = planes if planes is not None else abi.make_planes()
+    res = abi.qlp_result()
+    pp = None
+    if lens_params is not None:
+        arr = np.ascontiguousarray(lens_params, dtype=np.float64)
+        pp = arr.ctypes.data_as(C.POINTER(C.c_double))
+    L.oracle_eval(C.byref(image_bufs.image), C.byref(psf_buf.psf), C.byref(opts), lenses, len(lens_spec),
+                  C.byref(pl), pp, float(regparam), C.byref(res))
+    return res.as_dict()
+
+
+def threads():
+    return lib().oracle_threads()

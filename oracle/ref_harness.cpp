@@ -1,0 +1,281 @@
+// Golden-vector harness for the pixel-image likelihood (test infrastructure).
+//
+// Links the unmodified QLens reference objects (built by oracle/Makefile.ref)
+// and runs a script through QLens::process_commands to set up the mock data,
+// mask, PSF width, lens model and source-grid settings.  It then evaluates the
+// likelihood twice:
+//   1. through the entry point itself,
+//      QLens::invert_image_surface_brightness_map (lens.cpp:12293), which gives
+//      the reference -2 log(evidence) and chi^2_0;
+//   2. step by step along the Cartesian branch (lens.cpp:12431-12624), so the
+//      intermediates can be written out before clear_pixel_matrices frees them
+//      (pixelgrid.cpp:13104).
+// Every array goes to <outdir>/<name>.<f64|i32|u8> as raw little-endian data,
+// and the scalars go to <outdir>/scalars.txt.  tests/golden/make_golden.py
+// packs them into the committed .npz fixtures.
+//
+// Usage: qlens_harness <script.in> <outdir> [max_dense_rows]
+
+#include <cstdio>
+#include <cstdlib>
+#include <cmath>
+#include <complex>
+#include <fstream>
+#include <sstream>
+#include <iomanip>
+#include <map>
+#include <set>
+#include <vector>
+#include <string>
+#include <omp.h>
+#include <unistd.h>
+
+// The intermediates live in protected/private members.  Widening the access
+// in this translation unit only changes name lookup, not the object layout.
+#define private public
+#define protected public
+#include "qlens.h"
+#include "pixelgrid.h"
+#include "profile.h"
+#undef private
+#undef protected
+
+// ImagePixelGrid keeps these members in its implicit (class-default) private
+// section, which the #define above cannot reach.  Explicit template
+// instantiation is exempt from access checking, so a pointer-to-member can be
+// taken there and handed out through a friend function.
+template <typename Tag, typename Tag::type Member>
+struct MemberGrab { friend typename Tag::type grab(Tag) { return Member; } };
+#define GRAB(TAG, CLS, TYPE, NAME) \
+	struct TAG { typedef TYPE CLS::*type; friend type grab(TAG); }; \
+	template struct MemberGrab<TAG, &CLS::NAME>;
+GRAB(G_in_mask, ImagePixelGrid, bool**, pixel_in_mask)
+GRAB(G_nsplits, ImagePixelGrid, int**, nsplits)
+GRAB(G_subsrc, ImagePixelGrid, lensvector***, subpixel_center_sourcepts)
+GRAB(G_act_i, ImagePixelGrid, int*, active_image_pixel_i)
+GRAB(G_act_j, ImagePixelGrid, int*, active_image_pixel_j)
+
+static std::string g_out;
+
+template <typename T>
+static void dump(const char* name, const char* ext, const T* data, size_t n)
+{
+	std::string fn = g_out + "/" + name + "." + ext;
+	FILE* f = fopen(fn.c_str(), "wb");
+	if (!f) { fprintf(stderr, "cannot write %s\n", fn.c_str()); exit(2); }
+	if (n) fwrite(data, sizeof(T), n, f);
+	fclose(f);
+}
+static void dumpd(const char* name, const std::vector<double>& v) { dump(name, "f64", v.data(), v.size()); }
+static void dumpi(const char* name, const std::vector<int>& v) { dump(name, "i32", v.data(), v.size()); }
+static void dumpu(const char* name, const std::vector<unsigned char>& v) { dump(name, "u8", v.data(), v.size()); }
+
+int main(int argc, char** argv)
+{
+	if (argc < 3) { fprintf(stderr, "usage: %s script.in outdir [max_dense_rows]\n", argv[0]); return 1; }
+	g_out = argv[2];
+	long max_dense_rows = (argc > 3) ? atol(argv[3]) : -1;
+
+	int nthreads = 1;
+	#pragma omp parallel
+	{
+		#pragma omp master
+		nthreads = omp_get_num_threads();
+	}
+	Grid::allocate_multithreaded_variables(nthreads);
+	SourcePixel::allocate_multithreaded_variables(nthreads);
+	DelaunayGrid::allocate_multithreaded_variables(nthreads);
+	ImagePixelGrid::allocate_multithreaded_variables(nthreads);
+	QLens::allocate_multithreaded_variables(nthreads);
+
+	QLens lens;
+	lens.set_mpi_params(0, 1);
+	lens.set_verbal_mode(false);
+	lens.set_quit_after_error(true);
+	lens.set_suppress_plots(true);
+	if (!lens.open_script_file(argv[1])) { fprintf(stderr, "cannot open script %s\n", argv[1]); return 1; }
+	lens.set_quit_after_reading_file(true);
+	lens.process_commands(true);
+
+	ImagePixelData* d = lens.image_pixel_data;
+	if (d == NULL) { fprintf(stderr, "script loaded no image data\n"); return 1; }
+	const int nx = d->npixels_x, ny = d->npixels_y;
+	const int mask_k = lens.assigned_mask ? lens.assigned_mask[0] : 0;
+
+	// ---------- inputs ----------
+	{
+		std::vector<double> xv(d->xvals, d->xvals + nx + 1), yv(d->yvals, d->yvals + ny + 1);
+		dumpd("xvals", xv); dumpd("yvals", yv);
+		std::vector<double> sb(nx * ny), cov(nx * ny);
+		std::vector<unsigned char> mk(nx * ny);
+		for (int i = 0; i < nx; i++)
+			for (int j = 0; j < ny; j++) {
+				sb[i * ny + j] = d->surface_brightness[i][j];
+				cov[i * ny + j] = (d->covinv_map != NULL) ? d->covinv_map[i][j] : 0.0;
+				mk[i * ny + j] = d->in_mask[mask_k][i][j] ? 1 : 0;
+			}
+		dumpd("data", sb); dumpd("covinv", cov); dumpu("mask", mk);
+	}
+
+	// ---------- 1. the entry point itself ----------
+	double chisq0_entry = 0;
+	double m2logev_entry = lens.invert_surface_brightness_map_from_data(chisq0_entry, false, true);
+	const double logdetF_entry = lens.Fmatrix_log_determinant;
+	const double logdetR_entry = lens.Rmatrix_log_determinant;
+
+	// ---------- 2. the Cartesian branch, step by step ----------
+	ImagePixelGrid* g = lens.image_pixel_grids[0];
+	int src_i = 0;
+	if (lens.cartesian_srcgrids[src_i] == NULL) lens.cartesian_srcgrids[src_i] = new SourcePixelGrid(&lens);
+	SourcePixelGrid* sg = lens.cartesian_srcgrids[src_i];
+	g->redo_lensing_calculations(false);
+	g->set_cartesian_srcgrid(sg);
+	double sxmin = lens.sourcegrid_xmin, sxmax = lens.sourcegrid_xmax, symin = lens.sourcegrid_ymin, symax = lens.sourcegrid_ymax;
+	if (lens.auto_sourcegrid) {
+		g->find_optimal_sourcegrid(sxmin, sxmax, symin, symax, lens.sourcegrid_limit_xmin, lens.sourcegrid_limit_xmax, lens.sourcegrid_limit_ymin, lens.sourcegrid_limit_ymax);
+		if (sg->srcgrid_size_scale != 0) {
+			double xw = sg->srcgrid_size_scale * (sxmax - sxmin), yw = sg->srcgrid_size_scale * (symax - symin);
+			double xc = (sxmax + sxmin) / 2, yc = (symax + symin) / 2;
+			sxmin = xc - xw / 2; sxmax = xc + xw / 2; symin = yc - yw / 2; symax = yc + yw / 2;
+		}
+	}
+	const int snx = lens.srcgrid_npixels_x, sny = lens.srcgrid_npixels_y;
+	sg->create_pixel_grid(&lens, sxmin, sxmax, symin, symax, snx, sny);
+	sg->set_image_pixel_grid(g);
+	lens.regparam_ptr = &(sg->regparam);
+	bool** in_mask = g->*grab(G_in_mask());
+	int** nsplits = g->*grab(G_nsplits());
+	lensvector*** subsrc = g->*grab(G_subsrc());
+
+	// sub-pixel source points, in the reference's own (pixel j-outer, i-inner; subcell) order over masked pixels
+	{
+		std::vector<double> spx, spy;
+		std::vector<int> sp_pix;
+		for (int j = 0; j < ny; j++)
+			for (int i = 0; i < nx; i++)
+				if (in_mask[i][j]) {
+					int ns = nsplits[i][j] * nsplits[i][j];
+					for (int k = 0; k < ns; k++) {
+						spx.push_back(subsrc[i][j][k][0]);
+						spy.push_back(subsrc[i][j][k][1]);
+					}
+					sp_pix.push_back(i * ny + j);
+				}
+		dumpd("srcpt_x", spx); dumpd("srcpt_y", spy); dumpi("masked_pixels", sp_pix);
+	}
+
+	if (!lens.assign_pixel_mappings(0, false)) { fprintf(stderr, "assign_pixel_mappings failed\n"); return 3; }
+	lens.assign_foreground_mappings(0);
+	{
+		std::vector<double> corners_x(snx + 1), corners_y(sny + 1);
+		for (int i = 0; i < snx; i++) corners_x[i] = sg->cell[i][0]->corner_pt[0][0];
+		corners_x[snx] = sg->cell[snx - 1][0]->corner_pt[2][0];
+		for (int j = 0; j < sny; j++) corners_y[j] = sg->cell[0][j]->corner_pt[0][1];
+		corners_y[sny] = sg->cell[0][sny - 1]->corner_pt[1][1];
+		dumpd("src_corner_x", corners_x); dumpd("src_corner_y", corners_y);
+		std::vector<int> act(snx * sny);
+		for (int j = 0; j < sny; j++)
+			for (int i = 0; i < snx; i++)
+				act[j * snx + i] = sg->cell[i][j]->active_pixel ? sg->cell[i][j]->active_index : -1;
+		dumpi("active_index", act);
+		std::vector<int> api(lens.image_npixels);
+		int* act_i = g->*grab(G_act_i());
+		int* act_j = g->*grab(G_act_j());
+		for (int k = 0; k < lens.image_npixels; k++) api[k] = act_i[k] * ny + act_j[k];
+		dumpi("active_pixels", api);
+	}
+
+	lens.initialize_pixel_matrices(0, false);
+	const int npix = lens.image_npixels, nsrc = lens.source_n_amps;
+	const int nnz = lens.image_pixel_location_Lmatrix[npix];
+	{
+		std::vector<int> rp(lens.image_pixel_location_Lmatrix, lens.image_pixel_location_Lmatrix + npix + 1);
+		std::vector<int> ci(lens.Lmatrix_index, lens.Lmatrix_index + nnz);
+		std::vector<double> v(lens.Lmatrix, lens.Lmatrix + nnz);
+		dumpi("L_rowptr", rp); dumpi("L_index", ci); dumpd("L_value", v);
+	}
+	lens.create_regularization_matrix(0);
+	const double logdetR_steps = lens.Rmatrix_log_determinant;
+	{
+		int rnn = lens.Rmatrix_index[nsrc];
+		std::vector<double> rv(lens.Rmatrix, lens.Rmatrix + rnn);
+		std::vector<int> ri(lens.Rmatrix_index, lens.Rmatrix_index + rnn);
+		dumpd("R_value", rv); dumpi("R_index", ri);
+	}
+	lens.convert_Lmatrix_to_dense();
+	lens.PSF_convolution_Lmatrix_dense(0, false);
+	{
+		std::vector<double> psf(lens.psf_npixels_x * lens.psf_npixels_y);
+		for (int i = 0; i < lens.psf_npixels_x; i++)
+			for (int j = 0; j < lens.psf_npixels_y; j++) psf[i * lens.psf_npixels_y + j] = lens.psf_matrix[i][j];
+		dumpd("psf", psf);
+		long rows = (max_dense_rows < 0 || max_dense_rows > npix) ? npix : max_dense_rows;
+		std::vector<double> Ld((size_t)rows * nsrc);
+		for (long r = 0; r < rows; r++)
+			for (int c = 0; c < nsrc; c++) Ld[r * nsrc + c] = lens.Lmatrix_dense[r][c];
+		dumpd("Lpsf_rows", Ld);
+		// column sums and a row-weighted checksum of the full PSF-convolved L
+		std::vector<double> colsum(nsrc, 0.0), rowsum(npix, 0.0);
+		for (int r = 0; r < npix; r++)
+			for (int c = 0; c < nsrc; c++) { colsum[c] += lens.Lmatrix_dense[r][c]; rowsum[r] += lens.Lmatrix_dense[r][c]; }
+		dumpd("Lpsf_colsum", colsum); dumpd("Lpsf_rowsum", rowsum);
+	}
+	g->fill_surface_brightness_vector();
+	if (!lens.ignore_foreground_in_chisq) {
+		lens.calculate_foreground_pixel_surface_brightness(0, true);
+		lens.store_foreground_pixel_surface_brightness(0);
+	}
+	lens.create_lensing_matrices_from_Lmatrix_dense(0, false);
+	{
+		std::vector<double> D(lens.Dvector, lens.Dvector + nsrc);
+		dumpd("D", D);
+		std::vector<double> Fdiag(nsrc), Fp(lens.Fmatrix_packed.array(), lens.Fmatrix_packed.array() + (size_t)nsrc * (nsrc + 1) / 2);
+		size_t idx = 0;
+		for (int i = 0; i < nsrc; i++) { Fdiag[i] = Fp[idx]; idx += nsrc - i; }
+		dumpd("F_diag", Fdiag);
+		if (nsrc <= 1200) dumpd("F_packed_upper", Fp);
+	}
+	lens.invert_lens_mapping_dense(0, false);
+	const double logdetF_steps = lens.Fmatrix_log_determinant;
+	{
+		std::vector<double> s(lens.source_pixel_vector, lens.source_pixel_vector + nsrc);
+		dumpd("s", s);
+	}
+	lens.calculate_image_pixel_surface_brightness_dense();
+	{
+		std::vector<double> m(lens.image_surface_brightness, lens.image_surface_brightness + npix);
+		dumpd("model", m);
+	}
+	lens.store_image_pixel_surface_brightness(0);
+	double regterms = lens.calculate_regularization_prior_term(lens.regparam_ptr);
+	const double regparam = *lens.regparam_ptr;
+
+	std::ofstream sc((g_out + "/scalars.txt").c_str());
+	sc << std::setprecision(17);
+	sc << "m2logev " << m2logev_entry << "\n";
+	sc << "chisq0 " << chisq0_entry << "\n";
+	sc << "logdetF " << logdetF_entry << "\n";
+	sc << "logdetR " << logdetR_entry << "\n";
+	sc << "logdetF_steps " << logdetF_steps << "\n";
+	sc << "logdetR_steps " << logdetR_steps << "\n";
+	sc << "regterms " << regterms << "\n";
+	sc << "regparam " << regparam << "\n";
+	sc << "n_active_pixels " << npix << "\n";
+	sc << "n_active_src " << nsrc << "\n";
+	sc << "L_nnz " << nnz << "\n";
+	sc << "src_xmin " << sxmin << "\nsrc_xmax " << sxmax << "\nsrc_ymin " << symin << "\nsrc_ymax " << symax << "\n";
+	sc << "srcgrid_nx " << snx << "\nsrcgrid_ny " << sny << "\n";
+	sc << "nx " << nx << "\nny " << ny << "\n";
+	sc << "psf_nx " << lens.psf_npixels_x << "\npsf_ny " << lens.psf_npixels_y << "\n";
+	sc << "nsplit " << lens.default_imgpixel_nsplit << "\n";
+	sc << "use_noise_map " << (lens.use_noise_map ? 1 : 0) << "\n";
+	sc << "background_pixel_noise " << lens.background_pixel_noise << "\n";
+	sc << "nthreads " << nthreads << "\n";
+	sc.close();
+	printf("m2logev=%.17g chisq0=%.17g logdetF=%.17g logdetR=%.17g npix=%d nsrc=%d nnz=%d\n",
+		m2logev_entry, chisq0_entry, logdetF_entry, logdetR_entry, npix, nsrc, nnz);
+	fflush(stdout);
+	// The reference's teardown after a hand-driven inversion frees some
+	// matrices twice; everything is on disk now, so leave without running it.
+	_exit(0);
+}

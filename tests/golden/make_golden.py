@@ -1,0 +1,217 @@
+"""Generate the committed golden fixtures from the compiled QLens reference.
+
+Run in a container that has the reference sources (read-only) and g++:
+
+    make -f oracle/Makefile.ref -j8 REF=/root/reference
+    python tests/golden/make_golden.py
+
+For every case below this writes a QLens script, runs oracle/_ref/qlens_harness
+on it (the reference's own mock-data generator, lens models and pixel
+likelihood, see oracle/ref_harness.cpp) and packs what the harness dumped into
+tests/golden/<case>.npz.  The .npz holds:
+
+* inputs the product needs: pixel corner coordinates, data, inverse-variance
+  map, mask, PSF matrix and the lens/source-grid configuration;
+* reference intermediates: sub-pixel source points, pre-PSF L in CSR form,
+  active source cells, R, D, diag(F) (full packed F for small grids), s, the
+  model image, and a few rows plus row/column sums of the PSF-convolved L;
+* reference scalars: chi^2_0, log det F, log det R, regularisation terms and
+  -2 log(evidence) as returned by QLens::invert_image_surface_brightness_map.
+
+The lens configuration is stored in the library's own parameter convention
+(SPLE: b, alpha, s, q, theta_deg, xc, yc; SHEAR: shear, theta_deg, xc, yc),
+which is the same convention the QLens 'lens' command uses.
+"""
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(REPO, "oracle", "_ref", "qlens_harness")
+
+# Each case: QLens script lines (everything up to, but not including, the
+# inversion) and the lens model in library convention.
+CASES = {
+    # 80x80 SIE + shear, the configuration of the reference's headline
+    # single-likelihood run (r < 2.5" mask, 2x2 split, 30x30 source, lambda=10).
+    "cfg1": dict(
+        script="""random_seed 10
+grid -2 2 -2 2
+img_npixels 80 80
+emode 1
+lens sple 1.2 1 0 0.8 30 0 0 shear=0.05 10
+source sersic 1 0.15 1.5 0.8 20 0.05 0
+psf_width 0.04247
+bg_pixel_noise 0.02
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0 2.5
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 30 30
+fit regularization curvature
+regparam 10
+imgpixel_nsplit 2
+split_imgpixels on
+inversion_method dense
+""",
+        lenses=[dict(type="sple", params=[1.2, 1.0, 0.0, 0.8, 30.0, 0.0, 0.0]),
+                dict(type="shear", params=[0.05, 10.0, 0.0, 0.0])],
+        dense_rows=48,
+        full_F=False,
+    ),
+    # small SIE + shear off the origin, 3x3 split, annular mask, 8x8 source
+    "tiny_sie": dict(
+        script="""random_seed 3
+grid -1.2 1.2 -1.2 1.2
+img_npixels 24 24
+emode 1
+lens sple 0.7 1 0 0.7 40 0.05 -0.03 shear=0.03 -20
+source sersic 2 0.12 1.2 0.85 10 0.02 0.03
+psf_width 0.06
+bg_pixel_noise 0.03
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0.2 1.2
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 8 8
+fit regularization curvature
+regparam 5
+imgpixel_nsplit 3
+split_imgpixels on
+inversion_method dense
+""",
+        lenses=[dict(type="sple", params=[0.7, 1.0, 0.0, 0.7, 40.0, 0.05, -0.03]),
+                dict(type="shear", params=[0.03, -20.0, 0.05, -0.03])],
+        dense_rows=-1,
+        full_F=True,
+    ),
+    # power-law slope alpha != 1 (Tessore et al. series), 4x4 split, annulus
+    "powerlaw": dict(
+        script="""random_seed 7
+grid -2 2 -2 2
+img_npixels 40 40
+emode 1
+lens sple 1.1 1.15 0 0.75 -35 0.02 0.01 shear=0.06 25
+source sersic 1.5 0.2 1 0.7 -15 0.04 -0.02
+psf_width 0.05
+bg_pixel_noise 0.01
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0.5 1.9
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 14 14
+fit regularization curvature
+regparam 20
+imgpixel_nsplit 4
+split_imgpixels on
+inversion_method dense
+""",
+        lenses=[dict(type="sple", params=[1.1, 1.15, 0.0, 0.75, -35.0, 0.02, 0.01]),
+                dict(type="shear", params=[0.06, 25.0, 0.02, 0.01])],
+        dense_rows=-1,
+        full_F=True,
+    ),
+    # fixed source grid smaller than the lensed source: some sub-pixels and
+    # some whole image pixels map outside the grid, some source cells stay
+    # inactive (unmapped pixels then add data^2 to chi^2)
+    "fixed_grid": dict(
+        script="""random_seed 5
+grid -1.5 1.5 -1.5 1.5
+img_npixels 30 30
+emode 1
+lens sple 0.9 1 0 0.8 10 0 0 shear=0.04 60
+source sersic 2 0.1 1.5 0.9 0 0.03 0.02
+psf_width 0.05
+bg_pixel_noise 0.02
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0 1.5
+fit source_mode cartesian
+srcgrid -0.12 0.18 -0.15 0.09
+auto_src_npixels off
+src_npixels 10 9
+fit regularization curvature
+regparam 3
+imgpixel_nsplit 2
+split_imgpixels on
+inversion_method dense
+""",
+        lenses=[dict(type="sple", params=[0.9, 1.0, 0.0, 0.8, 10.0, 0.0, 0.0]),
+                dict(type="shear", params=[0.04, 60.0, 0.0, 0.0])],
+        dense_rows=-1,
+        full_F=True,
+    ),
+}
+
+ARRAYS_F64 = ["xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
+              "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
+              "F_diag", "F_packed_upper", "s", "model"]
+ARRAYS_I32 = ["masked_pixels", "active_index", "active_pixels", "L_rowptr", "L_index", "R_index"]
+ARRAYS_U8 = ["mask"]
+
+
+def run_case(name, case, outdir):
+    tmp = tempfile.mkdtemp(prefix="golden_" + name + "_")
+    try:
+        script = os.path.join(tmp, name + ".in")
+        with open(script, "w") as f:
+            f.write(case["script"])
+        dump = os.path.join(tmp, "dump")
+        os.makedirs(dump)
+        env = dict(os.environ, OMP_NUM_THREADS="4")
+        r = subprocess.run([HARNESS, script, dump, str(case["dense_rows"])], cwd=tmp, env=env,
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("harness failed on %s:\n%s\n%s" % (name, r.stdout[-2000:], r.stderr[-2000:]))
+        out = {}
+        for key, dt, ext in ([(k, np.float64, "f64") for k in ARRAYS_F64] +
+                             [(k, np.int32, "i32") for k in ARRAYS_I32] +
+                             [(k, np.uint8, "u8") for k in ARRAYS_U8]):
+            p = os.path.join(dump, key + "." + ext)
+            if os.path.exists(p):
+                out[key] = np.fromfile(p, dtype=dt)
+        scalars = {}
+        with open(os.path.join(dump, "scalars.txt")) as f:
+            for line in f:
+                k, v = line.split()
+                scalars[k] = float(v)
+        meta = dict(name=name, lenses=case["lenses"], script=case["script"], scalars=scalars)
+        out["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(os.path.join(outdir, name + ".npz"), **out)
+        print("%-10s -2logev=%.10f chi2=%.6f logdetF=%.6f logdetR=%.6f npix=%d nsrc=%d" % (
+            name, scalars["m2logev"], scalars["chisq0"], scalars["logdetF"], scalars["logdetR"],
+            scalars["n_active_pixels"], scalars["n_active_src"]))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+def main(argv):
+    if not os.path.exists(HARNESS):
+        sys.exit("build the harness first: make -f oracle/Makefile.ref -j8 REF=/root/reference")
+    names = argv[1:] or list(CASES)
+    for n in names:
+        run_case(n, CASES[n], HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv)

@@ -1,0 +1,43 @@
+"""Load the committed golden fixtures (tests/golden/*.npz) into ABI inputs."""
+import json
+import os
+
+import numpy as np
+
+from qlens_gb300 import abi
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["tiny_sie", "fixed_grid", "powerlaw", "cfg1"]
+
+
+class Golden:
+    def __init__(self, name):
+        self.name = name
+        z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+        self.arr = {k: z[k] for k in z.files}
+        self.meta = json.loads(bytes(self.arr.pop("meta_json")).decode())
+        self.sc = self.meta["scalars"]
+        self.lenses = self.meta["lenses"]
+        nx, ny = int(self.sc["nx"]), int(self.sc["ny"])
+        self.nx, self.ny = nx, ny
+        covinv = self.arr["covinv"] if int(self.sc["use_noise_map"]) else None
+        self.image = abi.ImageBuffers(self.arr["xvals"], self.arr["yvals"], self.arr["data"],
+                                      self.arr["mask"], covinv, self.sc["background_pixel_noise"])
+        psf = self.arr["psf"].reshape(int(self.sc["psf_nx"]), int(self.sc["psf_ny"]))
+        self.psf = abi.PSFBuffer(psf)
+        o = abi.srcgrid_defaults()
+        o.nsplit = int(self.sc["nsplit"])
+        o.npixels_x = int(self.sc["srcgrid_nx"])
+        o.npixels_y = int(self.sc["srcgrid_ny"])
+        o.regparam = float(self.sc["regparam"])
+        o.regularization = 1
+        o.auto_sourcegrid = 1
+        for line in self.meta["script"].splitlines():
+            w = line.split()
+            if w and w[0] == "srcgrid" and len(w) == 5:
+                o.auto_sourcegrid = 0
+                o.xmin, o.xmax, o.ymin, o.ymax = map(float, w[1:])
+        self.opts = o
+
+    def params(self):
+        return abi.flat_params(self.lenses)
