@@ -1,0 +1,394 @@
+// ctx.cpp -- context set-up, workspace, and the per-evaluation launch sequence.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <cstdio>
+#include <vector>
+#include <algorithm>
+#include "qlpix_ctx.h"
+
+namespace qlpix {
+
+void psf_init_attributes();
+int mixed_init(qlp_ctx* c);
+void mixed_free(qlp_ctx* c);
+int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st);
+
+static int cuda_fail(cudaError_t e, const char* where)
+{
+    set_error("CUDA error in %s: %d", where, (int)e);
+    return (e == cudaErrorMemoryAllocation) ? QLP_ERR_NOMEM : QLP_ERR_CUDA;
+}
+
+#define CK(x, where) do { cudaError_t e__ = (x); if (e__ != cudaSuccess) return cuda_fail(e__, where); } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t n)
+{
+    return cudaMalloc((void**)p, sizeof(T) * (n > 0 ? n : 1));
+}
+
+static int round64(int x) { return (x + 63) & ~63; }
+
+// Masked pixels in the order QLens lists them (setup_ray_tracing_arrays,
+// pixelgrid.cpp:9996-10005: j outer, i inner).
+static std::vector<int> masked_list(const unsigned char* mask, int nx, int ny)
+{
+    std::vector<int> v;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++)
+            if (mask[i * ny + j]) v.push_back(i * ny + j);
+    return v;
+}
+
+static void free_work(Work& w)
+{
+    void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
+                    w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
+                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.gs, w.out};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    memset(&w, 0, sizeof(w));
+}
+
+// Workspace for up to n_mask masked pixels, nsub sub-pixels each and Mcells
+// source cells.
+static int alloc_work(qlp_ctx* c, int n_mask, int nsub, int Mcells, int snx_max, int sny_max)
+{
+    Work& w = c->w;
+    free_work(w);
+    const int Mc = round64(std::max(Mcells, 64));
+    const size_t n_sub = (size_t)n_mask * nsub;
+    const size_t nnz = 3 * n_sub;
+    CK(dalloc(&w.spx, n_sub), "alloc"); CK(dalloc(&w.spy, n_sub), "alloc");
+    CK(dalloc(&w.cx, snx_max + 1), "alloc"); CK(dalloc(&w.cy, sny_max + 1), "alloc");
+    CK(dalloc(&w.ccx, snx_max), "alloc"); CK(dalloc(&w.ccy, sny_max), "alloc");
+    CK(dalloc(&w.cell3, 3 * n_sub), "alloc"); CK(dalloc(&w.w3, 3 * n_sub), "alloc");
+    CK(dalloc(&w.mapped, Mcells), "alloc"); CK(dalloc(&w.active_index, Mcells), "alloc");
+    CK(dalloc(&w.pixmaps, n_mask), "alloc"); CK(dalloc(&w.rowidx, n_mask), "alloc");
+    CK(dalloc(&w.pixindex, (size_t)c->nx * c->ny), "alloc");
+    CK(dalloc(&w.rowpix, n_mask), "alloc");
+    CK(dalloc(&w.rowptr, n_mask + 1), "alloc");
+    CK(dalloc(&w.Lidx, nnz), "alloc"); CK(dalloc(&w.Lval, nnz), "alloc");
+    CK(dalloc(&w.cidx, nnz), "alloc"); CK(dalloc(&w.cval, nnz), "alloc"); CK(dalloc(&w.ccnt, n_mask), "alloc");
+    w.ldL = Mc;
+    CK(dalloc(&w.Lpsf, (size_t)n_mask * Mc), "alloc L'");
+    CK(dalloc(&w.dvec, n_mask), "alloc"); CK(dalloc(&w.cvec, n_mask), "alloc");
+    w.ldF = Mc;
+    CK(dalloc(&w.D, Mc), "alloc");
+    CK(dalloc(&w.F, (size_t)Mc * Mc), "alloc F");
+    CK(dalloc(&w.R, (size_t)Mc * Mc), "alloc R");
+    CK(dalloc(&w.s, Mc), "alloc"); CK(dalloc(&w.tmp, Mc), "alloc");
+    CK(dalloc(&w.model, n_mask), "alloc");
+    const size_t part = std::max((size_t)((n_mask + 255) / 256 + 1) * Mc, (size_t)Mc * 4);
+    CK(dalloc(&w.partial, part), "alloc");
+    CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc");
+    CK(cudaMemset(w.Lpsf, 0, sizeof(double) * (size_t)n_mask * Mc), "memset");
+    c->M_cap = Mc;
+    c->N_cap = n_mask;
+    c->nsub_cap = nsub;
+    return QLP_OK;
+}
+
+int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts* opts)
+{
+    c->nx = im->npixels_x;
+    c->ny = im->npixels_y;
+    c->opts = *opts;
+    const int nx = c->nx, ny = c->ny, npx = nx * ny;
+    c->mpix = masked_list(im->in_mask, nx, ny);
+    CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "stream");
+    c->stream = c->own_stream;
+    for (int i = 0; i <= QLP_N_STAGES; i++) CK(cudaEventCreate(&c->ev[i]), "event");
+    CK(cudaMallocHost((void**)&c->h_out, sizeof(EvalOut)), "pinned");
+
+    std::vector<double> covinv(npx);
+    const bool noise_map = im->covinv_map != nullptr;
+    const double cov_inverse = (im->background_pixel_noise == 0) ? 1.0
+                               : 1.0 / (im->background_pixel_noise * im->background_pixel_noise);
+    for (int t = 0; t < npx; t++) covinv[t] = noise_map ? im->covinv_map[t] : cov_inverse;
+    CK(dalloc(&c->d_xvals, nx + 1), "alloc"); CK(dalloc(&c->d_yvals, ny + 1), "alloc");
+    CK(dalloc(&c->d_data, npx), "alloc"); CK(dalloc(&c->d_covinv, npx), "alloc");
+    CK(dalloc(&c->d_psf, (size_t)psf->nx * psf->ny), "alloc");
+    CK(dalloc(&c->d_mpix, c->mpix.size()), "alloc");
+    CK(cudaMemcpy(c->d_xvals, im->xvals, sizeof(double) * (nx + 1), cudaMemcpyHostToDevice), "h2d");
+    CK(cudaMemcpy(c->d_yvals, im->yvals, sizeof(double) * (ny + 1), cudaMemcpyHostToDevice), "h2d");
+    CK(cudaMemcpy(c->d_data, im->surface_brightness, sizeof(double) * npx, cudaMemcpyHostToDevice), "h2d");
+    CK(cudaMemcpy(c->d_covinv, covinv.data(), sizeof(double) * npx, cudaMemcpyHostToDevice), "h2d");
+    CK(cudaMemcpy(c->d_psf, psf->matrix, sizeof(double) * psf->nx * psf->ny, cudaMemcpyHostToDevice), "h2d");
+    if (!c->mpix.empty())
+        CK(cudaMemcpy(c->d_mpix, c->mpix.data(), sizeof(int) * c->mpix.size(), cudaMemcpyHostToDevice), "h2d");
+
+    StaticData& sd = c->sd;
+    sd.nx = nx; sd.ny = ny;
+    sd.n_mask = (int)c->mpix.size();
+    sd.nsplit = opts->nsplit;
+    sd.nsub = opts->nsplit * opts->nsplit;
+    sd.n_sub = sd.n_mask * sd.nsub;
+    sd.pnx = psf->nx; sd.pny = psf->ny;
+    sd.use_noise_map = noise_map ? 1 : 0;
+    sd.cov_inverse = cov_inverse;
+    sd.xvals = c->d_xvals; sd.yvals = c->d_yvals; sd.data = c->d_data; sd.covinv = c->d_covinv;
+    sd.mpix = c->d_mpix; sd.psf = c->d_psf;
+
+    SrcOpts& so = c->so;
+    so.snx = opts->npixels_x; so.sny = opts->npixels_y;
+    so.auto_grid = opts->auto_sourcegrid;
+    so.xmin = opts->xmin; so.xmax = opts->xmax; so.ymin = opts->ymin; so.ymax = opts->ymax;
+    so.lxmin = opts->limit_xmin; so.lxmax = opts->limit_xmax; so.lymin = opts->limit_ymin; so.lymax = opts->limit_ymax;
+    so.noise_threshold = opts->noise_threshold;
+    so.size_scale = opts->size_scale;
+    so.regularization = opts->regularization;
+    so.regparam = opts->regparam;
+
+    psf_init_attributes();
+    int snx = std::max(so.snx, 2), sny = std::max(so.sny, 2);
+    int r = alloc_work(c, sd.n_mask, sd.nsub, snx * sny, snx, sny);
+    if (r != QLP_OK) return r;
+    return QLP_OK;
+}
+
+void ctx_free(qlp_ctx* c)
+{
+    mixed_free(c);
+    free_work(c->w);
+    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    if (c->h_out) cudaFreeHost(c->h_out);
+    for (int i = 0; i <= QLP_N_STAGES; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+static int build_lens_model(qlp_ctx* c, const double* lens_params, LensModel& lm)
+{
+    if (c->lenses.empty()) { set_error("%s (%d)", "no lens model set", 0); return QLP_ERR_ARG; }
+    memset(&lm, 0, sizeof(lm));
+    lm.nlens = (int)c->lenses.size();
+    lm.n_planes = c->planes.n_planes;
+    for (int i = 0; i < QLP_MAX_PLANES; i++) {
+        lm.zfac[i] = c->planes.zfac[i];
+        for (int j = 0; j < QLP_MAX_PLANES; j++) lm.beta[i][j] = c->planes.beta[i][j];
+    }
+    int off = 0;
+    for (int k = 0; k < lm.nlens; k++) {
+        const qlp_lens& d = c->lenses[k];
+        const double* p = lens_params ? lens_params + off : d.p;
+        int r = make_lens_rec(lm.lens[k], d.type, d.plane, p);
+        if (r != QLP_OK) { set_error("%s (lens %d)", "unsupported lens parameters", k); return r; }
+        off += n_params_of(d.type);
+    }
+    return QLP_OK;
+}
+
+// The launch sequence of one evaluation on stream st; the image set-up in
+// c->sd / c->so decides the mask and source grid.
+static int run_pipeline(qlp_ctx* c, const LensModel& lm, double regparam, cudaStream_t st, bool timed)
+{
+    StaticData& sd = c->sd;
+    SrcOpts& so = c->so;
+    Work& w = c->w;
+    const int Mc = c->M_cap;
+    const int N_max = sd.n_mask;
+    if (timed) cudaEventRecord(c->ev[0], st);
+    launch_raytrace(sd, lm, w, st);
+    if (timed) cudaEventRecord(c->ev[1], st);
+    launch_grid(sd, so, w, st);
+    launch_locate(sd, so, w, st);
+    launch_compact(sd, so, w, st);
+    launch_build_L(sd, so, w, st);
+    if (timed) cudaEventRecord(c->ev[2], st);
+    launch_psf(sd, so, w, Mc, st);
+    launch_dvec(sd, w, N_max, st);
+    if (timed) cudaEventRecord(c->ev[3], st);
+    if (c->precision == QLP_MIXED) {
+        int r = run_inversion_mixed(c, regparam, st);
+        if (r != QLP_OK) return r;
+        if (timed) { cudaEventRecord(c->ev[4], st); cudaEventRecord(c->ev[5], st); }
+    } else {
+        launch_D(w, N_max, Mc, st);
+        launch_syrk_fp64(sd, w, N_max, Mc, st);
+        launch_regularization(so, w, Mc, regparam, st);
+        if (timed) cudaEventRecord(c->ev[4], st);
+        if (so.regularization) {
+            launch_cholesky_fp64(w.R, w.ldF, Mc, w.gs, 1, st);
+            launch_logdet(w.R, w.ldF, Mc, w, 1, st);
+        }
+        launch_cholesky_fp64(w.F, w.ldF, Mc, w.gs, 0, st);
+        launch_logdet(w.F, w.ldF, Mc, w, 0, st);
+        launch_solve_fp64(w, Mc, st);
+        if (timed) cudaEventRecord(c->ev[5], st);
+    }
+    launch_model_chi2(sd, so, w, N_max, Mc, regparam, st);
+    if (timed) cudaEventRecord(c->ev[6], st);
+    return QLP_OK;
+}
+
+static void fill_result(const EvalOut& o, qlp_result* out)
+{
+    memset(out, 0, sizeof(*out));
+    out->chisq0 = o.chisq0;
+    out->logdet_F = o.logdet_F;
+    out->logdet_R = o.logdet_R;
+    out->Es_times_two = o.Es_times_two;
+    out->regterms = o.regterms;
+    out->m2logev = o.m2logev;
+    out->n_active_pixels = o.n_active_pixels;
+    out->n_active_src = o.n_active_src;
+    out->L_nnz = o.L_nnz;
+    out->status = o.status;
+    out->refine_iters = o.refine_iters;
+}
+
+int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result* out)
+{
+    memset(out, 0, sizeof(*out));
+    cudaSetDevice(c->device);
+    if (c->so.snx < 2 || c->so.sny < 2) {
+        out->m2logev = 2e30; out->status = QLP_ERR_GRID_TOO_SMALL;
+        return QLP_ERR_GRID_TOO_SMALL;
+    }
+    LensModel lm;
+    int r = build_lens_model(c, lens_params, lm);
+    if (r != QLP_OK) { out->status = r; return r; }
+    if (regparam <= 0) regparam = c->opts.regparam;
+    long long l0 = kernel_launch_counter();
+    cudaStream_t st = c->stream;
+    CK(cudaMemsetAsync(c->w.out, 0, sizeof(EvalOut), st), "memset");
+    r = run_pipeline(c, lm, regparam, st, true);
+    if (r != QLP_OK) { out->status = r; return r; }
+    CK(cudaMemcpyAsync(c->h_out, c->w.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaGetLastError(), "launch");
+    CK(cudaStreamSynchronize(st), "eval");
+    c->last_launches = kernel_launch_counter() - l0;
+    for (int i = 0; i < QLP_N_STAGES; i++) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
+    fill_result(*c->h_out, out);
+    return out->status;
+}
+
+int ctx_set_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)
+{
+    cudaSetDevice(c->device);
+    std::vector<int> all;
+    c->mask_off.clear(); c->mask_cnt.clear();
+    size_t npx = (size_t)c->nx * c->ny;
+    for (int k = 0; k < n_masks; k++) {
+        std::vector<int> v = masked_list(masks + k * npx, c->nx, c->ny);
+        c->mask_off.push_back((int)all.size());
+        c->mask_cnt.push_back((int)v.size());
+        all.insert(all.end(), v.begin(), v.end());
+    }
+    if (c->d_inst_mpix) { cudaFree(c->d_inst_mpix); c->d_inst_mpix = nullptr; }
+    CK(dalloc(&c->d_inst_mpix, all.size()), "alloc");
+    if (!all.empty())
+        CK(cudaMemcpy(c->d_inst_mpix, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice), "h2d");
+    return QLP_OK;
+}
+
+// Batched evaluation: every instance runs the same device pipeline with its
+// own mask and source grid, back to back on the stream, with one host
+// synchronisation for the whole batch.
+int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, const qlp_instance* inst, int n,
+                   qlp_result* out)
+{
+    cudaSetDevice(c->device);
+    const int np = [&] { int s = 0; for (auto& l : c->lenses) s += n_params_of(l.type); return s; }();
+    // capacity: largest mask and source grid of the batch
+    int nmask_max = (int)c->mpix.size(), cells_max = c->so.snx * c->so.sny, snx_max = c->so.snx, sny_max = c->so.sny;
+    for (int i = 0; i < n && inst; i++) {
+        if (inst[i].mask_id >= (int)c->mask_cnt.size()) { set_error("%s %d", "bad mask id", inst[i].mask_id); return QLP_ERR_ARG; }
+        if (inst[i].mask_id >= 0) nmask_max = std::max(nmask_max, c->mask_cnt[inst[i].mask_id]);
+        if (inst[i].src_npixels_x < 2 || inst[i].src_npixels_y < 2) continue;
+        cells_max = std::max(cells_max, inst[i].src_npixels_x * inst[i].src_npixels_y);
+        snx_max = std::max(snx_max, inst[i].src_npixels_x);
+        sny_max = std::max(sny_max, inst[i].src_npixels_y);
+    }
+    if (nmask_max > c->N_cap || round64(cells_max) > c->M_cap || snx_max > c->so.snx || sny_max > c->so.sny) {
+        int r = alloc_work(c, std::max(nmask_max, c->N_cap), c->sd.nsub, std::max(cells_max, c->M_cap),
+                           std::max(snx_max, c->so.snx), std::max(sny_max, c->so.sny));
+        if (r != QLP_OK) return r;
+        if (c->precision == QLP_MIXED) { mixed_free(c); }
+    }
+    std::vector<EvalOut> res(n > 0 ? n : 1);
+    EvalOut* d_res = nullptr;
+    CK(dalloc(&d_res, n > 0 ? n : 1), "alloc");
+    const StaticData sd0 = c->sd;
+    const SrcOpts so0 = c->so;
+    EvalOut* out0 = c->w.out;
+    cudaStream_t st = c->stream;
+    long long l0 = kernel_launch_counter();
+    int rc = QLP_OK;
+    for (int i = 0; i < n; i++) {
+        LensModel lm;
+        int r = build_lens_model(c, params + (size_t)i * np, lm);
+        double lam = (regparams && regparams[i] > 0) ? regparams[i] : c->opts.regparam;
+        if (inst) {
+            if (inst[i].mask_id >= 0) {
+                c->sd.mpix = c->d_inst_mpix + c->mask_off[inst[i].mask_id];
+                c->sd.n_mask = c->mask_cnt[inst[i].mask_id];
+                c->sd.n_sub = c->sd.n_mask * c->sd.nsub;
+            }
+            if (inst[i].src_npixels_x > 0) { c->so.snx = inst[i].src_npixels_x; c->so.sny = inst[i].src_npixels_y; }
+        }
+        c->w.out = d_res + i;
+        cudaMemsetAsync(c->w.out, 0, sizeof(EvalOut), st);
+        if (r == QLP_OK && (c->so.snx < 2 || c->so.sny < 2)) r = QLP_ERR_GRID_TOO_SMALL;
+        if (r == QLP_OK) r = run_pipeline(c, lm, lam, st, false);
+        res[i].status = r;
+        c->sd = sd0;
+        c->so = so0;
+        if (r != QLP_OK && rc == QLP_OK) rc = r;
+    }
+    c->w.out = out0;
+    std::vector<int> pre(n);
+    for (int i = 0; i < n; i++) pre[i] = res[i].status;
+    cudaError_t e = cudaMemcpyAsync(res.data(), d_res, sizeof(EvalOut) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_res);
+    if (e != cudaSuccess) return cuda_fail(e, "batch");
+    c->last_launches = kernel_launch_counter() - l0;
+    for (int i = 0; i < n; i++) {
+        fill_result(res[i], &out[i]);
+        if (pre[i] != QLP_OK) {
+            out[i].status = pre[i];
+            out[i].m2logev = (pre[i] == QLP_ERR_GRID_TOO_SMALL) ? 2e30 : 0;
+        }
+    }
+    return rc;
+}
+
+int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value, int* active_index,
+             double* D, double* s, double* model)
+{
+    cudaSetDevice(c->device);
+    Work& w = c->w;
+    GridState gs;
+    CK(cudaMemcpy(&gs, w.gs, sizeof(gs), cudaMemcpyDeviceToHost), "d2h");
+    const int nsub = c->sd.n_sub;
+    if (srcpt_xy) {
+        std::vector<double> x(nsub), y(nsub);
+        CK(cudaMemcpy(x.data(), w.spx, sizeof(double) * nsub, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(y.data(), w.spy, sizeof(double) * nsub, cudaMemcpyDeviceToHost), "d2h");
+        for (int t = 0; t < nsub; t++) { srcpt_xy[2 * t] = x[t]; srcpt_xy[2 * t + 1] = y[t]; }
+    }
+    if (L_rowptr) CK(cudaMemcpy(L_rowptr, w.rowptr, sizeof(int) * (gs.N + 1), cudaMemcpyDeviceToHost), "d2h");
+    if (L_index) CK(cudaMemcpy(L_index, w.Lidx, sizeof(int) * gs.nnz, cudaMemcpyDeviceToHost), "d2h");
+    if (L_value) CK(cudaMemcpy(L_value, w.Lval, sizeof(double) * gs.nnz, cudaMemcpyDeviceToHost), "d2h");
+    if (active_index) CK(cudaMemcpy(active_index, w.active_index, sizeof(int) * gs.snx * gs.sny, cudaMemcpyDeviceToHost), "d2h");
+    if (D) CK(cudaMemcpy(D, w.D, sizeof(double) * gs.M, cudaMemcpyDeviceToHost), "d2h");
+    if (s) CK(cudaMemcpy(s, w.s, sizeof(double) * gs.M, cudaMemcpyDeviceToHost), "d2h");
+    if (model) CK(cudaMemcpy(model, w.model, sizeof(double) * gs.N, cudaMemcpyDeviceToHost), "d2h");
+    return QLP_OK;
+}
+
+int ctx_dump_Lpsf(qlp_ctx* c, int rows, double* out)
+{
+    cudaSetDevice(c->device);
+    GridState gs;
+    CK(cudaMemcpy(&gs, c->w.gs, sizeof(gs), cudaMemcpyDeviceToHost), "d2h");
+    if (rows > gs.N) rows = gs.N;
+    if (rows <= 0 || gs.M <= 0) return QLP_OK;
+    CK(cudaMemcpy2D(out, sizeof(double) * gs.M, c->w.Lpsf, sizeof(double) * c->w.ldL, sizeof(double) * gs.M, rows,
+                    cudaMemcpyDeviceToHost), "d2h");
+    return QLP_OK;
+}
+
+}  // namespace qlpix

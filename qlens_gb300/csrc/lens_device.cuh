@@ -1,0 +1,134 @@
+// lens_device.cuh -- FP64 deflection of the lens models on the device.
+// Included by translation units built with --fmad=false.
+#pragma once
+#include "qlpix_internal.h"
+
+namespace qlpix {
+
+// SPLE_Lens::deflection_angular_factor (models.cpp:336-351): the Tessore et
+// al. (2015) series for the core-free elliptical power law, complex products
+// written out as (ac - bd, ad + bc); |z|^2 through hypot like std::norm.
+__device__ __forceinline__ void sple_angular_factor(const LensRec& L, double phi, double& fr, double& fi)
+{
+    double beta = 2.0 / (2 - L.alpha);
+    double ff = (1 - L.q) / (1 + L.q);
+    double s1, c1;
+    sincos(phi, &s1, &c1);
+    fr = 1.0 * c1; fi = 1.0 * s1;
+    double orr = fr, oi = fi;
+    double s2, c2;
+    sincos(2 * phi, &s2, &c2);
+    int i = 1;
+    double nw, nf;
+    do {
+        double rho = ff * (beta * i - 1) / (beta * i + 1);
+        double pr = -(rho * c2), pi = -(rho * s2);
+        double nr = pr * orr - pi * oi;
+        double ni = pr * oi + pi * orr;
+        orr = nr; oi = ni;
+        fr += orr; fi += oi;
+        i++;
+        double a = hypot(orr, oi); nw = a * a;
+        double c = hypot(fr, fi);  nf = c * c;
+    } while (nw > 1e-16 * nf && i < 1000);
+}
+
+__device__ __forceinline__ void sple_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+{
+    if (L.kind == 1) {
+        // SPLE_Lens::deflection_elliptical_iso (models.cpp:208-216)
+        double psi = sqrt(L.qsq * (L.ssq + x * x) + y * y);
+        double u = sqrt(1 - L.qsq);
+        double pre = L.bprime * L.q / u;
+        dx = pre * atan(u * x / (psi + L.sprime));
+        dy = pre * atanh(u * y / (psi + L.qsq * L.sprime));
+    } else if (L.kind == 2) {
+        // SPLE_Lens::deflection_elliptical_nocore (models.cpp:244-262)
+        double R = sqrt(x * x + y * y / L.qsq);
+        double phi = atan(fabs(y / (L.q * x)));
+        if (x < 0) {
+            if (y < 0) phi = phi - M_PI;
+            else phi = M_PI - phi;
+        } else if (y < 0) {
+            phi = -phi;
+        }
+        double fr, fi;
+        sple_angular_factor(L, phi, fr, fi);
+        double scal = 2 * L.bprime * L.q / (1 + L.q) * pow(L.bprime / R, L.alpha - 1);
+        dx = scal * fr;
+        dy = scal * fi;
+    } else {
+        // LensProfile::deflection_spherical_default (profile.cpp:2281-2290)
+        double rsq = x * x + y * y, kapavg;
+        if (L.alpha == 1.0) kapavg = L.b * (sqrt(L.s * L.s + rsq) - L.s) / rsq;
+        else kapavg = (pow(L.b, L.alpha) * (pow(rsq + L.s * L.s, 1 - L.alpha / 2) - pow(L.s, 2 - L.alpha))) / rsq;
+        dx = kapavg * x;
+        dy = kapavg * y;
+    }
+}
+
+}  // namespace qlpix
+#include "nfw_device.cuh"
+namespace qlpix {
+
+// LensProfile::deflection (profile.cpp:1782-1805); Shear::deflection (models.cpp:2266-2272)
+__device__ __forceinline__ void lens_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+{
+    if (L.type == QLP_LENS_SHEAR) {
+        x -= L.xc; y -= L.yc;
+        dx = x * L.shear1 + y * L.shear2;
+        dy = -y * L.shear1 + x * L.shear2;
+        return;
+    }
+    x -= L.xc;
+    y -= L.yc;
+    const bool rot = (L.sintheta != 0);
+    if (rot) {
+        double xp = x * L.costheta + y * L.sintheta;
+        y = -x * L.sintheta + y * L.costheta;
+        x = xp;
+    }
+    double ax, ay;
+    if (L.type == QLP_LENS_SPLE) sple_deflection(L, x, y, ax, ay);
+    else nfw_deflection(L, x, y, ax, ay);
+    if (rot) {
+        double xp = ax * L.costheta - ay * L.sintheta;
+        ay = ax * L.sintheta + ay * L.costheta;
+        ax = xp;
+    }
+    dx = ax; dy = ay;
+}
+
+// QLens::deflection + QLens::find_sourcept (lenscalc.cpp:81-113, 325-330)
+__device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, double y, double& bx, double& by)
+{
+    double defx = 0, defy = 0;
+    double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
+    #pragma unroll 1
+    for (int i = 0; i < lm.n_planes; i++) {
+        dsx[i] = 0; dsy[i] = 0;
+        if (lm.zfac[i] != 0.0) {
+            double xi = x, yi = y;
+            #pragma unroll 1
+            for (int j = 0; j < i; j++) {
+                xi -= lm.beta[i - 1][j] * dsx[j];
+                yi -= lm.beta[i - 1][j] * dsy[j];
+            }
+            #pragma unroll 1
+            for (int k = 0; k < lm.nlens; k++) {
+                if (lm.lens[k].plane != i) continue;
+                double ax, ay;
+                lens_deflection(lm.lens[k], xi, yi, ax, ay);
+                dsx[i] += ax; dsy[i] += ay;
+            }
+            dsx[i] *= lm.zfac[i];
+            dsy[i] *= lm.zfac[i];
+            defx += dsx[i];
+            defy += dsy[i];
+        }
+    }
+    bx = x - defx;
+    by = y - defy;
+}
+
+}  // namespace qlpix

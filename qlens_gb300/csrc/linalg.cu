@@ -1,0 +1,537 @@
+// linalg.cu -- FP64 dense algebra of the inversion:
+//   D = L'^T C^-1 d, F = L'^T C^-1 L' (SYRK), curvature R and F += lambda R,
+//   blocked Cholesky of F and R, log det, the two triangular solves, the
+//   model image, chi^2, s^T R s and the final -2 log(evidence).
+// Reference: QLens::create_lensing_matrices_from_Lmatrix_dense
+// (pixelgrid.cpp:15590-15736), add_regularization_term_to_dense_Fmatrix
+// (15781-15819), invert_lens_mapping_dense (17346-17396), Cholesky_dcmp_packed
+// (17071-17105), Cholesky_solve_lower_packed (17230-17246),
+// Cholesky_logdet_lower_packed (17201-17210), Rmatrix_determinant_dense
+// (18176-18191), calculate_image_pixel_surface_brightness_dense (18268-18290),
+// calculate_regularization_prior_term (15821-15863), chi^2 and evidence
+// assembly (lens.cpp:12950-13016, 12608-12615).
+//
+// Matrices are dense row-major with leading dimension ldF; the lower triangle
+// holds F (and later its Cholesky factor).  Sizes past the active count M are
+// padded to a multiple of 64 with an identity block, which leaves log det and
+// the solution unchanged.  Every kernel reads N and M from the device-side
+// GridState, so the launch sequence never waits for the host.
+#include "qlpix_internal.h"
+
+namespace qlpix {
+
+#define NB 64
+
+__device__ __forceinline__ int mpad64(int M) { return (M + 63) & ~63; }
+
+// ---- data and inverse-variance per active row ----
+__global__ void k_dvec(StaticData sd, const GridState* __restrict__ gs, const int* __restrict__ rowpix,
+                       double* __restrict__ dvec, double* __restrict__ cvec)
+{
+    const int N = gs->N;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        int pix = rowpix[r];
+        dvec[r] = sd.data[pix];
+        cvec[r] = sd.use_noise_map ? sd.covinv[pix] : sd.cov_inverse;
+    }
+}
+
+void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st)
+{
+    if (N_max == 0) return;
+    k_dvec<<<(N_max + 255) / 256, 256, 0, st>>>(sd, w.gs, w.rowpix, w.dvec, w.cvec);
+    count_launches(1);
+}
+
+// ---- D = L'^T (C^-1 d): column sums over row chunks, then a fixed-order sum ----
+#define D_CHUNK 256
+__global__ void k_D_partial(const GridState* __restrict__ gs, const double* __restrict__ L, int ldL,
+                            const double* __restrict__ dvec, const double* __restrict__ cvec,
+                            double* __restrict__ part, int M_max)
+{
+    const int N = gs->N, M = gs->M;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r0 = blockIdx.y * D_CHUNK;
+    if (col >= M || r0 >= N) return;
+    const int r1 = min(r0 + D_CHUNK, N);
+    double acc = 0;
+    for (int r = r0; r < r1; r++) acc += L[(size_t)r * ldL + col] * dvec[r] * cvec[r];
+    part[(size_t)blockIdx.y * M_max + col] = acc;
+}
+
+__global__ void k_D_final(const GridState* __restrict__ gs, const double* __restrict__ part, double* __restrict__ D,
+                          int M_max)
+{
+    const int N = gs->N, M = gs->M;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= mpad64(M)) return;
+    double acc = 0;
+    if (col < M) {
+        const int nch = (N + D_CHUNK - 1) / D_CHUNK;
+        for (int c = 0; c < nch; c++) acc += part[(size_t)c * M_max + col];
+    }
+    D[col] = acc;
+}
+
+void launch_D(Work& w, int N_max, int M_max, cudaStream_t st)
+{
+    dim3 g((M_max + 127) / 128, (N_max + D_CHUNK - 1) / D_CHUNK);
+    k_D_partial<<<g, 128, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.dvec, w.cvec, w.partial, M_max);
+    k_D_final<<<(w.ldF + 127) / 128, 128, 0, st>>>(w.gs, w.partial, w.D, M_max);
+    count_launches(2);
+}
+
+// ---- F = L'^T C^-1 L', lower 64x64 tiles, FP64 ----
+__device__ __forceinline__ void tri_index(int t, int& bi, int& bj)
+{
+    int i = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= t) i++;
+    while (i * (i + 1) / 2 > t) i--;
+    bi = i;
+    bj = t - i * (i + 1) / 2;
+}
+
+__global__ void __launch_bounds__(256) k_syrk64(const GridState* __restrict__ gs, const double* __restrict__ L,
+                                                int ldL, const double* __restrict__ cvec, int use_noise_map,
+                                                double cov_inverse, double* __restrict__ F, int ldF)
+{
+    __shared__ double As[16][NB + 1];
+    __shared__ double Bs[16][NB + 1];
+    int bi, bj;
+    tri_index(blockIdx.x, bi, bj);
+    const int N = gs->N, Mp = mpad64(gs->M);
+    if (bi * NB >= Mp) return;
+    const int a0 = bi * NB, b0 = bj * NB;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = 0;
+    for (int p0 = 0; p0 < N; p0 += 16) {
+        #pragma unroll
+        for (int e = 0; e < 4; e++) {
+            int idx = threadIdx.x + e * 256;   // 0..1023 over 16 x 64
+            int kk = idx >> 6, x = idx & 63;
+            int p = p0 + kk;
+            double va = 0, vb = 0;
+            if (p < N) {
+                va = L[(size_t)p * ldL + a0 + x];
+                vb = L[(size_t)p * ldL + b0 + x];
+                if (use_noise_map) vb *= cvec[p];
+            }
+            As[kk][x] = va;
+            Bs[kk][x] = vb;
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int kk = 0; kk < 16; kk++) {
+            double ra[4], rb[4];
+            #pragma unroll
+            for (int u = 0; u < 4; u++) ra[u] = As[kk][ty * 4 + u];
+            #pragma unroll
+            for (int v = 0; v < 4; v++) rb[v] = Bs[kk][tx * 4 + v];
+            #pragma unroll
+            for (int u = 0; u < 4; u++)
+                #pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] += ra[u] * rb[v];
+        }
+        __syncthreads();
+    }
+    const double scale = use_noise_map ? 1.0 : cov_inverse;
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) F[(size_t)(a0 + ty * 4 + u) * ldF + b0 + tx * 4 + v] = acc[u][v] * scale;
+}
+
+void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st)
+{
+    (void)N_max;
+    int nb = (M_max + NB - 1) / NB;
+    int tiles = nb * (nb + 1) / 2;
+    k_syrk64<<<tiles, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.cvec, sd.use_noise_map, sd.cov_inverse, w.F, w.ldF);
+    count_launches(1);
+}
+
+// ---- curvature R (dense lower) and F += lambda R ----
+// R = Hx^T Hx + Hy^T Hy with Hx rows (-2 at a, +1 at active x-neighbours) and
+// Hy likewise (SourcePixel::generate_hmatrices, pixelgrid.cpp:2968-3071;
+// generate_Rmatrix_from_hmatrices 3073-3240).  In closed form per active cell:
+// diagonal 8 + #active 4-neighbours, -4 for an active +-1 neighbour, +1 for an
+// active +-2 neighbour whose middle cell is active.
+__device__ __forceinline__ int act_at(const int* ai, int snx, int sny, int i, int j)
+{
+    if (i < 0 || j < 0 || i >= snx || j >= sny) return -1;
+    return ai[j * snx + i];
+}
+
+__global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ ai, int snx, int sny,
+                      double regparam, double* __restrict__ F, double* __restrict__ R, int ldF, int do_reg)
+{
+    const int M = gs->M, Mp = mpad64(M);
+    const int ncell = snx * sny;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
+        if (c >= ncell) {   // identity padding
+            int i = M + (c - ncell);
+            F[(size_t)i * ldF + i] = 1.0;
+            if (do_reg) R[(size_t)i * ldF + i] = 1.0;
+            continue;
+        }
+        if (!do_reg) continue;
+        const int a = ai[c];
+        if (a < 0) continue;
+        const int ci = c % snx, cj = c / snx;
+        int nb1[4] = {act_at(ai, snx, sny, ci + 1, cj), act_at(ai, snx, sny, ci - 1, cj),
+                      act_at(ai, snx, sny, ci, cj + 1), act_at(ai, snx, sny, ci, cj - 1)};
+        int nb2[4] = {act_at(ai, snx, sny, ci + 2, cj), act_at(ai, snx, sny, ci - 2, cj),
+                      act_at(ai, snx, sny, ci, cj + 2), act_at(ai, snx, sny, ci, cj - 2)};
+        double diag = 8.0;
+        for (int k = 0; k < 4; k++) if (nb1[k] >= 0) diag += 1.0;
+        R[(size_t)a * ldF + a] = diag;
+        F[(size_t)a * ldF + a] += regparam * diag;
+        for (int k = 0; k < 4; k++) {
+            int b = nb1[k];
+            if (b >= 0 && b < a) { R[(size_t)a * ldF + b] = -4.0; F[(size_t)a * ldF + b] += regparam * -4.0; }
+            int b2 = nb2[k];
+            if (b2 >= 0 && nb1[k] >= 0 && b2 < a) { R[(size_t)a * ldF + b2] = 1.0; F[(size_t)a * ldF + b2] += regparam * 1.0; }
+        }
+    }
+}
+
+void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regparam, cudaStream_t st)
+{
+    const int ncell = so.snx * so.sny;
+    if (so.regularization) cudaMemsetAsync(w.R, 0, sizeof(double) * (size_t)w.ldF * w.ldF, st);
+    int total = ncell + 64;
+    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regparam, w.F, w.R, w.ldF,
+                                               so.regularization);
+    count_launches(1);
+    (void)M_max;
+}
+
+// ---- blocked Cholesky (lower), nb = 64 ----
+__global__ void __launch_bounds__(256) k_potrf(double* __restrict__ A, int ld, int k, GridState* gs, int which)
+{
+    __shared__ double S[NB][NB + 1];
+    const int nblk = mpad64(gs->M) / NB;
+    if (k >= nblk) return;
+    const int o = k * NB;
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        S[r][c] = (c <= r) ? A[(size_t)(o + r) * ld + o + c] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < NB; j++) {
+        if (threadIdx.x == 0) {
+            double d = S[j][j];
+            if (d < 0) {
+                // Cholesky_dcmp_packed continues with sqrt(|d|) and flags the matrix (pixelgrid.cpp:17094-17099)
+                int* flag = which ? &gs->not_spd_R : &gs->not_spd_F;
+                if (*flag == 0) *flag = o + j + 1;
+            }
+            S[j][j] = sqrt(fabs(d));
+        }
+        __syncthreads();
+        const double djj = S[j][j];
+        for (int i = j + 1 + threadIdx.x; i < NB; i += blockDim.x) S[i][j] /= djj;
+        __syncthreads();
+        const int rem = NB - j - 1;
+        for (int idx = threadIdx.x; idx < rem * rem; idx += blockDim.x) {
+            int i = j + 1 + idx / rem, c = j + 1 + idx % rem;
+            if (c <= i) S[i][c] -= S[i][j] * S[c][j];
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        if (c <= r) A[(size_t)(o + r) * ld + o + c] = S[r][c];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_trsm(double* __restrict__ A, int ld, int k, const GridState* __restrict__ gs)
+{
+    __shared__ double Lk[NB][NB + 1];
+    __shared__ double X[NB][NB + 1];
+    const int nblk = mpad64(gs->M) / NB;
+    const int i = k + 1 + blockIdx.x;
+    if (i >= nblk) return;
+    const int o = k * NB, ro = i * NB;
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        Lk[r][c] = (c <= r) ? A[(size_t)(o + r) * ld + o + c] : 0.0;
+        X[r][c] = A[(size_t)(ro + r) * ld + o + c];
+    }
+    __syncthreads();
+    // X Lk^T = A_ik, column by column
+    for (int c = 0; c < NB; c++) {
+        const double dcc = Lk[c][c];
+        for (int r = threadIdx.x; r < NB; r += blockDim.x) X[r][c] /= dcc;
+        __syncthreads();
+        const int rem = NB - c - 1;
+        for (int idx = threadIdx.x; idx < NB * rem; idx += blockDim.x) {
+            int r = idx / rem, c2 = c + 1 + idx % rem;
+            X[r][c2] -= X[r][c] * Lk[c2][c];
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        A[(size_t)(ro + r) * ld + o + c] = X[r][c];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_chol_update(double* __restrict__ A, int ld, int k,
+                                                     const GridState* __restrict__ gs)
+{
+    __shared__ double Li[NB][NB + 1];
+    __shared__ double Lj[NB][NB + 1];
+    const int nblk = mpad64(gs->M) / NB;
+    int ti, tj;
+    tri_index(blockIdx.x, ti, tj);
+    const int i = k + 1 + ti, j = k + 1 + tj;
+    if (i >= nblk) return;
+    const int o = k * NB;
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        Li[r][c] = A[(size_t)(i * NB + r) * ld + o + c];
+        Lj[r][c] = A[(size_t)(j * NB + r) * ld + o + c];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = 0;
+    #pragma unroll 8
+    for (int kk = 0; kk < NB; kk++) {
+        double ra[4], rb[4];
+        #pragma unroll
+        for (int u = 0; u < 4; u++) ra[u] = Li[ty * 4 + u][kk];
+        #pragma unroll
+        for (int v = 0; v < 4; v++) rb[v] = Lj[tx * 4 + v][kk];
+        #pragma unroll
+        for (int u = 0; u < 4; u++)
+            #pragma unroll
+            for (int v = 0; v < 4; v++) acc[u][v] += ra[u] * rb[v];
+    }
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) {
+            size_t off = (size_t)(i * NB + ty * 4 + u) * ld + j * NB + tx * 4 + v;
+            A[off] -= acc[u][v];
+        }
+}
+
+int launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, cudaStream_t st)
+{
+    const int nbm = (M_max + NB - 1) / NB;
+    int n = 0;
+    for (int k = 0; k < nbm; k++) {
+        k_potrf<<<1, 256, 0, st>>>(A, ld, k, const_cast<GridState*>(gs), which);
+        n++;
+        const int rem = nbm - k - 1;
+        if (rem > 0) {
+            k_trsm<<<rem, 256, 0, st>>>(A, ld, k, gs);
+            k_chol_update<<<rem * (rem + 1) / 2, 256, 0, st>>>(A, ld, k, gs);
+            n += 2;
+        }
+    }
+    count_launches(n);
+    return n;
+}
+
+// ---- log det = 2 sum log L_ii over the active part ----
+__global__ void __launch_bounds__(1024) k_logdet(const double* __restrict__ A, int ld, const GridState* __restrict__ gs,
+                                                 EvalOut* out, int which)
+{
+    __shared__ double red[32];
+    const int M = gs->M;
+    double acc = 0;
+    // fixed per-thread strided order, then a fixed tree: deterministic
+    for (int i = threadIdx.x; i < M; i += blockDim.x) acc += log(fabs(A[(size_t)i * ld + i]));
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += red[k];
+        if (which) out->logdet_R = 2 * t;
+        else out->logdet_F = 2 * t;
+    }
+}
+
+void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st)
+{
+    (void)M_max;
+    k_logdet<<<1, 1024, 0, st>>>(A, ld, w.gs, w.out, which);
+    count_launches(1);
+}
+
+// ---- F s = D with the Cholesky factor: blocked forward and backward substitution ----
+__global__ void __launch_bounds__(1024) k_solve(const double* __restrict__ A, int ld, const GridState* __restrict__ gs,
+                                                const double* __restrict__ D, double* __restrict__ s, double* y)
+{
+    __shared__ double part[16][NB + 1];
+    const int Mp = mpad64(gs->M);
+    const int nblk = Mp / NB;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < Mp; i += blockDim.x) y[i] = D[i];
+    __syncthreads();
+    // forward: L y = D
+    for (int kb = 0; kb < nblk; kb++) {
+        const int o = kb * NB;
+        {   // y[o+r] -= L[o+r, 0:o] . y[0:o]; 16 threads per row
+            const int r = tid >> 4, t = tid & 15;
+            double acc = 0;
+            for (int c = t; c < o; c += 16) acc += A[(size_t)(o + r) * ld + c] * y[c];
+            for (int off = 8; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+            __syncthreads();
+            if (t == 0) y[o + r] -= acc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            for (int c = 0; c < NB; c++) {
+                if (lane == 0) y[o + c] /= A[(size_t)(o + c) * ld + o + c];
+                __syncwarp();
+                const double yc = y[o + c];
+                for (int r = c + 1 + lane; r < NB; r += 32) y[o + r] -= A[(size_t)(o + r) * ld + o + c] * yc;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+    }
+    // backward: L^T s = y
+    for (int i = tid; i < Mp; i += blockDim.x) s[i] = 0;
+    __syncthreads();
+    for (int kb = nblk - 1; kb >= 0; kb--) {
+        const int o = kb * NB, e = o + NB;
+        {   // part[t][c] = sum_{r >= e, r = e + t (mod 16)} L[r][o+c] s[r]
+            const int c = tid & 63, t = tid >> 6;
+            double acc = 0;
+            for (int r = e + t; r < Mp; r += 16) acc += A[(size_t)r * ld + o + c] * s[r];
+            part[t][c] = acc;
+        }
+        __syncthreads();
+        if (tid < NB) {
+            double acc = 0;
+            for (int t = 0; t < 16; t++) acc += part[t][tid];
+            y[o + tid] -= acc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            for (int c = NB - 1; c >= 0; c--) {
+                if (lane == 0) s[o + c] = y[o + c] / A[(size_t)(o + c) * ld + o + c];
+                __syncwarp();
+                const double sc = s[o + c];
+                for (int r = lane; r < c; r += 32) y[o + r] -= A[(size_t)(o + c) * ld + o + r] * sc;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+    }
+}
+
+void launch_solve_fp64(Work& w, int M_max, cudaStream_t st)
+{
+    (void)M_max;
+    k_solve<<<1, 1024, 0, st>>>(w.F, w.ldF, w.gs, w.D, w.s, w.tmp);
+    count_launches(1);
+}
+
+// ---- model image, chi^2, s^T R s and the evidence ----
+__global__ void __launch_bounds__(256) k_model(const GridState* __restrict__ gs, const double* __restrict__ L,
+                                               int ldL, const double* __restrict__ s, double* __restrict__ model)
+{
+    const int N = gs->N, M = gs->M;
+    const int lane = threadIdx.x & 31;
+    for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < N; r += gridDim.x * (blockDim.x >> 5)) {
+        const double* row = L + (size_t)r * ldL;
+        double acc = 0;
+        for (int c = lane; c < M; c += 32) acc += row[c] * s[c];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) model[r] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_final(StaticData sd, SrcOpts so, const GridState* __restrict__ gs,
+                                                const int* __restrict__ rowidx, const double* __restrict__ model,
+                                                const double* __restrict__ s, const int* __restrict__ ai,
+                                                double regparam, EvalOut* out)
+{
+    __shared__ double red[2][32];
+    const int M = gs->M;
+    double chi = 0, es = 0;
+    for (int m = threadIdx.x; m < sd.n_mask; m += blockDim.x) {
+        const int pix = sd.mpix[m];
+        const double c = sd.use_noise_map ? sd.covinv[pix] : sd.cov_inverse;
+        const int r = rowidx[m];
+        double dd = (r >= 0) ? model[r] - sd.data[pix] : sd.data[pix];
+        chi += dd * dd * c;
+    }
+    if (so.regularization && regparam != 0) {
+        const int snx = so.snx, sny = so.sny;
+        for (int cidx = threadIdx.x; cidx < snx * sny; cidx += blockDim.x) {
+            const int a = ai[cidx];
+            if (a < 0) continue;
+            const int ci = cidx % snx, cj = cidx / snx;
+            int nb1[4] = {act_at(ai, snx, sny, ci + 1, cj), act_at(ai, snx, sny, ci - 1, cj),
+                          act_at(ai, snx, sny, ci, cj + 1), act_at(ai, snx, sny, ci, cj - 1)};
+            int nb2[4] = {act_at(ai, snx, sny, ci + 2, cj), act_at(ai, snx, sny, ci - 2, cj),
+                          act_at(ai, snx, sny, ci, cj + 2), act_at(ai, snx, sny, ci, cj - 2)};
+            double diag = 8.0, rs = 0;
+            for (int k = 0; k < 4; k++) {
+                if (nb1[k] >= 0) { diag += 1.0; rs += -4.0 * s[nb1[k]]; }
+                if (nb2[k] >= 0 && nb1[k] >= 0) rs += s[nb2[k]];
+            }
+            rs += diag * s[a];
+            es += s[a] * rs;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        chi += __shfl_xor_sync(0xffffffffu, chi, o);
+        es += __shfl_xor_sync(0xffffffffu, es, o);
+    }
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = chi; red[1][threadIdx.x >> 5] = es; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double c2 = 0, e2 = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { c2 += red[0][k]; e2 += red[1][k]; }
+        double regterms = 0, loglike = 0;
+        if (so.regularization && M > 0) {
+            if (regparam != 0) {
+                regterms = regparam * e2 - M * log(regparam) - out->logdet_R;
+                loglike += regterms;
+            }
+            loglike += out->logdet_F;
+        }
+        loglike += c2;
+        int status = gs->status;
+        if (status == 0 && (gs->not_spd_F || gs->not_spd_R)) status = QLP_ERR_NOT_SPD;
+        out->chisq0 = c2;
+        out->Es_times_two = e2;
+        out->regterms = regterms;
+        out->m2logev = (status == QLP_ERR_NO_SOURCE_PIXELS) ? 2e30 : loglike;
+        out->n_active_pixels = gs->N;
+        out->n_active_src = M;
+        out->L_nnz = gs->nnz;
+        out->status = status;
+    }
+}
+
+void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max, double regparam,
+                       cudaStream_t st)
+{
+    (void)M_max;
+    if (N_max > 0) {
+        int blocks = (N_max + 7) / 8;
+        if (blocks > 152 * 16) blocks = 152 * 16;
+        k_model<<<blocks, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.s, w.model);
+    }
+    k_final<<<1, 1024, 0, st>>>(sd, so, w.gs, w.rowidx, w.model, w.s, w.active_index, regparam, w.out);
+    count_launches(2);
+}
+
+}  // namespace qlpix

@@ -1,0 +1,249 @@
+// qlpix_api.cpp -- host runtime and C ABI of libqlpix (see include/qlpix.h).
+//
+// The host side keeps QLens's set-up semantics: the image pixel grid and mask
+// of ImagePixelData/ImagePixelGrid (pixelgrid.cpp:9622-9700, 9940-10099), the
+// lens meta-parameters of update_meta_parameters (profile.cpp:1625-1689,
+// models.cpp:101-108, 2212-2224) evaluated with the host libm exactly as the
+// reference evaluates them, and the sentinel returns of
+// QLens::invert_image_surface_brightness_map (lens.cpp:12293-13195).
+// Everything per evaluation runs on one CUDA stream with no host round trip
+// until the final scalars are copied back.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <atomic>
+#include <algorithm>
+#include "qlpix_internal.h"
+#include "qlpix_ctx.h"
+
+namespace qlpix {
+
+static std::atomic<long long> g_launches{0};
+void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long kernel_launch_counter() { return g_launches.load(); }
+
+static thread_local std::string t_err;
+void set_error(const char* fmt, const char* a, int code)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), fmt, a, code);
+    t_err = buf;
+}
+
+static const double QL_HALFPI = 1.57079632679;                 // mathexpr.h:10
+static double deg2rad(double t) { return 0.017453292519943295 * t; }  // mathexpr.h:27
+
+int n_params_of(int type)
+{
+    switch (type) {
+        case QLP_LENS_SPLE: return 7;
+        case QLP_LENS_SHEAR: return 4;
+        case QLP_LENS_NFW: return 6;
+    }
+    return 0;
+}
+
+// LensProfile::set_angle with orient_major_axis_north (profile.cpp:1625-1637)
+static void set_angle(LensRec& L, double theta_deg)
+{
+    double theta = deg2rad(theta_deg);
+    double c = cos(theta), s = sin(theta);
+    L.sintheta = c;
+    L.costheta = -s;
+}
+
+int make_lens_rec(LensRec& L, int type, int plane, const double* p)
+{
+    memset(&L, 0, sizeof(L));
+    L.type = type;
+    L.plane = plane;
+    if (type == QLP_LENS_SPLE) {
+        L.b = p[0]; L.alpha = p[1]; L.s = p[2]; L.q = p[3];
+        if (L.s < 0) L.s = -L.s;
+        if (!(L.q > 0) || L.q > 1) return QLP_ERR_ARG;
+        set_angle(L, p[4]);
+        L.xc = p[5]; L.yc = p[6];
+        double f = 1.0 / sqrt(L.q);         // emode 1 (profile.cpp:1686-1689)
+        L.bprime = L.b * f;
+        L.sprime = L.s * f;
+        L.qsq = L.q * L.q;
+        L.ssq = L.sprime * L.sprime;
+        if (L.q == 1.0) L.kind = 0;
+        else if (L.alpha == 1.0) L.kind = 1;
+        else if (L.s == 0.0) L.kind = 2;
+        else return QLP_ERR_ARG;           // cored power law, q<1: quadrature, not supported here
+    } else if (type == QLP_LENS_SHEAR) {
+        double theta_eff = deg2rad(p[1]) + QL_HALFPI;
+        L.shear1 = p[0] * cos(2 * theta_eff);
+        L.shear2 = p[0] * sin(2 * theta_eff);
+        L.xc = p[2]; L.yc = p[3];
+    } else if (type == QLP_LENS_NFW) {
+        L.ks = p[0]; L.rs = p[1]; L.q = p[2];
+        if (!(L.q > 0) || L.q > 1 || !(L.rs > 0)) return QLP_ERR_ARG;
+        set_angle(L, p[3]);
+        L.xc = p[4]; L.yc = p[5];
+        L.f_major_axis = 1.0 / sqrt(L.q);
+        L.qsq = L.q * L.q;
+        L.epsilon = 1 - L.qsq;
+    } else {
+        return QLP_ERR_ARG;
+    }
+    return QLP_OK;
+}
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t n)
+{
+    return cudaMalloc((void**)p, sizeof(T) * (n > 0 ? n : 1));
+}
+
+}  // namespace qlpix
+
+using namespace qlpix;
+
+static int fail(int code, const char* msg)
+{
+    t_err = msg;
+    return code;
+}
+
+extern "C" {
+
+void qlp_srcgrid_defaults(qlp_srcgrid_opts* o)
+{
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->nsplit = 2;                      // default_imgpixel_nsplit (lens.cpp:497)
+    o->npixels_x = o->npixels_y = 20;
+    o->auto_sourcegrid = 1;             // lens.cpp:390
+    o->xmin = -1; o->xmax = 1; o->ymin = -1; o->ymax = 1;   // lens.cpp:377
+    o->limit_xmin = -1e30; o->limit_xmax = 1e30; o->limit_ymin = -1e30; o->limit_ymax = 1e30;
+    o->noise_threshold = 0;             // lens.cpp:433
+    o->size_scale = 0;                  // pixelgrid.cpp:561
+    o->regularization = 1;              // curvature (lens.cpp:403)
+    o->regparam = 100;                  // pixelgrid.cpp:558
+}
+
+const char* qlp_last_error(void) { return t_err.c_str(); }
+
+long long qlp_last_launch_count(const qlp_ctx* ctx) { return ctx ? ctx->last_launches : 0; }
+
+qlp_ctx* qlp_create(const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts* opts, int device, int* status)
+{
+    int st_dummy;
+    if (!status) status = &st_dummy;
+    *status = QLP_OK;
+    if (!im || !im->xvals || !im->yvals || !im->surface_brightness || !im->in_mask) {
+        *status = fail(QLP_ERR_NO_DATA, "no image data");
+        return nullptr;
+    }
+    if (!psf || !psf->matrix || psf->nx < 1 || psf->ny < 1 || !opts || opts->nsplit < 1 ||
+        im->npixels_x < 1 || im->npixels_y < 1) {
+        *status = fail(QLP_ERR_ARG, "bad image/psf/options");
+        return nullptr;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+        *status = fail(QLP_ERR_NO_DEVICE, "no CUDA device available");
+        return nullptr;
+    }
+    qlp_ctx* c = new qlp_ctx();
+    c->device = device;
+    cudaSetDevice(device);
+    int code = ctx_init(c, im, psf, opts);
+    if (code != QLP_OK) {
+        ctx_free(c);
+        delete c;
+        *status = code;
+        return nullptr;
+    }
+    return c;
+}
+
+int qlp_set_lens_model(qlp_ctx* c, const qlp_lens* lenses, int nlens, const qlp_planes* planes)
+{
+    if (!c || !lenses || nlens <= 0 || nlens > QLP_MAX_LENSES) return fail(QLP_ERR_ARG, "bad lens model");
+    c->lenses.assign(lenses, lenses + nlens);
+    memset(&c->planes, 0, sizeof(c->planes));
+    if (planes) c->planes = *planes;
+    else { c->planes.n_planes = 1; c->planes.zfac[0] = 1.0; }
+    if (c->planes.n_planes < 1 || c->planes.n_planes > QLP_MAX_PLANES) return fail(QLP_ERR_ARG, "bad planes");
+    for (int k = 0; k < nlens; k++)
+        if (lenses[k].plane < 0 || lenses[k].plane >= c->planes.n_planes || n_params_of(lenses[k].type) == 0)
+            return fail(QLP_ERR_ARG, "bad lens type or plane");
+    return QLP_OK;
+}
+
+int qlp_n_params(const qlp_ctx* c)
+{
+    if (!c) return 0;
+    int n = 0;
+    for (auto& l : c->lenses) n += n_params_of(l.type);
+    return n;
+}
+
+int qlp_set_precision(qlp_ctx* c, int mode)
+{
+    if (!c || (mode != QLP_FP64 && mode != QLP_MIXED)) return fail(QLP_ERR_ARG, "bad precision mode");
+    c->precision = mode;
+    return QLP_OK;
+}
+
+int qlp_set_stream(qlp_ctx* c, void* stream)
+{
+    if (!c) return fail(QLP_ERR_ARG, "null context");
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return QLP_OK;
+}
+
+int qlp_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result* out)
+{
+    if (!c || !out) return fail(QLP_ERR_ARG, "null argument");
+    return ctx_eval(c, lens_params, regparam, out);
+}
+
+int qlp_set_instance_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)
+{
+    if (!c || (n_masks > 0 && !masks) || n_masks < 0) return fail(QLP_ERR_ARG, "bad masks");
+    return ctx_set_masks(c, masks, n_masks);
+}
+
+int qlp_eval_batch(qlp_ctx* c, const double* params, const double* regparams, const qlp_instance* inst, int n,
+                   qlp_result* out)
+{
+    if (!c || !out || n < 0 || (n > 0 && !params)) return fail(QLP_ERR_ARG, "bad batch arguments");
+    return ctx_eval_batch(c, params, regparams, inst, n, out);
+}
+
+int qlp_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value, int* active_index,
+             double* D, double* s, double* model)
+{
+    if (!c) return fail(QLP_ERR_ARG, "null context");
+    return ctx_dump(c, srcpt_xy, L_rowptr, L_index, L_value, active_index, D, s, model);
+}
+
+int qlp_dump_Lpsf(qlp_ctx* c, int rows, double* out)
+{
+    if (!c || !out || rows < 0) return fail(QLP_ERR_ARG, "bad arguments");
+    return ctx_dump_Lpsf(c, rows, out);
+}
+
+int qlp_stage_times(qlp_ctx* c, float* ms, int n)
+{
+    if (!c || !ms || n < QLP_N_STAGES) return fail(QLP_ERR_ARG, "bad arguments");
+    for (int i = 0; i < QLP_N_STAGES; i++) ms[i] = c->stage_ms[i];
+    return QLP_OK;
+}
+
+void qlp_destroy(qlp_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    ctx_free(c);
+    delete c;
+}
+
+}  // extern "C"

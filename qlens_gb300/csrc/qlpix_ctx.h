@@ -1,0 +1,64 @@
+// qlpix_ctx.h -- the context object behind qlp_ctx* (host runtime).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "qlpix_internal.h"
+
+#define QLP_N_STAGES 6
+
+struct qlp_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int precision = QLP_FP64;
+
+    // lens model
+    std::vector<qlp_lens> lenses;
+    qlp_planes planes{};
+
+    // host copies of the static inputs
+    int nx = 0, ny = 0;
+    std::vector<int> mpix;                // masked pixels of the image mask (j-outer, i-inner)
+    qlp_srcgrid_opts opts{};
+
+    // device copies
+    double* d_xvals = nullptr;
+    double* d_yvals = nullptr;
+    double* d_data = nullptr;
+    double* d_covinv = nullptr;
+    double* d_psf = nullptr;
+    int* d_mpix = nullptr;
+
+    // extra masks for batched evaluation (device mpix lists, concatenated)
+    std::vector<int> mask_off, mask_cnt;
+    int* d_inst_mpix = nullptr;
+    int max_inst_src = 0;                 // largest source grid requested by a batch (cells)
+
+    qlpix::StaticData sd{};
+    qlpix::SrcOpts so{};
+    qlpix::Work w{};
+    int M_cap = 0;                        // workspace capacity in source cells (multiple of 64)
+    int N_cap = 0;                        // workspace capacity in masked pixels
+    int nsub_cap = 0;
+
+    qlpix::EvalOut* h_out = nullptr;      // pinned
+    cudaEvent_t ev[QLP_N_STAGES + 1] = {};
+    float stage_ms[QLP_N_STAGES] = {};
+    long long last_launches = 0;
+};
+
+namespace qlpix {
+int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts* opts);
+void ctx_free(qlp_ctx* c);
+int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result* out);
+int ctx_set_masks(qlp_ctx* c, const unsigned char* masks, int n_masks);
+int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, const qlp_instance* inst, int n,
+                   qlp_result* out);
+int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value, int* active_index,
+             double* D, double* s, double* model);
+int ctx_dump_Lpsf(qlp_ctx* c, int rows, double* out);
+int make_lens_rec(LensRec& L, int type, int plane, const double* p);
+int n_params_of(int type);
+void set_error(const char* fmt, const char* a, int code);
+}  // namespace qlpix

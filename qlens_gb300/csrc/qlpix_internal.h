@@ -1,0 +1,126 @@
+// qlpix_internal.h -- device-side data structures shared by the kernels and
+// the host runtime of libqlpix.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/qlpix.h"
+
+namespace qlpix {
+
+// One lens, reduced to the constants its deflection needs.  Filled on the
+// host with the same libm calls QLens makes in update_meta_parameters
+// (models.cpp:101-108, 2212-2224; profile.cpp:1625-1689).
+struct LensRec {
+    int type;        // QLP_LENS_*
+    int plane;       // lens-redshift plane
+    int kind;        // SPLE: 0 spherical, 1 elliptical alpha=1, 2 elliptical core-free
+    int nfw_mode;    // NFW: 0 quadrature, 1 surrogate
+    double xc, yc, costheta, sintheta;
+    double q, qsq, b, bprime, s, sprime, ssq, alpha;
+    double shear1, shear2;
+    double ks, rs, f_major_axis, epsilon;   // NFW
+};
+
+struct LensModel {
+    int nlens;
+    int n_planes;
+    double zfac[QLP_MAX_PLANES];
+    double beta[QLP_MAX_PLANES][QLP_MAX_PLANES];
+    LensRec lens[QLP_MAX_LENSES];
+};
+
+// Source-grid state computed on the device each evaluation.
+struct GridState {
+    double xmin, xmax, ymin, ymax;    // bounds after auto-sizing
+    int snx, sny;                     // cells
+    int M;                            // active source cells
+    int N;                            // active image pixels
+    int nnz;                          // pre-PSF L nonzeros
+    int status;                       // QLP_* status raised on the device
+    int not_spd_F, not_spd_R;         // first failing pivot + 1 (0 = fine)
+};
+
+// Scalars of one evaluation, written by the final assembly kernel.
+struct EvalOut {
+    double chisq0, logdet_F, logdet_R, Es_times_two, regterms, m2logev;
+    int n_active_pixels, n_active_src, L_nnz, status, refine_iters, pad;
+};
+
+struct StaticData {            // per-context, uploaded once
+    int nx, ny;                // image pixels
+    int n_mask;                // masked pixels
+    int nsplit, nsub;          // split factor, sub-pixels per pixel
+    int n_sub;                 // n_mask * nsub
+    int pnx, pny;              // PSF size
+    int use_noise_map;
+    double cov_inverse;        // uniform 1/sigma^2 when !use_noise_map
+    const double* xvals;       // nx+1
+    const double* yvals;       // ny+1
+    const double* data;        // nx*ny
+    const double* covinv;      // nx*ny (filled with cov_inverse when uniform)
+    const int* mpix;           // n_mask: i*ny+j, j-outer / i-inner order
+    const double* psf;         // pnx*pny
+};
+
+struct SrcOpts {
+    int snx, sny;
+    int auto_grid;
+    double xmin, xmax, ymin, ymax;
+    double lxmin, lxmax, lymin, lymax;
+    double noise_threshold, size_scale;
+    int regularization;
+    double regparam;
+};
+
+// Per-evaluation device workspace (sized for the largest case at creation).
+struct Work {
+    double* spx;  double* spy;         // n_sub source points
+    double* cx;   double* cy;          // snx+1, sny+1 cell corners
+    double* ccx;  double* ccy;         // snx, sny cell centres
+    int* cell3;   double* w3;          // 3 per sub-pixel
+    int* mapped;                       // snx*sny flags
+    int* active_index;                 // snx*sny
+    int* pixmaps;                      // n_mask: # mapped sub-pixels (0 = pixel unmapped)
+    int* rowidx;                       // n_mask: active row or -1
+    int* pixindex;                     // nx*ny: active row or -1
+    int* rowpix;                       // n_mask: image pixel of each active row
+    int* rowptr;                       // N+1
+    int* Lidx;    double* Lval;        // pre-PSF L, CSR
+    int* cidx;    double* cval; int* ccnt;   // compressed rows (duplicates summed), same capacity
+    double* Lpsf;                      // N x ldL, FP64
+    int ldL;                           // leading dimension of Lpsf (>= M_max)
+    double* dvec; double* cvec;        // N: data and C^-1 per active row
+    double* D;                         // M
+    double* F;                         // M x ldF (lower triangle)
+    double* R;                         // M x ldF (lower triangle)
+    int ldF;
+    double* s;   double* tmp;          // M
+    double* model;                     // N
+    double* partial;                   // reduction scratch
+    GridState* gs;
+    EvalOut* out;
+};
+
+// ---- kernels (launch wrappers implemented in the .cu files) ----
+void launch_raytrace(const StaticData& sd, const LensModel& lm, Work& w, cudaStream_t st);
+void launch_grid(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
+void launch_locate(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
+void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
+void launch_build_L(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
+void launch_psf(const StaticData& sd, const SrcOpts& so, Work& w, int M_max, cudaStream_t st);
+void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st);
+void launch_D(Work& w, int N_max, int M_max, cudaStream_t st);
+void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st);
+void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regparam, cudaStream_t st);
+int  launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, cudaStream_t st);
+void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st);
+void launch_solve_fp64(Work& w, int M_max, cudaStream_t st);
+void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max,
+                       double regparam, cudaStream_t st);
+void init_kernel_attributes();
+long long kernel_launch_counter();
+void count_launches(int n);
+
+}  // namespace qlpix
+
+#define QLP_CUDA_CHECK(x) do { cudaError_t e__ = (x); if (e__ != cudaSuccess) return e__; } while (0)

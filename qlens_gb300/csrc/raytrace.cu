@@ -1,0 +1,44 @@
+// raytrace.cu -- FP64 ray shooting of the split image pixels.
+//
+// One thread per sub-pixel.  The sub-pixel centre and the lens equation are
+// evaluated in QLens's operation order so that the source points agree with
+// the reference to the last bit wherever the transcendental functions agree:
+//   sub-pixel centre  (1-u0)*x_i + u0*x_{i+1}     set_nsplits, pixelgrid.cpp:10898-10938
+//   beta = theta - sum_planes zfac_i alpha_i      QLens::deflection, lenscalc.cpp:81-113
+//   per-lens shift / rotate / deflect / rotate    LensProfile::deflection, profile.cpp:1782-1805
+// This file is compiled with --fmad=false: no multiply-add is contracted, the
+// same as the reference on x86-64.
+#include "qlpix_internal.h"
+#include "lens_device.cuh"
+
+namespace qlpix {
+
+__global__ void __launch_bounds__(256) k_raytrace(StaticData sd, LensModel lm, double* __restrict__ spx,
+                                                  double* __restrict__ spy)
+{
+    const int ns = sd.nsplit, nsub = sd.nsub;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < sd.n_sub; t += gridDim.x * blockDim.x) {
+        int m = t / nsub, k = t - m * nsub;
+        int pix = sd.mpix[m];
+        int i = pix / sd.ny, j = pix - i * sd.ny;
+        int ii = k / ns, jj = k - ii * ns;
+        double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
+        double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
+        double px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
+        double py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
+        double bx, by;
+        find_sourcept(lm, px, py, bx, by);
+        spx[t] = bx;
+        spy[t] = by;
+    }
+}
+
+void launch_raytrace(const StaticData& sd, const LensModel& lm, Work& w, cudaStream_t st)
+{
+    if (sd.n_sub == 0) return;
+    int blocks = (sd.n_sub + 255) / 256;
+    k_raytrace<<<blocks, 256, 0, st>>>(sd, lm, w.spx, w.spy);
+    count_launches(1);
+}
+
+}  // namespace qlpix

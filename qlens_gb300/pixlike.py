@@ -1,0 +1,242 @@
+"""Host-side mirror of QLens's pixel-likelihood interface over libqlpix.so.
+
+``PixelLikelihood`` plays the role of the QLens object for the Cartesian
+pixel inversion: it holds the image data (ImagePixelData), the source-grid
+settings, the PSF and the lens list, and ``invert_image_surface_brightness_map``
+returns -2 log(evidence) and chi^2_0 like
+QLens::invert_image_surface_brightness_map (lens.cpp:12293).  Every evaluation
+runs on the GPU through the C ABI in include/qlpix.h; there is no CPU path, and
+a missing or unloadable library raises instead of falling back.
+"""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import abi
+
+_lib = None
+
+
+class LibraryUnavailable(RuntimeError):
+    pass
+
+
+def library_path():
+    return os.path.join(abi.package_dir(), "_lib", "libqlpix.so")
+
+
+def load_library(build_if_missing=False):
+    """Load libqlpix.so (built by qlens_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path) and build_if_missing:
+        from . import build
+        build.build()
+    if not os.path.exists(path):
+        raise LibraryUnavailable("libqlpix.so not built: run python -c 'import __graft_entry__ as g; g.build()'")
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.qlp_srcgrid_defaults.argtypes = [P(abi.qlp_srcgrid_opts)]
+    L.qlp_create.restype = C.c_void_p
+    L.qlp_create.argtypes = [P(abi.qlp_image), P(abi.qlp_psf), P(abi.qlp_srcgrid_opts), C.c_int, P(C.c_int)]
+    L.qlp_set_lens_model.argtypes = [C.c_void_p, P(abi.qlp_lens), C.c_int, P(abi.qlp_planes)]
+    L.qlp_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.qlp_eval.argtypes = [C.c_void_p, P(C.c_double), C.c_double, P(abi.qlp_result)]
+    L.qlp_n_params.argtypes = [C.c_void_p]
+    L.qlp_set_instance_masks.argtypes = [C.c_void_p, P(C.c_ubyte), C.c_int]
+    L.qlp_eval_batch.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(abi.qlp_instance), C.c_int,
+                                 P(abi.qlp_result)]
+    L.qlp_dump.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_int),
+                           P(C.c_double), P(C.c_double), P(C.c_double)]
+    L.qlp_dump_Lpsf.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
+    L.qlp_stage_times.argtypes = [C.c_void_p, P(C.c_float), C.c_int]
+    L.qlp_last_launch_count.restype = C.c_longlong
+    L.qlp_last_launch_count.argtypes = [C.c_void_p]
+    L.qlp_last_error.restype = C.c_char_p
+    L.qlp_destroy.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class QLPixError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("qlpix status %d: %s" % (code, msg))
+        self.code = code
+
+
+def gaussian_psf(sigma_x, sigma_y, pixel_x, pixel_y, psf_threshold=0.01):
+    """QLens::generate_PSF_matrix (pixelgrid.cpp:14601-14668), no supersampling."""
+    sigma_fraction = math.sqrt(-2 * math.log(psf_threshold))
+    nxh_dec = sigma_fraction * sigma_x / pixel_x
+    nyh_dec = sigma_fraction * sigma_y / pixel_y
+    nxh, nyh = int(nxh_dec), int(nyh_dec)
+    if nxh_dec - nxh > 0.5:
+        nxh += 1
+    if nyh_dec - nyh > 0.5:
+        nyh += 1
+    nx, ny = 2 * nxh + 1, 2 * nyh + 1
+    xmax_sup = ((2 * nxh + 1) * pixel_x - pixel_x) / 2
+    ymax_sup = ((2 * nyh + 1) * pixel_y - pixel_y) / 2
+    psf = np.empty((nx, ny))
+    norm = 0.0
+    x = -xmax_sup
+    for i in range(nx):
+        y = -ymax_sup
+        for j in range(ny):
+            psf[i, j] = math.exp(-0.5 * ((x / sigma_x) ** 2 + (y / sigma_y) ** 2))
+            norm += psf[i, j]
+            y += pixel_y
+        x += pixel_x
+    return psf / norm
+
+
+def pixel_corners(nx, xmin, xmax):
+    """ImagePixelGrid corner coordinates: xmin + i*pixel_xlength (pixelgrid.cpp:9581-9590)."""
+    step = (xmax - xmin) / nx
+    return np.array([xmin + i * step for i in range(nx + 1)])
+
+
+class PixelLikelihood:
+    """One GPU context: image data, mask, PSF, source-grid settings and lens list."""
+
+    def __init__(self, xvals, yvals, data, mask, psf, covinv=None, bg_noise=0.0, nsplit=2,
+                 src_npixels=(20, 20), auto_sourcegrid=True, sourcegrid=(-1, 1, -1, 1),
+                 regularization=True, regparam=100.0, device=0, precision=abi.QLP_FP64):
+        self.lib = load_library()
+        self._img = abi.ImageBuffers(xvals, yvals, data, mask, covinv, bg_noise)
+        self._psf = abi.PSFBuffer(psf)
+        o = abi.srcgrid_defaults()
+        o.nsplit = int(nsplit)
+        o.npixels_x, o.npixels_y = int(src_npixels[0]), int(src_npixels[1])
+        o.auto_sourcegrid = 1 if auto_sourcegrid else 0
+        o.xmin, o.xmax, o.ymin, o.ymax = map(float, sourcegrid)
+        o.regularization = 1 if regularization else 0
+        o.regparam = float(regparam)
+        self.opts = o
+        self._create(device)
+        self.set_precision(precision)
+        self.lens_spec = None
+
+    @classmethod
+    def from_opts(cls, image_bufs, psf_buf, opts, device=0, precision=abi.QLP_FP64):
+        self = cls.__new__(cls)
+        self.lib = load_library()
+        self._img, self._psf, self.opts = image_bufs, psf_buf, opts
+        self._create(device)
+        self.set_precision(precision)
+        self.lens_spec = None
+        return self
+
+    def _create(self, device):
+        st = C.c_int(0)
+        self.ctx = self.lib.qlp_create(C.byref(self._img.image), C.byref(self._psf.psf), C.byref(self.opts),
+                                       int(device), C.byref(st))
+        if not self.ctx:
+            raise QLPixError(st.value, self.lib.qlp_last_error().decode())
+
+    def _check(self, code):
+        if code not in (abi.QLP_OK,):
+            raise QLPixError(code, self.lib.qlp_last_error().decode())
+
+    def set_precision(self, mode):
+        self._check(self.lib.qlp_set_precision(self.ctx, int(mode)))
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.qlp_set_stream(self.ctx, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def set_lens_model(self, spec, zfac=None, beta=None):
+        self.lens_spec = spec
+        lenses = abi.make_lenses(spec)
+        planes = abi.make_planes(zfac, beta)
+        self._planes = planes
+        self._check(self.lib.qlp_set_lens_model(self.ctx, lenses, len(spec), C.byref(planes)))
+
+    @property
+    def n_params(self):
+        return self.lib.qlp_n_params(self.ctx)
+
+    def invert_image_surface_brightness_map(self, params=None, regparam=0.0):
+        """Returns the qlp_result as a dict (m2logev = -2 log evidence, chisq0, ...)."""
+        res = abi.qlp_result()
+        pp = None
+        if params is not None:
+            arr = np.ascontiguousarray(params, dtype=np.float64)
+            pp = _dp(arr)
+        self.lib.qlp_eval(self.ctx, pp, float(regparam), C.byref(res))
+        return res.as_dict()
+
+    def set_instance_masks(self, masks):
+        m = np.ascontiguousarray(masks, dtype=np.uint8)
+        self._masks = m
+        self._check(self.lib.qlp_set_instance_masks(self.ctx, m.ctypes.data_as(C.POINTER(C.c_ubyte)), m.shape[0]))
+
+    def eval_batch(self, params, regparams=None, mask_ids=None, src_sizes=None):
+        params = np.ascontiguousarray(params, dtype=np.float64)
+        n = params.shape[0]
+        out = (abi.qlp_result * n)()
+        rp = None
+        if regparams is not None:
+            self._rp = np.ascontiguousarray(regparams, dtype=np.float64)
+            rp = _dp(self._rp)
+        inst = None
+        if mask_ids is not None or src_sizes is not None:
+            inst = (abi.qlp_instance * n)()
+            for i in range(n):
+                inst[i].mask_id = -1 if mask_ids is None else int(mask_ids[i])
+                if src_sizes is None:
+                    inst[i].src_npixels_x = inst[i].src_npixels_y = 0
+                else:
+                    inst[i].src_npixels_x, inst[i].src_npixels_y = map(int, src_sizes[i])
+        code = self.lib.qlp_eval_batch(self.ctx, _dp(params), rp, inst, n, out)
+        if code not in (abi.QLP_OK, abi.QLP_ERR_NOT_SPD, abi.QLP_ERR_NO_SOURCE_PIXELS, abi.QLP_ERR_GRID_TOO_SMALL):
+            self._check(code)
+        return [out[i].as_dict() for i in range(n)]
+
+    def dump(self, n_sub, res):
+        """Intermediates of the last single evaluation (parity hooks)."""
+        N, M, nnz = res["n_active_pixels"], res["n_active_src"], res["L_nnz"]
+        sp = np.empty(2 * n_sub)
+        rp = np.empty(N + 1, dtype=np.int32)
+        li = np.empty(max(nnz, 1), dtype=np.int32)
+        lv = np.empty(max(nnz, 1))
+        ai = np.empty(self.opts.npixels_x * self.opts.npixels_y, dtype=np.int32)
+        D = np.empty(max(M, 1))
+        s = np.empty(max(M, 1))
+        model = np.empty(max(N, 1))
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        self._check(self.lib.qlp_dump(self.ctx, _dp(sp), ip(rp), ip(li), _dp(lv), ip(ai), _dp(D), _dp(s), _dp(model)))
+        return dict(srcpt=sp, L_rowptr=rp, L_index=li[:nnz], L_value=lv[:nnz], active_index=ai, D=D[:M], s=s[:M],
+                    model=model[:N])
+
+    def dump_Lpsf(self, rows, M):
+        out = np.empty((rows, M))
+        self._check(self.lib.qlp_dump_Lpsf(self.ctx, rows, _dp(out)))
+        return out
+
+    def stage_times(self):
+        ms = (C.c_float * 6)()
+        self._check(self.lib.qlp_stage_times(self.ctx, ms, 6))
+        return list(ms)
+
+    def last_launch_count(self):
+        return self.lib.qlp_last_launch_count(self.ctx)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.qlp_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
