@@ -1,0 +1,300 @@
+"""Throughput of the GB300 pixel-image likelihood (evaluations per second).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl qlpix|reference]
+                    [--config cfg2] [--batch B] [--precision mixed|fp64]
+
+A step is one batch of B likelihood evaluations: B lens-parameter vectors are
+drawn from the configuration's prior box and evaluated through the public C
+ABI (qlp_eval_batch).  The default workload is the reference's larger
+single-likelihood configuration (200x200 pixels at 0.04", annular mask,
+4x4 split, 21x21 Airy-like PSF, 64x64 source grid, power-law lens + shear),
+on seeded synthetic data.  `value` is evaluations per second of device time
+(inputs resident: image, mask and PSF are uploaded once when the context is
+created); `e2e` is the same metric through the public call with the step's
+parameter vectors in pinned host memory and the results read back, timed on
+the host.  Under torchrun every rank evaluates its own batches (replicas, weak
+scaling) and the slowest rank's time counts.
+
+--impl reference times the reference's CPU implementation of the same
+workload (the oracle port of QLens's dense inversion, OpenMP over all host
+cores) and prints the same JSON line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 at |ΔlogL|<0.1"
+UNIT = "evals/s"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def make_context(wl, precision):
+    from qlens_gb300 import PixelLikelihood, abi
+    prec = abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64
+    pl = PixelLikelihood(wl.xvals, wl.yvals, wl.data, wl.mask, wl.psf, covinv=None, bg_noise=wl.noise,
+                         nsplit=wl.nsplit, src_npixels=wl.src_npixels, regparam=wl.regparam, precision=prec)
+    pl.set_lens_model(wl.lenses)
+    return pl
+
+
+def algorithmic_syrk_flops(res):
+    """2 * N_pix * M(M+1)/2 per evaluation (the F = L'^T C^-1 L' contraction)."""
+    tot = 0.0
+    for r in res:
+        N, M = r["n_active_pixels"], r["n_active_src"]
+        tot += N * M * (M + 1.0)
+    return tot
+
+
+def cpu_port_eval(wl, params, threads=None):
+    """One evaluation of the oracle port (CPU) on the workload; returns seconds."""
+    from oracle import oracle as O
+    from qlens_gb300 import abi
+    img = abi.ImageBuffers(wl.xvals, wl.yvals, wl.data, wl.mask, None, wl.noise)
+    psf = abi.PSFBuffer(wl.psf)
+    o = abi.srcgrid_defaults()
+    o.nsplit = wl.nsplit
+    o.npixels_x, o.npixels_y = wl.src_npixels
+    o.regparam = wl.regparam
+    t = time.perf_counter()
+    r = O.evaluate(img, psf, o, wl.lenses, lens_params=params)
+    return time.perf_counter() - t, r
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from qlens_gb300 import synthetic
+    from oracle import oracle as O
+    O.build()
+    wl = synthetic.CONFIGS[args.config]()
+    rng = np.random.default_rng(4321)
+    cores = O.threads()
+    for _ in range(args.warmup):
+        cpu_port_eval(wl, wl.draw(rng, 1)[0])
+    times = []
+    for _ in range(args.steps):
+        dt, _r = cpu_port_eval(wl, wl.draw(rng, 1)[0])
+        times.append(dt)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl.name, "batch_per_step": 1, **wl.describe()},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d evaluations, one per step, OpenMP over %d host threads" % (args.steps, cores)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="qlpix", choices=["qlpix", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3"])
+    ap.add_argument("--batch", type=int, default=0, help="evaluations per step (default per precision)")
+    ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
+                    choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+
+    from qlens_gb300 import synthetic, abi
+    wl = synthetic.CONFIGS[args.config]()
+    precision = args.precision
+    pl = make_context(wl, precision)
+    try:
+        pl.set_precision(abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64)
+        probe = pl.invert_image_surface_brightness_map(wl.draw(np.random.default_rng(0), 1)[0])
+        if probe["status"] != 0:
+            raise RuntimeError("mixed path status %d" % probe["status"])
+    except Exception:
+        precision = "fp64"
+        pl.set_precision(abi.QLP_FP64)
+    B = args.batch or (16 if precision == "mixed" else 2)
+    stream = torch.cuda.current_stream()
+    pl.set_stream(stream.cuda_stream)
+
+    rng = np.random.default_rng(1234 + rank)
+    batches = [wl.draw(rng, B) for _ in range(args.warmup + args.steps)]
+    pinned = [torch.from_numpy(b).pin_memory() for b in batches]
+
+    for k in range(args.warmup):
+        pl.eval_batch(pinned[k].numpy())
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    dev_ms = 0.0
+    stage = np.zeros(6)
+    launches = 0
+    results = []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for k in range(args.steps):
+        res = pl.eval_batch(pinned[args.warmup + k].numpy())
+        dev_ms += pl.last_device_ms()
+        stage += np.array(pl.stage_times())
+        launches += pl.last_launch_count()
+        results.extend(res)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    span_ms = e0.elapsed_time(e1)
+
+    # slowest rank decides
+    if dist:
+        t = torch.tensor([dev_ms, wall, span_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms, wall, span_ms = t.tolist()
+
+    n_evals = B * args.steps * world
+    value = n_evals / (dev_ms / 1e3)
+    e2e = n_evals / wall
+    bad = [r for r in results if r["status"] != 0]
+
+    # roofline of the dominant kernel: the F = L'^T C^-1 L' contraction
+    peaks = _peaks()
+    syrk_ms = stage[3]
+    flops = algorithmic_syrk_flops(results)
+    achieved = flops / (syrk_ms / 1e3) / 1e12 if syrk_ms > 0 else None
+    if precision == "mixed":
+        peak = peaks.get("bf16_tflops", 1900.0)
+        peak_note = "measured bf16 burst (MEASURED_PEAKS.json)" if "bf16_tflops" in peaks else "fallback bf16"
+        bound = "tensor"
+    else:
+        peak = 1.25
+        peak_note = "nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)"
+        bound = "fp64"
+    roofline = {"bound": bound, "kernel": "F = L'^T C^-1 L' (SYRK)", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": peak_note, "algorithmic_flops_per_step": flops / args.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        dt, _r = cpu_port_eval(wl, wl.draw(np.random.default_rng(99), 1)[0])
+        from oracle import oracle as O
+        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": O.threads(), "kind": "port",
+               "sample": "1 evaluation of the same workload by the oracle port of QLens's dense inversion"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-tensor+f64" if precision == "mixed" else "f64",
+            "data": "synthetic (seeded mock image; parameters drawn from the prior box)",
+            "config": {**wl.describe(), "batch_per_step": B, "precision": precision,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set (dense L' %.0f MB) exceeds the 129 MB L2" % (
+                           8e-6 * max(r["n_active_pixels"] for r in results) * max(r["n_active_src"] for r in results))},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(B * batches[0].shape[1] * 8),
+                    "d2h_bytes_per_step": int(B * 72)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "stage_ms_per_eval": [x / (B * args.steps) for x in stage],
+            "failed_evals": len(bad),
+            "stream_span_ms": span_ms,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    pl.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

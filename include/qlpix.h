@@ -179,10 +179,16 @@ int qlp_dump(qlp_ctx* ctx, double* srcpt_xy, int* L_rowptr, int* L_index, double
  * columns) of the last qlp_eval. */
 int qlp_dump_Lpsf(qlp_ctx* ctx, int rows, double* out);
 
-/* Milliseconds of device time per stage of the last qlp_eval (CUDA events):
- * [0] ray shooting, [1] grid+mapping, [2] L+PSF, [3] F/D assembly,
- * [4] factorisations+solve, [5] model+chi^2.  n >= 6. */
+/* Milliseconds of device time per stage of the last qlp_eval or
+ * qlp_eval_batch (CUDA events on the context's stream, summed over the
+ * batch): [0] ray shooting, [1] grid + mapping + L, [2] PSF convolution and
+ * D, [3] F = L'^T C^-1 L' (the SYRK), [4] regularisation, factorisations and
+ * solve, [5] model image, chi^2 and evidence.  n >= 6. */
 int qlp_stage_times(qlp_ctx* ctx, float* ms, int n);
+
+/* Device time in milliseconds from the first to the last kernel of the last
+ * qlp_eval / qlp_eval_batch. */
+int qlp_last_device_time(qlp_ctx* ctx, float* ms);
 
 /* Number of kernel launches issued by the last qlp_eval / qlp_eval_batch. */
 long long qlp_last_launch_count(const qlp_ctx* ctx);

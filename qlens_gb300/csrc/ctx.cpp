@@ -12,7 +12,7 @@ namespace qlpix {
 void psf_init_attributes();
 int mixed_init(qlp_ctx* c);
 void mixed_free(qlp_ctx* c);
-int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st);
+int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st, cudaEvent_t* ev);
 
 static int cuda_fail(cudaError_t e, const char* where)
 {
@@ -155,6 +155,7 @@ void ctx_free(qlp_ctx* c)
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);
     for (int i = 0; i <= QLP_N_STAGES; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
 
@@ -180,34 +181,34 @@ static int build_lens_model(qlp_ctx* c, const double* lens_params, LensModel& lm
 }
 
 // The launch sequence of one evaluation on stream st; the image set-up in
-// c->sd / c->so decides the mask and source grid.
-static int run_pipeline(qlp_ctx* c, const LensModel& lm, double regparam, cudaStream_t st, bool timed)
+// c->sd / c->so decides the mask and source grid.  ev (QLP_N_STAGES+1 events
+// or null) brackets the stages.
+static int run_pipeline(qlp_ctx* c, const LensModel& lm, double regparam, cudaStream_t st, cudaEvent_t* ev)
 {
     StaticData& sd = c->sd;
     SrcOpts& so = c->so;
     Work& w = c->w;
     const int Mc = c->M_cap;
     const int N_max = sd.n_mask;
-    if (timed) cudaEventRecord(c->ev[0], st);
+    if (ev) cudaEventRecord(ev[0], st);
     launch_raytrace(sd, lm, w, st);
-    if (timed) cudaEventRecord(c->ev[1], st);
+    if (ev) cudaEventRecord(ev[1], st);
     launch_grid(sd, so, w, st);
     launch_locate(sd, so, w, st);
     launch_compact(sd, so, w, st);
     launch_build_L(sd, so, w, st);
-    if (timed) cudaEventRecord(c->ev[2], st);
+    if (ev) cudaEventRecord(ev[2], st);
     launch_psf(sd, so, w, Mc, st);
     launch_dvec(sd, w, N_max, st);
-    if (timed) cudaEventRecord(c->ev[3], st);
     if (c->precision == QLP_MIXED) {
-        int r = run_inversion_mixed(c, regparam, st);
+        int r = run_inversion_mixed(c, regparam, st, ev);
         if (r != QLP_OK) return r;
-        if (timed) { cudaEventRecord(c->ev[4], st); cudaEventRecord(c->ev[5], st); }
     } else {
         launch_D(w, N_max, Mc, st);
+        if (ev) cudaEventRecord(ev[3], st);
         launch_syrk_fp64(sd, w, N_max, Mc, st);
+        if (ev) cudaEventRecord(ev[4], st);
         launch_regularization(so, w, Mc, regparam, st);
-        if (timed) cudaEventRecord(c->ev[4], st);
         if (so.regularization) {
             launch_cholesky_fp64(w.R, w.ldF, Mc, w.gs, 1, st);
             launch_logdet(w.R, w.ldF, Mc, w, 1, st);
@@ -215,10 +216,10 @@ static int run_pipeline(qlp_ctx* c, const LensModel& lm, double regparam, cudaSt
         launch_cholesky_fp64(w.F, w.ldF, Mc, w.gs, 0, st);
         launch_logdet(w.F, w.ldF, Mc, w, 0, st);
         launch_solve_fp64(w, Mc, st);
-        if (timed) cudaEventRecord(c->ev[5], st);
     }
+    if (ev) cudaEventRecord(ev[5], st);
     launch_model_chi2(sd, so, w, N_max, Mc, regparam, st);
-    if (timed) cudaEventRecord(c->ev[6], st);
+    if (ev) cudaEventRecord(ev[6], st);
     return QLP_OK;
 }
 
@@ -253,13 +254,14 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     long long l0 = kernel_launch_counter();
     cudaStream_t st = c->stream;
     CK(cudaMemsetAsync(c->w.out, 0, sizeof(EvalOut), st), "memset");
-    r = run_pipeline(c, lm, regparam, st, true);
+    r = run_pipeline(c, lm, regparam, st, c->ev);
     if (r != QLP_OK) { out->status = r; return r; }
     CK(cudaMemcpyAsync(c->h_out, c->w.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, st), "d2h");
     CK(cudaGetLastError(), "launch");
     CK(cudaStreamSynchronize(st), "eval");
     c->last_launches = kernel_launch_counter() - l0;
     for (int i = 0; i < QLP_N_STAGES; i++) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
+    cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
     fill_result(*c->h_out, out);
     return out->status;
 }
@@ -314,6 +316,12 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
     const SrcOpts so0 = c->so;
     EvalOut* out0 = c->w.out;
     cudaStream_t st = c->stream;
+    const int ne = QLP_N_STAGES + 1;
+    while ((int)c->ev_pool.size() < ne * n) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e), "event");
+        c->ev_pool.push_back(e);
+    }
     long long l0 = kernel_launch_counter();
     int rc = QLP_OK;
     for (int i = 0; i < n; i++) {
@@ -331,7 +339,7 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         c->w.out = d_res + i;
         cudaMemsetAsync(c->w.out, 0, sizeof(EvalOut), st);
         if (r == QLP_OK && (c->so.snx < 2 || c->so.sny < 2)) r = QLP_ERR_GRID_TOO_SMALL;
-        if (r == QLP_OK) r = run_pipeline(c, lm, lam, st, false);
+        if (r == QLP_OK) r = run_pipeline(c, lm, lam, st, &c->ev_pool[(size_t)ne * i]);
         res[i].status = r;
         c->sd = sd0;
         c->so = so0;
@@ -345,6 +353,21 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
     cudaFree(d_res);
     if (e != cudaSuccess) return cuda_fail(e, "batch");
     c->last_launches = kernel_launch_counter() - l0;
+    for (int k = 0; k < QLP_N_STAGES; k++) c->stage_ms[k] = 0;
+    c->device_ms = 0;
+    int first = -1, last = -1;
+    for (int i = 0; i < n; i++) {
+        if (pre[i] != QLP_OK) continue;
+        if (first < 0) first = i;
+        last = i;
+        for (int k = 0; k < QLP_N_STAGES; k++) {
+            float t = 0;
+            cudaEventElapsedTime(&t, c->ev_pool[(size_t)ne * i + k], c->ev_pool[(size_t)ne * i + k + 1]);
+            c->stage_ms[k] += t;
+        }
+    }
+    if (first >= 0)
+        cudaEventElapsedTime(&c->device_ms, c->ev_pool[(size_t)ne * first], c->ev_pool[(size_t)ne * last + QLP_N_STAGES]);
     for (int i = 0; i < n; i++) {
         fill_result(res[i], &out[i]);
         if (pre[i] != QLP_OK) {

@@ -238,6 +238,13 @@ int qlp_stage_times(qlp_ctx* c, float* ms, int n)
     return QLP_OK;
 }
 
+int qlp_last_device_time(qlp_ctx* c, float* ms)
+{
+    if (!c || !ms) return fail(QLP_ERR_ARG, "bad arguments");
+    *ms = c->device_ms;
+    return QLP_OK;
+}
+
 void qlp_destroy(qlp_ctx* c)
 {
     if (!c) return;

@@ -44,7 +44,9 @@ struct qlp_ctx {
 
     qlpix::EvalOut* h_out = nullptr;      // pinned
     cudaEvent_t ev[QLP_N_STAGES + 1] = {};
+    std::vector<cudaEvent_t> ev_pool;     // (QLP_N_STAGES+1) per batched instance
     float stage_ms[QLP_N_STAGES] = {};
+    float device_ms = 0;
     long long last_launches = 0;
 };
 

@@ -55,6 +55,7 @@ def load_library(build_if_missing=False):
                            P(C.c_double), P(C.c_double), P(C.c_double)]
     L.qlp_dump_Lpsf.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
     L.qlp_stage_times.argtypes = [C.c_void_p, P(C.c_float), C.c_int]
+    L.qlp_last_device_time.argtypes = [C.c_void_p, P(C.c_float)]
     L.qlp_last_launch_count.restype = C.c_longlong
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
     L.qlp_last_error.restype = C.c_char_p
@@ -226,6 +227,11 @@ class PixelLikelihood:
         ms = (C.c_float * 6)()
         self._check(self.lib.qlp_stage_times(self.ctx, ms, 6))
         return list(ms)
+
+    def last_device_ms(self):
+        ms = C.c_float(0)
+        self._check(self.lib.qlp_last_device_time(self.ctx, C.byref(ms)))
+        return ms.value
 
     def last_launch_count(self):
         return self.lib.qlp_last_launch_count(self.ctx)
