@@ -31,7 +31,7 @@ UNITS = [
     ("ctx.cpp", []),
     ("qlpix_api.cpp", []),
 ]
-HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh"]
+HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "chol.cuh", "tc_syrk.cuh"]
 
 
 def _newer(src, obj, deps):
@@ -64,7 +64,7 @@ def build(verbose=False, jobs=None):
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), units))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcuda"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))

@@ -263,6 +263,7 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     for (int i = 0; i < QLP_N_STAGES; i++) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
     cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
     fill_result(*c->h_out, out);
+    if (c->precision == QLP_MIXED) out->refine_iters = 2;
     return out->status;
 }
 
@@ -370,6 +371,7 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         cudaEventElapsedTime(&c->device_ms, c->ev_pool[(size_t)ne * first], c->ev_pool[(size_t)ne * last + QLP_N_STAGES]);
     for (int i = 0; i < n; i++) {
         fill_result(res[i], &out[i]);
+        if (c->precision == QLP_MIXED) out[i].refine_iters = 2;
         if (pre[i] != QLP_OK) {
             out[i].status = pre[i];
             out[i].m2logev = (pre[i] == QLP_ERR_GRID_TOO_SMALL) ? 2e30 : 0;

@@ -17,6 +17,7 @@
 // the solution unchanged.  Every kernel reads N and M from the device-side
 // GridState, so the launch sequence never waits for the host.
 #include "qlpix_internal.h"
+#include "chol.cuh"
 
 namespace qlpix {
 
@@ -82,15 +83,6 @@ void launch_D(Work& w, int N_max, int M_max, cudaStream_t st)
 }
 
 // ---- F = L'^T C^-1 L', lower 64x64 tiles, FP64 ----
-__device__ __forceinline__ void tri_index(int t, int& bi, int& bj)
-{
-    int i = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
-    while ((i + 1) * (i + 2) / 2 <= t) i++;
-    while (i * (i + 1) / 2 > t) i--;
-    bi = i;
-    bj = t - i * (i + 1) / 2;
-}
-
 __global__ void __launch_bounds__(256) k_syrk64(const GridState* __restrict__ gs, const double* __restrict__ L,
                                                 int ldL, const double* __restrict__ cvec, int use_noise_map,
                                                 double cov_inverse, double* __restrict__ F, int ldF)
@@ -210,234 +202,23 @@ void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regpara
     (void)M_max;
 }
 
-// ---- blocked Cholesky (lower), nb = 64 ----
-__global__ void __launch_bounds__(256) k_potrf(double* __restrict__ A, int ld, int k, GridState* gs, int which)
-{
-    __shared__ double S[NB][NB + 1];
-    const int nblk = mpad64(gs->M) / NB;
-    if (k >= nblk) return;
-    const int o = k * NB;
-    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        S[r][c] = (c <= r) ? A[(size_t)(o + r) * ld + o + c] : 0.0;
-    }
-    __syncthreads();
-    for (int j = 0; j < NB; j++) {
-        if (threadIdx.x == 0) {
-            double d = S[j][j];
-            if (d < 0) {
-                // Cholesky_dcmp_packed continues with sqrt(|d|) and flags the matrix (pixelgrid.cpp:17094-17099)
-                int* flag = which ? &gs->not_spd_R : &gs->not_spd_F;
-                if (*flag == 0) *flag = o + j + 1;
-            }
-            S[j][j] = sqrt(fabs(d));
-        }
-        __syncthreads();
-        const double djj = S[j][j];
-        for (int i = j + 1 + threadIdx.x; i < NB; i += blockDim.x) S[i][j] /= djj;
-        __syncthreads();
-        const int rem = NB - j - 1;
-        for (int idx = threadIdx.x; idx < rem * rem; idx += blockDim.x) {
-            int i = j + 1 + idx / rem, c = j + 1 + idx % rem;
-            if (c <= i) S[i][c] -= S[i][j] * S[c][j];
-        }
-        __syncthreads();
-    }
-    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        if (c <= r) A[(size_t)(o + r) * ld + o + c] = S[r][c];
-    }
-}
-
-__global__ void __launch_bounds__(256) k_trsm(double* __restrict__ A, int ld, int k, const GridState* __restrict__ gs)
-{
-    __shared__ double Lk[NB][NB + 1];
-    __shared__ double X[NB][NB + 1];
-    const int nblk = mpad64(gs->M) / NB;
-    const int i = k + 1 + blockIdx.x;
-    if (i >= nblk) return;
-    const int o = k * NB, ro = i * NB;
-    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        Lk[r][c] = (c <= r) ? A[(size_t)(o + r) * ld + o + c] : 0.0;
-        X[r][c] = A[(size_t)(ro + r) * ld + o + c];
-    }
-    __syncthreads();
-    // X Lk^T = A_ik, column by column
-    for (int c = 0; c < NB; c++) {
-        const double dcc = Lk[c][c];
-        for (int r = threadIdx.x; r < NB; r += blockDim.x) X[r][c] /= dcc;
-        __syncthreads();
-        const int rem = NB - c - 1;
-        for (int idx = threadIdx.x; idx < NB * rem; idx += blockDim.x) {
-            int r = idx / rem, c2 = c + 1 + idx % rem;
-            X[r][c2] -= X[r][c] * Lk[c2][c];
-        }
-        __syncthreads();
-    }
-    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        A[(size_t)(ro + r) * ld + o + c] = X[r][c];
-    }
-}
-
-__global__ void __launch_bounds__(256) k_chol_update(double* __restrict__ A, int ld, int k,
-                                                     const GridState* __restrict__ gs)
-{
-    __shared__ double Li[NB][NB + 1];
-    __shared__ double Lj[NB][NB + 1];
-    const int nblk = mpad64(gs->M) / NB;
-    int ti, tj;
-    tri_index(blockIdx.x, ti, tj);
-    const int i = k + 1 + ti, j = k + 1 + tj;
-    if (i >= nblk) return;
-    const int o = k * NB;
-    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        Li[r][c] = A[(size_t)(i * NB + r) * ld + o + c];
-        Lj[r][c] = A[(size_t)(j * NB + r) * ld + o + c];
-    }
-    __syncthreads();
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4];
-    #pragma unroll
-    for (int u = 0; u < 4; u++)
-        #pragma unroll
-        for (int v = 0; v < 4; v++) acc[u][v] = 0;
-    #pragma unroll 8
-    for (int kk = 0; kk < NB; kk++) {
-        double ra[4], rb[4];
-        #pragma unroll
-        for (int u = 0; u < 4; u++) ra[u] = Li[ty * 4 + u][kk];
-        #pragma unroll
-        for (int v = 0; v < 4; v++) rb[v] = Lj[tx * 4 + v][kk];
-        #pragma unroll
-        for (int u = 0; u < 4; u++)
-            #pragma unroll
-            for (int v = 0; v < 4; v++) acc[u][v] += ra[u] * rb[v];
-    }
-    #pragma unroll
-    for (int u = 0; u < 4; u++)
-        #pragma unroll
-        for (int v = 0; v < 4; v++) {
-            size_t off = (size_t)(i * NB + ty * 4 + u) * ld + j * NB + tx * 4 + v;
-            A[off] -= acc[u][v];
-        }
-}
-
+// ---- Cholesky, log det and solve: the templates of chol.cuh in FP64 ----
 int launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, cudaStream_t st)
 {
-    const int nbm = (M_max + NB - 1) / NB;
-    int n = 0;
-    for (int k = 0; k < nbm; k++) {
-        k_potrf<<<1, 256, 0, st>>>(A, ld, k, const_cast<GridState*>(gs), which);
-        n++;
-        const int rem = nbm - k - 1;
-        if (rem > 0) {
-            k_trsm<<<rem, 256, 0, st>>>(A, ld, k, gs);
-            k_chol_update<<<rem * (rem + 1) / 2, 256, 0, st>>>(A, ld, k, gs);
-            n += 2;
-        }
-    }
-    count_launches(n);
-    return n;
-}
-
-// ---- log det = 2 sum log L_ii over the active part ----
-__global__ void __launch_bounds__(1024) k_logdet(const double* __restrict__ A, int ld, const GridState* __restrict__ gs,
-                                                 EvalOut* out, int which)
-{
-    __shared__ double red[32];
-    const int M = gs->M;
-    double acc = 0;
-    // fixed per-thread strided order, then a fixed tree: deterministic
-    for (int i = threadIdx.x; i < M; i += blockDim.x) acc += log(fabs(A[(size_t)i * ld + i]));
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += red[k];
-        if (which) out->logdet_R = 2 * t;
-        else out->logdet_F = 2 * t;
-    }
+    return launch_cholesky_t<double>(A, ld, M_max, gs, which, st);
 }
 
 void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st)
 {
     (void)M_max;
-    k_logdet<<<1, 1024, 0, st>>>(A, ld, w.gs, w.out, which);
+    k_logdet_t<double><<<1, 1024, 0, st>>>(A, ld, w.gs, w.out, which);
     count_launches(1);
-}
-
-// ---- F s = D with the Cholesky factor: blocked forward and backward substitution ----
-__global__ void __launch_bounds__(1024) k_solve(const double* __restrict__ A, int ld, const GridState* __restrict__ gs,
-                                                const double* __restrict__ D, double* __restrict__ s, double* y)
-{
-    __shared__ double part[16][NB + 1];
-    const int Mp = mpad64(gs->M);
-    const int nblk = Mp / NB;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < Mp; i += blockDim.x) y[i] = D[i];
-    __syncthreads();
-    // forward: L y = D
-    for (int kb = 0; kb < nblk; kb++) {
-        const int o = kb * NB;
-        {   // y[o+r] -= L[o+r, 0:o] . y[0:o]; 16 threads per row
-            const int r = tid >> 4, t = tid & 15;
-            double acc = 0;
-            for (int c = t; c < o; c += 16) acc += A[(size_t)(o + r) * ld + c] * y[c];
-            for (int off = 8; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-            __syncthreads();
-            if (t == 0) y[o + r] -= acc;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            for (int c = 0; c < NB; c++) {
-                if (lane == 0) y[o + c] /= A[(size_t)(o + c) * ld + o + c];
-                __syncwarp();
-                const double yc = y[o + c];
-                for (int r = c + 1 + lane; r < NB; r += 32) y[o + r] -= A[(size_t)(o + r) * ld + o + c] * yc;
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-    }
-    // backward: L^T s = y
-    for (int i = tid; i < Mp; i += blockDim.x) s[i] = 0;
-    __syncthreads();
-    for (int kb = nblk - 1; kb >= 0; kb--) {
-        const int o = kb * NB, e = o + NB;
-        {   // part[t][c] = sum_{r >= e, r = e + t (mod 16)} L[r][o+c] s[r]
-            const int c = tid & 63, t = tid >> 6;
-            double acc = 0;
-            for (int r = e + t; r < Mp; r += 16) acc += A[(size_t)r * ld + o + c] * s[r];
-            part[t][c] = acc;
-        }
-        __syncthreads();
-        if (tid < NB) {
-            double acc = 0;
-            for (int t = 0; t < 16; t++) acc += part[t][tid];
-            y[o + tid] -= acc;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            for (int c = NB - 1; c >= 0; c--) {
-                if (lane == 0) s[o + c] = y[o + c] / A[(size_t)(o + c) * ld + o + c];
-                __syncwarp();
-                const double sc = s[o + c];
-                for (int r = lane; r < c; r += 32) y[o + r] -= A[(size_t)(o + c) * ld + o + r] * sc;
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-    }
 }
 
 void launch_solve_fp64(Work& w, int M_max, cudaStream_t st)
 {
     (void)M_max;
-    k_solve<<<1, 1024, 0, st>>>(w.F, w.ldF, w.gs, w.D, w.s, w.tmp);
+    k_solve_t<double><<<1, 1024, 0, st>>>(w.F, w.ldF, w.gs, w.D, w.s, w.tmp);
     count_launches(1);
 }
 

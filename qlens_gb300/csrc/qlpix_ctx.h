@@ -42,6 +42,7 @@ struct qlp_ctx {
     int N_cap = 0;                        // workspace capacity in masked pixels
     int nsub_cap = 0;
 
+    void* mixed = nullptr;                // mixed-precision workspace (mixed.cu)
     qlpix::EvalOut* h_out = nullptr;      // pinned
     cudaEvent_t ev[QLP_N_STAGES + 1] = {};
     std::vector<cudaEvent_t> ev_pool;     // (QLP_N_STAGES+1) per batched instance

@@ -1,0 +1,63 @@
+"""Mixed-precision path (3xTF32 tensor-core SYRK, FP32 Cholesky, FP64
+refinement) against the plain FP64 path and the reference goldens.
+
+Stated bound (the likelihood target): |delta log L| < 0.1, i.e.
+|delta(-2 log evidence)| < 0.2.  The measured error is ~1e-3 (log det F from
+the FP32-class factor); chi^2 and s^T R s use FP64-refined amplitudes and
+agree with the FP64 path to ~1e-8 relative.
+"""
+import numpy as np
+import pytest
+
+from goldens import CASES, Golden
+
+pytestmark = pytest.mark.gpu
+
+LOGL_TOL = 0.1          # |delta log L|
+M2_TOL = 2 * LOGL_TOL   # on -2 log(evidence)
+
+
+def _ctx(g, precision):
+    from qlens_gb300 import PixelLikelihood
+    pl = PixelLikelihood.from_opts(g.image, g.psf, g.opts, precision=precision)
+    pl.set_lens_model(g.lenses)
+    return pl
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_vs_reference(name):
+    from qlens_gb300 import QLP_MIXED
+    g = Golden(name)
+    pl = _ctx(g, QLP_MIXED)
+    r = pl.invert_image_surface_brightness_map()
+    assert r["status"] == 0, r
+    assert r["n_active_src"] == int(g.sc["n_active_src"])
+    assert r["L_nnz"] == int(g.sc["L_nnz"])
+    d = r["m2logev"] - g.sc["m2logev"]
+    print("%s: mixed -2logev %.6f ref %.6f diff %.2e (logdetF diff %.2e, chi2 rel %.2e)" % (
+        name, r["m2logev"], g.sc["m2logev"], d, r["logdet_F"] - g.sc["logdetF"],
+        (r["chisq0"] - g.sc["chisq0"]) / g.sc["chisq0"]))
+    assert abs(d) < M2_TOL
+    assert abs(r["logdet_R"] - g.sc["logdetR"]) < 0.05
+    assert abs(r["chisq0"] - g.sc["chisq0"]) / g.sc["chisq0"] < 1e-6
+    assert r["refine_iters"] >= 1
+    pl.close()
+
+
+def test_mixed_vs_fp64_random_draws():
+    from qlens_gb300 import QLP_FP64, QLP_MIXED, synthetic
+    wl = synthetic.cfg1()
+    from qlens_gb300 import PixelLikelihood
+    kw = dict(covinv=None, bg_noise=wl.noise, nsplit=wl.nsplit, src_npixels=wl.src_npixels, regparam=wl.regparam)
+    p64 = PixelLikelihood(wl.xvals, wl.yvals, wl.data, wl.mask, wl.psf, precision=QLP_FP64, **kw)
+    pmx = PixelLikelihood(wl.xvals, wl.yvals, wl.data, wl.mask, wl.psf, precision=QLP_MIXED, **kw)
+    for pl in (p64, pmx):
+        pl.set_lens_model(wl.lenses)
+    P = wl.draw(np.random.default_rng(7), 8)
+    a = p64.eval_batch(P)
+    b = pmx.eval_batch(P)
+    for ra, rb in zip(a, b):
+        assert ra["status"] == rb["status"] == 0
+        assert abs(ra["m2logev"] - rb["m2logev"]) < M2_TOL, (ra["m2logev"], rb["m2logev"])
+    p64.close()
+    pmx.close()
