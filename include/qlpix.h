@@ -150,6 +150,12 @@ int qlp_set_stream(qlp_ctx* ctx, void* stream);
  * QLens::invert_image_surface_brightness_map (lens.cpp:12293). */
 int qlp_eval(qlp_ctx* ctx, const double* lens_params, double regparam, qlp_result* out);
 
+/* Maximum number of evaluations of one qlp_eval_batch that run concurrently,
+ * each on its own stream with its own workspace (default 16, at most 32).
+ * More slots hide the sequential parts of each evaluation behind the others
+ * at the cost of one workspace per slot. */
+int qlp_set_batch_slots(qlp_ctx* ctx, int slots);
+
 /* Number of doubles in one lens-parameter vector for the current model. */
 int qlp_n_params(const qlp_ctx* ctx);
 

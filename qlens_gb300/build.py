@@ -27,6 +27,7 @@ UNITS = [
     ("mapping.cu", ["--fmad=false"]),
     ("psf.cu", ["--fmad=false"]),
     ("linalg.cu", []),
+    ("sparseops.cu", []),
     ("mixed.cu", []),
     ("ctx.cpp", []),
     ("qlpix_api.cpp", []),

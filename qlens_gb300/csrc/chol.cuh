@@ -27,10 +27,16 @@ __device__ __forceinline__ void tri_index(int t, int& bi, int& bj)
     bj = t - i * (i + 1) / 2;
 }
 
+// Factor the 64x64 diagonal tile in shared memory (two barriers per pivot:
+// scaled pivot column, then the rank-1 update), and, when Linv is given,
+// write the inverse of the factor: columns of L X = I by forward
+// substitution, four threads per column.
 template <typename T>
-__global__ void __launch_bounds__(256) k_potrf_t(T* __restrict__ A, int ld, int k, GridState* gs, int which)
+__global__ void __launch_bounds__(256) k_potrf_t(T* __restrict__ A, int ld, int k, GridState* gs, int which,
+                                                 T* __restrict__ Linv)
 {
     __shared__ T S[CB][CB + 1];
+    __shared__ T colj[CB];
     const int nblk = cpad64(gs->M) / CB;
     if (k >= nblk) return;
     const int o = k * CB;
@@ -40,29 +46,90 @@ __global__ void __launch_bounds__(256) k_potrf_t(T* __restrict__ A, int ld, int 
     }
     __syncthreads();
     for (int j = 0; j < CB; j++) {
-        if (threadIdx.x == 0) {
-            T d = S[j][j];
-            if (d < 0) {
+        if (threadIdx.x >= j && threadIdx.x < CB) {
+            const T d = S[j][j];
+            if (threadIdx.x == j && d < 0) {
+                // Cholesky_dcmp_packed continues with sqrt(|d|) and flags the matrix
                 int* flag = which ? &gs->not_spd_R : &gs->not_spd_F;
                 if (*flag == 0) *flag = o + j + 1;
             }
-            S[j][j] = sqrt(fabs(d));
+            const T sd = sqrt(fabs(d));
+            colj[threadIdx.x] = (threadIdx.x == j) ? sd : S[threadIdx.x][j] / sd;
         }
         __syncthreads();
-        const T djj = S[j][j];
-        for (int i = j + 1 + threadIdx.x; i < CB; i += blockDim.x) S[i][j] /= djj;
-        __syncthreads();
-        const int rem = CB - j - 1;
-        for (int idx = threadIdx.x; idx < rem * rem; idx += blockDim.x) {
-            int i = j + 1 + idx / rem, c = j + 1 + idx % rem;
-            if (c <= i) S[i][c] -= S[i][j] * S[c][j];
+        {
+            const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+            for (int i = j + 1 + ty; i < CB; i += 16) {
+                const T ci = colj[i];
+                for (int c = j + 1 + tx; c <= i; c += 16) S[i][c] -= ci * colj[c];
+            }
         }
+        if (threadIdx.x >= j && threadIdx.x < CB) S[threadIdx.x][j] = colj[threadIdx.x];
         __syncthreads();
     }
     for (int idx = threadIdx.x; idx < CB * CB; idx += blockDim.x) {
         int r = idx / CB, c = idx % CB;
         if (c <= r) A[(size_t)(o + r) * ld + o + c] = S[r][c];
     }
+    if (Linv == nullptr) return;
+    // X = L^-1 column by column; thread group g (4 lanes) owns column j = g.
+    __shared__ T X[CB][CB + 1];
+    const int j = threadIdx.x >> 2, q = threadIdx.x & 3;
+    for (int i = 0; i < CB; i++) {
+        T part = 0;
+        if (i > j)
+            for (int m = j + q; m < i; m += 4) part += S[i][m] * X[m][j];
+        part += __shfl_xor_sync(0xffffffffu, part, 1);
+        part += __shfl_xor_sync(0xffffffffu, part, 2);
+        if (q == 0) X[i][j] = (i < j) ? T(0) : (i == j ? T(1) / S[i][i] : -part / S[i][i]);
+        __syncwarp();
+    }
+    __syncthreads();
+    T* Lk = Linv + (size_t)k * CB * CB;
+    for (int idx = threadIdx.x; idx < CB * CB; idx += blockDim.x) Lk[idx] = X[idx / CB][idx % CB];
+}
+
+// Tiles below the diagonal: X = A_ik L_kk^-T = A_ik Linv^T, a 64x64x64 GEMM
+// per block row (the triangular solve through the explicit inverse of the
+// small diagonal factor, as blocked GPU Cholesky codes commonly do).
+template <typename T>
+__global__ void __launch_bounds__(256) k_trsm_inv_t(T* __restrict__ A, int ld, int k, const T* __restrict__ Linv,
+                                                    const GridState* __restrict__ gs)
+{
+    __shared__ T Ab[CB][CB + 1];
+    __shared__ T Li[CB][CB + 1];
+    const int nblk = cpad64(gs->M) / CB;
+    const int i = k + 1 + blockIdx.x;
+    if (i >= nblk) return;
+    const int o = k * CB, ro = i * CB;
+    for (int idx = threadIdx.x; idx < CB * CB; idx += blockDim.x) {
+        int r = idx / CB, c = idx % CB;
+        Ab[r][c] = A[(size_t)(ro + r) * ld + o + c];
+        Li[r][c] = Linv[(size_t)k * CB * CB + r * CB + c];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    T acc[4][4];
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = 0;
+    #pragma unroll 8
+    for (int m = 0; m < CB; m++) {
+        T ra[4], rb[4];
+        #pragma unroll
+        for (int u = 0; u < 4; u++) ra[u] = Ab[ty * 4 + u][m];
+        #pragma unroll
+        for (int v = 0; v < 4; v++) rb[v] = Li[tx * 4 + v][m];
+        #pragma unroll
+        for (int u = 0; u < 4; u++)
+            #pragma unroll
+            for (int v = 0; v < 4; v++) acc[u][v] += ra[u] * rb[v];
+    }
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) A[(size_t)(ro + ty * 4 + u) * ld + o + tx * 4 + v] = acc[u][v];
 }
 
 template <typename T>
@@ -142,17 +209,19 @@ __global__ void __launch_bounds__(256) k_chol_update_t(T* __restrict__ A, int ld
         }
 }
 
+// Linv: (M_cap/64) x 64 x 64 storage for the inverses of the diagonal
+// factors; the trsm step and the triangular solves use them.
 template <typename T>
-int launch_cholesky_t(T* A, int ld, int M_cap, const GridState* gs, int which, cudaStream_t st)
+int launch_cholesky_t(T* A, int ld, int M_cap, const GridState* gs, int which, cudaStream_t st, T* Linv)
 {
     const int nbm = (M_cap + CB - 1) / CB;
     int n = 0;
     for (int k = 0; k < nbm; k++) {
-        k_potrf_t<T><<<1, 256, 0, st>>>(A, ld, k, const_cast<GridState*>(gs), which);
-        n++;
         const int rem = nbm - k - 1;
+        k_potrf_t<T><<<1, 256, 0, st>>>(A, ld, k, const_cast<GridState*>(gs), which, Linv);
+        n++;
         if (rem > 0) {
-            k_trsm_t<T><<<rem, 256, 0, st>>>(A, ld, k, gs);
+            k_trsm_inv_t<T><<<rem, 256, 0, st>>>(A, ld, k, Linv, gs);
             k_chol_update_t<T><<<rem * (rem + 1) / 2, 256, 0, st>>>(A, ld, k, gs);
             n += 2;
         }
@@ -180,68 +249,110 @@ __global__ void __launch_bounds__(1024) k_logdet_t(const T* __restrict__ A, int 
     }
 }
 
-// F z = r with the Cholesky factor in A (lower): blocked forward and backward
-// substitution in one block; r, z, y are FP64.
+// F z = r with the Cholesky factor in A (lower) and the inverses of its
+// 64x64 diagonal blocks (Linv), one block of 1024 threads.  The arithmetic
+// type is T (float for the mixed path, double for the plain path); r and z
+// are FP64 in global memory, y and z are staged in shared memory as T.
+//   forward  y_k = Linv_k (r_k - sum_{j<k} L_kj y_j)
+//   backward z_k = Linv_k^T (y_k - sum_{j>k} L_jk^T z_j)
+// Dynamic shared memory: solve_smem_bytes<T>(M_cap).
 template <typename T>
-__global__ void __launch_bounds__(1024) k_solve_t(const T* __restrict__ A, int ld, const GridState* __restrict__ gs,
-                                                  const double* __restrict__ r, double* __restrict__ z, double* y)
+__host__ __device__ __forceinline__ size_t solve_smem_bytes(int M_cap)
 {
-    __shared__ double part[16][CB + 1];
+    return sizeof(T) * ((size_t)2 * M_cap + 2 * CB + 16 * (CB + 1));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_solve_t(const T* __restrict__ A, int ld, const T* __restrict__ Linv,
+                                                  const GridState* __restrict__ gs, const double* __restrict__ r,
+                                                  double* __restrict__ zout, int M_cap)
+{
+    extern __shared__ __align__(16) unsigned char sm_solve_raw[];
+    T* y = reinterpret_cast<T*>(sm_solve_raw);
+    T* z = y + M_cap;
+    T* t = z + M_cap;                 // [CB] block right-hand side
+    T* part = t + 2 * CB;             // [16][CB+1]
     const int Mp = cpad64(gs->M);
     const int nblk = Mp / CB;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < Mp; i += blockDim.x) y[i] = r[i];
+    for (int i = tid; i < Mp; i += blockDim.x) { y[i] = (T)r[i]; z[i] = 0; }
     __syncthreads();
+    // ---- forward ----
     for (int kb = 0; kb < nblk; kb++) {
         const int o = kb * CB;
-        {
-            const int row = tid >> 4, t = tid & 15;
-            double acc = 0;
-            for (int c = t; c < o; c += 16) acc += (double)A[(size_t)(o + row) * ld + c] * y[c];
-            for (int off = 8; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-            __syncthreads();
-            if (t == 0) y[o + row] -= acc;
+        for (int h = 0; h < 2; h++) {
+            const int row = warp * 2 + h;
+            const T* Ar = A + (size_t)(o + row) * ld;
+            T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+            int c = lane;
+            for (; c + 224 < o; c += 256) {
+                const T v0 = Ar[c], v1 = Ar[c + 32], v2 = Ar[c + 64], v3 = Ar[c + 96];
+                const T v4 = Ar[c + 128], v5 = Ar[c + 160], v6 = Ar[c + 192], v7 = Ar[c + 224];
+                a0 += v0 * y[c] + v4 * y[c + 128];
+                a1 += v1 * y[c + 32] + v5 * y[c + 160];
+                a2 += v2 * y[c + 64] + v6 * y[c + 192];
+                a3 += v3 * y[c + 96] + v7 * y[c + 224];
+            }
+            for (; c < o; c += 32) a0 += Ar[c] * y[c];
+            T acc = (a0 + a1) + (a2 + a3);
+            for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+            if (lane == 0) t[row] = y[o + row] - acc;
         }
         __syncthreads();
-        if (warp == 0) {
-            for (int c = 0; c < CB; c++) {
-                if (lane == 0) y[o + c] /= (double)A[(size_t)(o + c) * ld + o + c];
-                __syncwarp();
-                const double yc = y[o + c];
-                for (int rr = c + 1 + lane; rr < CB; rr += 32) y[o + rr] -= (double)A[(size_t)(o + rr) * ld + o + c] * yc;
-                __syncwarp();
-            }
+        {   // y_k = Linv_k t: 16 threads per row
+            const int row = tid >> 4, q = tid & 15;
+            const T* Lr = Linv + (size_t)kb * CB * CB + row * CB;
+            T acc = 0;
+            for (int m = q; m <= row; m += 16) acc += Lr[m] * t[m];
+            for (int off = 8; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+            if (q == 0) y[o + row] = acc;
         }
         __syncthreads();
     }
-    for (int i = tid; i < Mp; i += blockDim.x) z[i] = 0;
-    __syncthreads();
+    // ---- backward ----
     for (int kb = nblk - 1; kb >= 0; kb--) {
         const int o = kb * CB, e = o + CB;
         {
-            const int c = tid & 63, t = tid >> 6;
-            double acc = 0;
-            for (int rr = e + t; rr < Mp; rr += 16) acc += (double)A[(size_t)rr * ld + o + c] * z[rr];
-            part[t][c] = acc;
+            const int c = tid & 63, tt = tid >> 6;
+            T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+            int rr = e + tt;
+            for (; rr + 48 < Mp; rr += 64) {
+                const T v0 = A[(size_t)rr * ld + o + c];
+                const T v1 = A[(size_t)(rr + 16) * ld + o + c];
+                const T v2 = A[(size_t)(rr + 32) * ld + o + c];
+                const T v3 = A[(size_t)(rr + 48) * ld + o + c];
+                a0 += v0 * z[rr];
+                a1 += v1 * z[rr + 16];
+                a2 += v2 * z[rr + 32];
+                a3 += v3 * z[rr + 48];
+            }
+            for (; rr < Mp; rr += 16) a0 += A[(size_t)rr * ld + o + c] * z[rr];
+            part[tt * (CB + 1) + c] = (a0 + a1) + (a2 + a3);
         }
         __syncthreads();
         if (tid < CB) {
-            double acc = 0;
-            for (int t = 0; t < 16; t++) acc += part[t][tid];
-            y[o + tid] -= acc;
+            T acc = 0;
+            for (int q = 0; q < 16; q++) acc += part[q * (CB + 1) + tid];
+            t[tid] = y[o + tid] - acc;
         }
         __syncthreads();
-        if (warp == 0) {
-            for (int c = CB - 1; c >= 0; c--) {
-                if (lane == 0) z[o + c] = y[o + c] / (double)A[(size_t)(o + c) * ld + o + c];
-                __syncwarp();
-                const double zc = z[o + c];
-                for (int rr = lane; rr < c; rr += 32) y[o + rr] -= (double)A[(size_t)(o + c) * ld + o + rr] * zc;
-                __syncwarp();
-            }
+        {   // z_k = Linv_k^T t: column c of Linv, 16 threads per column
+            const int c = tid >> 4, q = tid & 15;
+            const T* Lk = Linv + (size_t)kb * CB * CB;
+            T acc = 0;
+            for (int m = c + q; m < CB; m += 16) acc += Lk[m * CB + c] * t[m];
+            for (int off = 8; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+            if (q == 0) z[o + c] = acc;
         }
         __syncthreads();
     }
+    for (int i = tid; i < Mp; i += blockDim.x) zout[i] = (double)z[i];
+}
+
+template <typename T>
+void solve_init_attributes()
+{
+    cudaFuncSetAttribute(k_solve_t<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 }  // namespace qlpix

@@ -1,4 +1,5 @@
-// ctx.cpp -- context set-up, workspace, and the per-evaluation launch sequence.
+// ctx.cpp -- context set-up, evaluation slots, and the per-evaluation launch
+// sequence.
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstring>
@@ -10,9 +11,8 @@
 namespace qlpix {
 
 void psf_init_attributes();
-int mixed_init(qlp_ctx* c);
-void mixed_free(qlp_ctx* c);
-int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st, cudaEvent_t* ev);
+void linalg_init_attributes();
+void sparseops_init_attributes();
 
 static int cuda_fail(cudaError_t e, const char* where)
 {
@@ -45,17 +45,25 @@ static void free_work(Work& w)
 {
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
-                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.gs, w.out};
+                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
 
-// Workspace for up to n_mask masked pixels, nsub sub-pixels each and Mcells
-// source cells.
-static int alloc_work(qlp_ctx* c, int n_mask, int nsub, int Mcells, int snx_max, int sny_max)
+static void free_slot(Slot& s)
 {
-    Work& w = c->w;
-    free_work(w);
+    mixed_free(s);
+    free_work(s.w);
+    s.M_cap = s.N_cap = s.nsub_cap = s.snx_cap = s.sny_cap = 0;
+    s.fp64_mats = false;
+}
+
+// Workspace of one slot for up to n_mask masked pixels (nsub sub-pixels each)
+// and Mcells source cells.  The FP64 F and R are allocated on first use.
+static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int snx_max, int sny_max)
+{
+    free_slot(s);
+    Work& w = s.w;
     const int Mc = round64(std::max(Mcells, 64));
     const size_t n_sub = (size_t)n_mask * nsub;
     const size_t nnz = 3 * n_sub;
@@ -71,22 +79,48 @@ static int alloc_work(qlp_ctx* c, int n_mask, int nsub, int Mcells, int snx_max,
     CK(dalloc(&w.Lidx, nnz), "alloc"); CK(dalloc(&w.Lval, nnz), "alloc");
     CK(dalloc(&w.cidx, nnz), "alloc"); CK(dalloc(&w.cval, nnz), "alloc"); CK(dalloc(&w.ccnt, n_mask), "alloc");
     w.ldL = Mc;
-    CK(dalloc(&w.Lpsf, (size_t)n_mask * Mc), "alloc L'");
     CK(dalloc(&w.dvec, n_mask), "alloc"); CK(dalloc(&w.cvec, n_mask), "alloc");
     w.ldF = Mc;
     CK(dalloc(&w.D, Mc), "alloc");
-    CK(dalloc(&w.F, (size_t)Mc * Mc), "alloc F");
-    CK(dalloc(&w.R, (size_t)Mc * Mc), "alloc R");
     CK(dalloc(&w.s, Mc), "alloc"); CK(dalloc(&w.tmp, Mc), "alloc");
     CK(dalloc(&w.model, n_mask), "alloc");
     const size_t part = std::max((size_t)((n_mask + 255) / 256 + 1) * Mc, (size_t)Mc * 4);
     CK(dalloc(&w.partial, part), "alloc");
+    CK(dalloc(&w.linv, (size_t)Mc * 64), "alloc");
     CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc");
-    CK(cudaMemset(w.Lpsf, 0, sizeof(double) * (size_t)n_mask * Mc), "memset");
-    c->M_cap = Mc;
-    c->N_cap = n_mask;
-    c->nsub_cap = nsub;
+    s.M_cap = Mc;
+    s.N_cap = n_mask;
+    s.nsub_cap = nsub;
+    s.snx_cap = snx_max;
+    s.sny_cap = sny_max;
     return QLP_OK;
+}
+
+// Dense FP64 L', F and R: only the plain path uses them.
+static int ensure_fp64_mats(Slot& s)
+{
+    if (s.fp64_mats) return QLP_OK;
+    CK(dalloc(&s.w.Lpsf, (size_t)s.N_cap * s.M_cap), "alloc L'");
+    CK(cudaMemset(s.w.Lpsf, 0, sizeof(double) * (size_t)s.N_cap * s.M_cap), "memset");
+    CK(dalloc(&s.w.F, (size_t)s.M_cap * s.M_cap), "alloc F");
+    CK(dalloc(&s.w.R, (size_t)s.M_cap * s.M_cap), "alloc R");
+    s.fp64_mats = true;
+    return QLP_OK;
+}
+
+// Make slot k exist with at least the given capacities.
+static int ensure_slot(qlp_ctx* c, int k, int n_mask, int cells, int snx, int sny)
+{
+    while ((int)c->slots.size() <= k) c->slots.emplace_back();
+    Slot& s = c->slots[k];
+    if (!s.stream) CK(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "stream");
+    if (!s.done) CK(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "event");
+    const int nsub = c->sd.nsub;
+    if (s.N_cap >= n_mask && s.M_cap >= round64(std::max(cells, 64)) && s.snx_cap >= snx && s.sny_cap >= sny &&
+        s.nsub_cap == nsub)
+        return QLP_OK;
+    return alloc_work(c, s, std::max(n_mask, s.N_cap), nsub, std::max(cells, s.M_cap), std::max(snx, s.snx_cap),
+                      std::max(sny, s.sny_cap));
 }
 
 int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts* opts)
@@ -99,7 +133,8 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "stream");
     c->stream = c->own_stream;
     for (int i = 0; i <= QLP_N_STAGES; i++) CK(cudaEventCreate(&c->ev[i]), "event");
-    CK(cudaMallocHost((void**)&c->h_out, sizeof(EvalOut)), "pinned");
+    CK(cudaEventCreate(&c->fork), "event");
+    CK(cudaEventCreate(&c->join), "event");
 
     std::vector<double> covinv(npx);
     const bool noise_map = im->covinv_map != nullptr;
@@ -141,20 +176,26 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     so.regparam = opts->regparam;
 
     psf_init_attributes();
+    linalg_init_attributes();
+    sparseops_init_attributes();
     int snx = std::max(so.snx, 2), sny = std::max(so.sny, 2);
-    int r = alloc_work(c, sd.n_mask, sd.nsub, snx * sny, snx, sny);
-    if (r != QLP_OK) return r;
-    return QLP_OK;
+    return ensure_slot(c, 0, sd.n_mask, snx * sny, snx, sny);
 }
 
 void ctx_free(qlp_ctx* c)
 {
-    mixed_free(c);
-    free_work(c->w);
-    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix};
+    for (Slot& s : c->slots) {
+        free_slot(s);
+        if (s.stream) cudaStreamDestroy(s.stream);
+        if (s.done) cudaEventDestroy(s.done);
+    }
+    c->slots.clear();
+    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix, c->d_res};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);
     for (int i = 0; i <= QLP_N_STAGES; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->fork) cudaEventDestroy(c->fork);
+    if (c->join) cudaEventDestroy(c->join);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
@@ -180,15 +221,16 @@ static int build_lens_model(qlp_ctx* c, const double* lens_params, LensModel& lm
     return QLP_OK;
 }
 
-// The launch sequence of one evaluation on stream st; the image set-up in
-// c->sd / c->so decides the mask and source grid.  ev (QLP_N_STAGES+1 events
+// The launch sequence of one evaluation on stream st with the workspace of
+// `slot`; sd / so select the mask and source grid.  ev (QLP_N_STAGES+1 events
 // or null) brackets the stages.
-static int run_pipeline(qlp_ctx* c, const LensModel& lm, double regparam, cudaStream_t st, cudaEvent_t* ev)
+static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const SrcOpts& so_in, const LensModel& lm,
+                        double regparam, cudaStream_t st, cudaEvent_t* ev)
 {
-    StaticData& sd = c->sd;
-    SrcOpts& so = c->so;
-    Work& w = c->w;
-    const int Mc = c->M_cap;
+    StaticData sd = sd_in;
+    SrcOpts so = so_in;
+    Work& w = slot.w;
+    const int Mc = slot.M_cap;
     const int N_max = sd.n_mask;
     if (ev) cudaEventRecord(ev[0], st);
     launch_raytrace(sd, lm, w, st);
@@ -197,28 +239,32 @@ static int run_pipeline(qlp_ctx* c, const LensModel& lm, double regparam, cudaSt
     launch_locate(sd, so, w, st);
     launch_compact(sd, so, w, st);
     launch_build_L(sd, so, w, st);
+    launch_rowpix(sd, w, st);
     if (ev) cudaEventRecord(ev[2], st);
-    launch_psf(sd, so, w, Mc, st);
     launch_dvec(sd, w, N_max, st);
-    if (c->precision == QLP_MIXED) {
-        int r = run_inversion_mixed(c, regparam, st, ev);
+    const bool mixed = (c->precision == QLP_MIXED);
+    if (mixed) {
+        int r = run_inversion_mixed(slot, sd, so, regparam, st, ev);
         if (r != QLP_OK) return r;
     } else {
+        int r = ensure_fp64_mats(slot);
+        if (r != QLP_OK) return r;
+        launch_psf(sd, so, w, Mc, st);
         launch_D(w, N_max, Mc, st);
         if (ev) cudaEventRecord(ev[3], st);
         launch_syrk_fp64(sd, w, N_max, Mc, st);
         if (ev) cudaEventRecord(ev[4], st);
         launch_regularization(so, w, Mc, regparam, st);
         if (so.regularization) {
-            launch_cholesky_fp64(w.R, w.ldF, Mc, w.gs, 1, st);
+            launch_cholesky_fp64(w.R, w.ldF, Mc, w.gs, 1, w.linv, st);
             launch_logdet(w.R, w.ldF, Mc, w, 1, st);
         }
-        launch_cholesky_fp64(w.F, w.ldF, Mc, w.gs, 0, st);
+        launch_cholesky_fp64(w.F, w.ldF, Mc, w.gs, 0, w.linv, st);
         launch_logdet(w.F, w.ldF, Mc, w, 0, st);
         launch_solve_fp64(w, Mc, st);
     }
     if (ev) cudaEventRecord(ev[5], st);
-    launch_model_chi2(sd, so, w, N_max, Mc, regparam, st);
+    launch_model_chi2(sd, so, w, N_max, Mc, regparam, st, mixed);
     if (ev) cudaEventRecord(ev[6], st);
     return QLP_OK;
 }
@@ -239,6 +285,23 @@ static void fill_result(const EvalOut& o, qlp_result* out)
     out->refine_iters = o.refine_iters;
 }
 
+static int ensure_results(qlp_ctx* c, int n)
+{
+    if (c->h_out_cap < n) {
+        if (c->h_out) cudaFreeHost(c->h_out);
+        c->h_out = nullptr;
+        CK(cudaMallocHost((void**)&c->h_out, sizeof(EvalOut) * n), "pinned");
+        c->h_out_cap = n;
+    }
+    if (c->d_res_cap < n) {
+        if (c->d_res) cudaFree(c->d_res);
+        c->d_res = nullptr;
+        CK(dalloc(&c->d_res, n), "alloc");
+        c->d_res_cap = n;
+    }
+    return QLP_OK;
+}
+
 int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result* out)
 {
     memset(out, 0, sizeof(*out));
@@ -251,18 +314,26 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     int r = build_lens_model(c, lens_params, lm);
     if (r != QLP_OK) { out->status = r; return r; }
     if (regparam <= 0) regparam = c->opts.regparam;
+    r = ensure_results(c, 1);
+    if (r != QLP_OK) return r;
+    if (c->precision == QLP_MIXED) {
+        r = mixed_init(c->slots[0]);
+        if (r != QLP_OK) { out->status = r; return r; }
+    }
+    Slot& s = c->slots[0];
     long long l0 = kernel_launch_counter();
     cudaStream_t st = c->stream;
-    CK(cudaMemsetAsync(c->w.out, 0, sizeof(EvalOut), st), "memset");
-    r = run_pipeline(c, lm, regparam, st, c->ev);
+    s.w.out = c->d_res;
+    CK(cudaMemsetAsync(s.w.out, 0, sizeof(EvalOut), st), "memset");
+    r = run_pipeline(c, s, c->sd, c->so, lm, regparam, st, c->ev);
     if (r != QLP_OK) { out->status = r; return r; }
-    CK(cudaMemcpyAsync(c->h_out, c->w.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaMemcpyAsync(c->h_out, c->d_res, sizeof(EvalOut), cudaMemcpyDeviceToHost, st), "d2h");
     CK(cudaGetLastError(), "launch");
     CK(cudaStreamSynchronize(st), "eval");
     c->last_launches = kernel_launch_counter() - l0;
     for (int i = 0; i < QLP_N_STAGES; i++) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
     cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
-    fill_result(*c->h_out, out);
+    fill_result(c->h_out[0], out);
     if (c->precision == QLP_MIXED) out->refine_iters = 2;
     return out->status;
 }
@@ -286,91 +357,97 @@ int ctx_set_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)
     return QLP_OK;
 }
 
-// Batched evaluation: every instance runs the same device pipeline with its
-// own mask and source grid, back to back on the stream, with one host
+// Batched evaluation: instance i runs on slot i % S, each slot on its own
+// stream, forked from and joined back into the context stream, with one host
 // synchronisation for the whole batch.
 int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, const qlp_instance* inst, int n,
                    qlp_result* out)
 {
     cudaSetDevice(c->device);
+    if (n == 0) return QLP_OK;
     const int np = [&] { int s = 0; for (auto& l : c->lenses) s += n_params_of(l.type); return s; }();
-    // capacity: largest mask and source grid of the batch
     int nmask_max = (int)c->mpix.size(), cells_max = c->so.snx * c->so.sny, snx_max = c->so.snx, sny_max = c->so.sny;
     for (int i = 0; i < n && inst; i++) {
-        if (inst[i].mask_id >= (int)c->mask_cnt.size()) { set_error("%s %d", "bad mask id", inst[i].mask_id); return QLP_ERR_ARG; }
+        if (inst[i].mask_id >= (int)c->mask_cnt.size()) {
+            set_error("%s %d", "bad mask id", inst[i].mask_id);
+            return QLP_ERR_ARG;
+        }
         if (inst[i].mask_id >= 0) nmask_max = std::max(nmask_max, c->mask_cnt[inst[i].mask_id]);
         if (inst[i].src_npixels_x < 2 || inst[i].src_npixels_y < 2) continue;
         cells_max = std::max(cells_max, inst[i].src_npixels_x * inst[i].src_npixels_y);
         snx_max = std::max(snx_max, inst[i].src_npixels_x);
         sny_max = std::max(sny_max, inst[i].src_npixels_y);
     }
-    if (nmask_max > c->N_cap || round64(cells_max) > c->M_cap || snx_max > c->so.snx || sny_max > c->so.sny) {
-        int r = alloc_work(c, std::max(nmask_max, c->N_cap), c->sd.nsub, std::max(cells_max, c->M_cap),
-                           std::max(snx_max, c->so.snx), std::max(sny_max, c->so.sny));
-        if (r != QLP_OK) return r;
-        if (c->precision == QLP_MIXED) { mixed_free(c); }
+    // slot count: bounded by the batch, the configured maximum and memory
+    int S = std::min(n, std::max(1, std::min(c->max_slots, QLP_MAX_SLOTS)));
+    for (int k = 0; k < S; k++) {
+        int r = ensure_slot(c, k, nmask_max, cells_max, std::max(snx_max, 2), std::max(sny_max, 2));
+        if (r == QLP_OK && c->precision == QLP_MIXED) r = mixed_init(c->slots[k]);
+        if (r != QLP_OK) {
+            if (k == 0) return r;
+            free_slot(c->slots[k]);
+            cudaGetLastError();
+            S = k;
+            break;
+        }
     }
-    std::vector<EvalOut> res(n > 0 ? n : 1);
-    EvalOut* d_res = nullptr;
-    CK(dalloc(&d_res, n > 0 ? n : 1), "alloc");
-    const StaticData sd0 = c->sd;
-    const SrcOpts so0 = c->so;
-    EvalOut* out0 = c->w.out;
-    cudaStream_t st = c->stream;
+    int r = ensure_results(c, n);
+    if (r != QLP_OK) return r;
     const int ne = QLP_N_STAGES + 1;
     while ((int)c->ev_pool.size() < ne * n) {
         cudaEvent_t e;
         CK(cudaEventCreate(&e), "event");
         c->ev_pool.push_back(e);
     }
+    cudaStream_t st0 = c->stream;
     long long l0 = kernel_launch_counter();
+    CK(cudaMemsetAsync(c->d_res, 0, sizeof(EvalOut) * n, st0), "memset");
+    CK(cudaEventRecord(c->fork, st0), "event");
+    for (int k = 0; k < S; k++) CK(cudaStreamWaitEvent(c->slots[k].stream, c->fork, 0), "wait");
+    std::vector<int> pre(n, QLP_OK);
     int rc = QLP_OK;
     for (int i = 0; i < n; i++) {
+        Slot& s = c->slots[i % S];
         LensModel lm;
-        int r = build_lens_model(c, params + (size_t)i * np, lm);
-        double lam = (regparams && regparams[i] > 0) ? regparams[i] : c->opts.regparam;
+        int ri = build_lens_model(c, params + (size_t)i * np, lm);
+        const double lam = (regparams && regparams[i] > 0) ? regparams[i] : c->opts.regparam;
+        StaticData sd = c->sd;
+        SrcOpts so = c->so;
         if (inst) {
             if (inst[i].mask_id >= 0) {
-                c->sd.mpix = c->d_inst_mpix + c->mask_off[inst[i].mask_id];
-                c->sd.n_mask = c->mask_cnt[inst[i].mask_id];
-                c->sd.n_sub = c->sd.n_mask * c->sd.nsub;
+                sd.mpix = c->d_inst_mpix + c->mask_off[inst[i].mask_id];
+                sd.n_mask = c->mask_cnt[inst[i].mask_id];
+                sd.n_sub = sd.n_mask * sd.nsub;
             }
-            if (inst[i].src_npixels_x > 0) { c->so.snx = inst[i].src_npixels_x; c->so.sny = inst[i].src_npixels_y; }
+            if (inst[i].src_npixels_x > 0) { so.snx = inst[i].src_npixels_x; so.sny = inst[i].src_npixels_y; }
         }
-        c->w.out = d_res + i;
-        cudaMemsetAsync(c->w.out, 0, sizeof(EvalOut), st);
-        if (r == QLP_OK && (c->so.snx < 2 || c->so.sny < 2)) r = QLP_ERR_GRID_TOO_SMALL;
-        if (r == QLP_OK) r = run_pipeline(c, lm, lam, st, &c->ev_pool[(size_t)ne * i]);
-        res[i].status = r;
-        c->sd = sd0;
-        c->so = so0;
-        if (r != QLP_OK && rc == QLP_OK) rc = r;
+        s.w.out = c->d_res + i;
+        if (ri == QLP_OK && (so.snx < 2 || so.sny < 2)) ri = QLP_ERR_GRID_TOO_SMALL;
+        if (ri == QLP_OK) ri = run_pipeline(c, s, sd, so, lm, lam, s.stream, &c->ev_pool[(size_t)ne * i]);
+        pre[i] = ri;
+        if (ri != QLP_OK && rc == QLP_OK) rc = ri;
     }
-    c->w.out = out0;
-    std::vector<int> pre(n);
-    for (int i = 0; i < n; i++) pre[i] = res[i].status;
-    cudaError_t e = cudaMemcpyAsync(res.data(), d_res, sizeof(EvalOut) * n, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d_res);
-    if (e != cudaSuccess) return cuda_fail(e, "batch");
+    for (int k = 0; k < S; k++) {
+        CK(cudaEventRecord(c->slots[k].done, c->slots[k].stream), "event");
+        CK(cudaStreamWaitEvent(st0, c->slots[k].done, 0), "wait");
+    }
+    CK(cudaEventRecord(c->join, st0), "event");
+    CK(cudaMemcpyAsync(c->h_out, c->d_res, sizeof(EvalOut) * n, cudaMemcpyDeviceToHost, st0), "d2h");
+    CK(cudaGetLastError(), "launch");
+    CK(cudaStreamSynchronize(st0), "batch");
     c->last_launches = kernel_launch_counter() - l0;
     for (int k = 0; k < QLP_N_STAGES; k++) c->stage_ms[k] = 0;
-    c->device_ms = 0;
-    int first = -1, last = -1;
     for (int i = 0; i < n; i++) {
         if (pre[i] != QLP_OK) continue;
-        if (first < 0) first = i;
-        last = i;
         for (int k = 0; k < QLP_N_STAGES; k++) {
             float t = 0;
             cudaEventElapsedTime(&t, c->ev_pool[(size_t)ne * i + k], c->ev_pool[(size_t)ne * i + k + 1]);
             c->stage_ms[k] += t;
         }
     }
-    if (first >= 0)
-        cudaEventElapsedTime(&c->device_ms, c->ev_pool[(size_t)ne * first], c->ev_pool[(size_t)ne * last + QLP_N_STAGES]);
+    cudaEventElapsedTime(&c->device_ms, c->fork, c->join);
     for (int i = 0; i < n; i++) {
-        fill_result(res[i], &out[i]);
+        fill_result(c->h_out[i], &out[i]);
         if (c->precision == QLP_MIXED) out[i].refine_iters = 2;
         if (pre[i] != QLP_OK) {
             out[i].status = pre[i];
@@ -384,7 +461,7 @@ int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* 
              double* D, double* s, double* model)
 {
     cudaSetDevice(c->device);
-    Work& w = c->w;
+    Work& w = c->slots[0].w;
     GridState gs;
     CK(cudaMemcpy(&gs, w.gs, sizeof(gs), cudaMemcpyDeviceToHost), "d2h");
     const int nsub = c->sd.n_sub;
@@ -397,7 +474,8 @@ int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* 
     if (L_rowptr) CK(cudaMemcpy(L_rowptr, w.rowptr, sizeof(int) * (gs.N + 1), cudaMemcpyDeviceToHost), "d2h");
     if (L_index) CK(cudaMemcpy(L_index, w.Lidx, sizeof(int) * gs.nnz, cudaMemcpyDeviceToHost), "d2h");
     if (L_value) CK(cudaMemcpy(L_value, w.Lval, sizeof(double) * gs.nnz, cudaMemcpyDeviceToHost), "d2h");
-    if (active_index) CK(cudaMemcpy(active_index, w.active_index, sizeof(int) * gs.snx * gs.sny, cudaMemcpyDeviceToHost), "d2h");
+    if (active_index)
+        CK(cudaMemcpy(active_index, w.active_index, sizeof(int) * gs.snx * gs.sny, cudaMemcpyDeviceToHost), "d2h");
     if (D) CK(cudaMemcpy(D, w.D, sizeof(double) * gs.M, cudaMemcpyDeviceToHost), "d2h");
     if (s) CK(cudaMemcpy(s, w.s, sizeof(double) * gs.M, cudaMemcpyDeviceToHost), "d2h");
     if (model) CK(cudaMemcpy(model, w.model, sizeof(double) * gs.N, cudaMemcpyDeviceToHost), "d2h");
@@ -407,11 +485,12 @@ int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* 
 int ctx_dump_Lpsf(qlp_ctx* c, int rows, double* out)
 {
     cudaSetDevice(c->device);
+    Work& w = c->slots[0].w;
     GridState gs;
-    CK(cudaMemcpy(&gs, c->w.gs, sizeof(gs), cudaMemcpyDeviceToHost), "d2h");
+    CK(cudaMemcpy(&gs, w.gs, sizeof(gs), cudaMemcpyDeviceToHost), "d2h");
     if (rows > gs.N) rows = gs.N;
-    if (rows <= 0 || gs.M <= 0) return QLP_OK;
-    CK(cudaMemcpy2D(out, sizeof(double) * gs.M, c->w.Lpsf, sizeof(double) * c->w.ldL, sizeof(double) * gs.M, rows,
+    if (rows <= 0 || gs.M <= 0 || !w.Lpsf) return QLP_OK;
+    CK(cudaMemcpy2D(out, sizeof(double) * gs.M, w.Lpsf, sizeof(double) * w.ldL, sizeof(double) * gs.M, rows,
                     cudaMemcpyDeviceToHost), "d2h");
     return QLP_OK;
 }

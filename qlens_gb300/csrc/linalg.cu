@@ -203,9 +203,17 @@ void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regpara
 }
 
 // ---- Cholesky, log det and solve: the templates of chol.cuh in FP64 ----
-int launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, cudaStream_t st)
+// Attributes are per translation unit: each .cu has its own instance of a
+// kernel template, so mixed.cu sets those of its float instances itself.
+void linalg_init_attributes()
 {
-    return launch_cholesky_t<double>(A, ld, M_max, gs, which, st);
+    solve_init_attributes<double>();
+}
+
+
+int launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, double* linv, cudaStream_t st)
+{
+    return launch_cholesky_t<double>(A, ld, M_max, gs, which, st, linv);
 }
 
 void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st)
@@ -218,7 +226,7 @@ void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaS
 void launch_solve_fp64(Work& w, int M_max, cudaStream_t st)
 {
     (void)M_max;
-    k_solve_t<double><<<1, 1024, 0, st>>>(w.F, w.ldF, w.gs, w.D, w.s, w.tmp);
+    k_solve_t<double><<<1, 1024, solve_smem_bytes<double>(w.ldF), st>>>(w.F, w.ldF, w.linv, w.gs, w.D, w.s, w.ldF);
     count_launches(1);
 }
 
@@ -303,10 +311,10 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd, SrcOpts so, const
 }
 
 void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max, double regparam,
-                       cudaStream_t st)
+                       cudaStream_t st, bool model_ready)
 {
     (void)M_max;
-    if (N_max > 0) {
+    if (N_max > 0 && !model_ready) {
         int blocks = (N_max + 7) / 8;
         if (blocks > 152 * 16) blocks = 152 * 16;
         k_model<<<blocks, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.s, w.model);

@@ -1,14 +1,17 @@
 // mixed.cu -- mixed-precision inversion: TF32 tensor-core SYRK (3xTF32 split),
 // FP32 Cholesky of F and R, FP64 log det accumulation and FP64 iterative
-// refinement of the source amplitudes with residuals from the FP64 L'.
+// refinement of the source amplitudes.
 //
-//   X      = (L' * sqrt(C^-1))^T split into TF32 hi + lo        k_convert_x
+//   L'32   = P L accumulated in FP32 (psf.cu)                   only feeds F
+//   X      = (L'32 * sqrt(C^-1))^T split into TF32 hi + lo      k_convert_x
 //   F32    = X X^T on tcgen05 (block-sparse over pixel blocks)   k_syrk_tc
 //   F32   += lambda R, R32 = R                                  k_reg32
 //   L_F L_F^T = F32, L_R L_R^T = R32 (FP32 blocked Cholesky)    chol.cuh
 //   log det F, log det R: 2 sum log diag, accumulated in FP64
-//   s = F32^-1 D, then twice: r = D - L'^T C^-1 L' s - lambda R s (FP64),
+//   D = L^T P^T (C^-1 d)                     (FP64, sparseops.cu)
+//   s = F32^-1 D, then twice: r = D - L^T P^T C^-1 P L s - lambda R s (FP64),
 //                              s += F32^-1 r
+//   model = P L s                             (FP64, for chi^2)
 // The plain FP64 path (linalg.cu) computes the same quantities entirely in
 // FP64; the mixed path's deviation from it is measured by the tests.
 #include <cuda.h>
@@ -20,6 +23,8 @@
 namespace qlpix {
 
 struct MixedWork {
+    float* L32 = nullptr;    // N_cap x ld32 PSF-convolved L, FP32
+    double* t = nullptr;     // N (image-plane scratch)
     float* X_hi = nullptr;
     float* X_lo = nullptr;
     int K_cap = 0;           // columns of X (image pixels), multiple of 32
@@ -35,11 +40,13 @@ struct MixedWork {
     double* z = nullptr;     // M
     double* y = nullptr;     // M (solve scratch)
     double* part = nullptr;
+    float* linvF = nullptr;  // inverses of the 64x64 diagonal Cholesky blocks
+    float* linvR = nullptr;
     CUtensorMap map_hi, map_lo;
     bool ready = false;
 };
 
-static MixedWork* mw_of(qlp_ctx* c);
+static MixedWork* mw_of(Slot& s) { return reinterpret_cast<MixedWork*>(s.mixed); }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -83,7 +90,7 @@ __device__ __forceinline__ float to_tf32(float f)
     return __uint_as_float(u);
 }
 
-__global__ void __launch_bounds__(256) k_convert_x(const GridState* __restrict__ gs, const double* __restrict__ L,
+__global__ void __launch_bounds__(256) k_convert_x(const GridState* __restrict__ gs, const float* __restrict__ L,
                                                    int ldL, const double* __restrict__ cvec, float* __restrict__ Xh,
                                                    float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
                                                    int nkb_cap)
@@ -96,16 +103,19 @@ __global__ void __launch_bounds__(256) k_convert_x(const GridState* __restrict__
     const int p0 = blockIdx.x * 32, a0 = blockIdx.y * 32;
     if (p0 >= Np || a0 >= Mp) return;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    __shared__ float sq[32];
+    if (threadIdx.x < 32) sq[threadIdx.x] = (p0 + threadIdx.x < N) ? (float)sqrt(cvec[p0 + threadIdx.x]) : 0.0f;
+    __syncthreads();
     bool any = false;
     for (int k = ty; k < 32; k += 8) {
         const int p = p0 + k, a = a0 + tx;
-        double x = 0;
-        if (p < N && a < M) x = L[(size_t)p * ldL + a] * sqrt(cvec[p]);
-        const float h = to_tf32((float)x);
-        const float l = to_tf32((float)(x - (double)h));
+        float x = 0;
+        if (p < N && a < M) x = L[(size_t)p * ldL + a] * sq[k];
+        const float h = to_tf32(x);
+        const float l = to_tf32(x - h);   // exact: h is x rounded to fewer bits
         th[k][tx] = h;
         tl[k][tx] = l;
-        any |= (x != 0.0);
+        any |= (x != 0.0f);
     }
     __syncthreads();
     for (int k = ty; k < 32; k += 8) {
@@ -182,50 +192,17 @@ __global__ void k_axpy(const GridState* __restrict__ gs, const double* __restric
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Mp; i += gridDim.x * blockDim.x) s[i] += z[i];
 }
 
-// u = L' s (one warp per row)
-__global__ void __launch_bounds__(256) k_gemv_rows(const GridState* __restrict__ gs, const double* __restrict__ L,
-                                                   int ldL, const double* __restrict__ s, double* __restrict__ u)
-{
-    const int N = gs->N, M = gs->M;
-    const int lane = threadIdx.x & 31;
-    for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < N; r += gridDim.x * (blockDim.x >> 5)) {
-        const double* row = L + (size_t)r * ldL;
-        double acc = 0;
-        for (int c = lane; c < M; c += 32) acc += row[c] * s[c];
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) u[r] = acc;
-    }
-}
-
-#define RC_CHUNK 256
-// partial[chunk][col] = sum_{rows in chunk} L'[row][col] c[row] u[row]
-__global__ void k_gemv_cols_partial(const GridState* __restrict__ gs, const double* __restrict__ L, int ldL,
-                                    const double* __restrict__ u, const double* __restrict__ cvec,
-                                    double* __restrict__ part, int M_cap)
-{
-    const int N = gs->N, M = gs->M;
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r0 = blockIdx.y * RC_CHUNK;
-    if (col >= M || r0 >= N) return;
-    const int r1 = min(r0 + RC_CHUNK, N);
-    double acc = 0;
-    for (int r = r0; r < r1; r++) acc += L[(size_t)r * ldL + col] * (cvec[r] * u[r]);
-    part[(size_t)blockIdx.y * M_cap + col] = acc;
-}
-
-// r = D - sum_chunks partial - lambda R s   (R applied by its stencil)
+// r = D - v - lambda R s   (v = L'^T C^-1 L' s; R applied by its stencil)
 __global__ void k_residual(const GridState* __restrict__ gs, const double* __restrict__ D,
-                           const double* __restrict__ part, int M_cap, const int* __restrict__ ai, int snx, int sny,
+                           const double* __restrict__ vv, const int* __restrict__ ai, int snx, int sny,
                            double regparam, int do_reg, const double* __restrict__ s, double* __restrict__ r)
 {
-    const int N = gs->N, M = gs->M;
+    const int M = gs->M;
     const int ncell = snx * sny;
-    const int nch = (N + RC_CHUNK - 1) / RC_CHUNK;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
         const int a = ai[c];
         if (a < 0) continue;
-        double v = 0;
-        for (int k = 0; k < nch; k++) v += part[(size_t)k * M_cap + a];
+        const double v = vv[a];
         double rs = 0;
         if (do_reg) {
             const int ci = c % snx, cj = c / snx;
@@ -246,27 +223,26 @@ __global__ void k_residual(const GridState* __restrict__ gs, const double* __res
 }
 
 // ---------------------------------------------------------------------------
-static MixedWork* mw_of(qlp_ctx* c) { return reinterpret_cast<MixedWork*>(c->mixed); }
-
-void mixed_free(qlp_ctx* c)
+void mixed_free(Slot& c)
 {
     MixedWork* m = mw_of(c);
     if (!m) return;
-    void* ptrs[] = {m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part};
+    void* ptrs[] = {m->L32, m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
+                    m->linvF, m->linvR};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
-    c->mixed = nullptr;
+    c.mixed = nullptr;
 }
 
-int mixed_init(qlp_ctx* c)
+int mixed_init(Slot& c)
 {
     MixedWork* m = mw_of(c);
-    const int M_cap = (c->M_cap + TC_TILE - 1) / TC_TILE * TC_TILE;
-    const int K_cap = (c->N_cap + TC_KB - 1) / TC_KB * TC_KB + TC_KB;
+    const int M_cap = (c.M_cap + TC_TILE - 1) / TC_TILE * TC_TILE;
+    const int K_cap = (c.N_cap + TC_KB - 1) / TC_KB * TC_KB + TC_KB;
     if (m && m->ready && m->M_cap >= M_cap && m->K_cap >= K_cap) return QLP_OK;
     mixed_free(c);
     m = new MixedWork();
-    c->mixed = m;
+    c.mixed = m;
     m->M_cap = M_cap;
     m->K_cap = K_cap;
     m->nkb_cap = K_cap / TC_KB;
@@ -278,12 +254,16 @@ int mixed_init(qlp_ctx* c)
     A((void**)&m->nz, (size_t)(M_cap / TC_TILE) * m->nkb_cap);
     A((void**)&m->F32, sizeof(float) * (size_t)M_cap * M_cap);
     A((void**)&m->R32, sizeof(float) * (size_t)M_cap * M_cap);
-    A((void**)&m->u, sizeof(double) * (size_t)(c->N_cap + 64));
+    A((void**)&m->L32, sizeof(float) * (size_t)c.N_cap * M_cap);
+    A((void**)&m->t, sizeof(double) * (size_t)(c.N_cap + 64));
+    A((void**)&m->u, sizeof(double) * (size_t)(c.N_cap + 64));
     A((void**)&m->v, sizeof(double) * M_cap);
     A((void**)&m->r, sizeof(double) * M_cap);
     A((void**)&m->z, sizeof(double) * M_cap);
     A((void**)&m->y, sizeof(double) * M_cap);
-    A((void**)&m->part, sizeof(double) * (size_t)M_cap * ((c->N_cap + RC_CHUNK - 1) / RC_CHUNK + 1));
+    A((void**)&m->part, sizeof(double) * (size_t)M_cap * (ltw_chunks(c.N_cap) + 1));
+    A((void**)&m->linvF, sizeof(float) * (size_t)M_cap * 64);
+    A((void**)&m->linvR, sizeof(float) * (size_t)M_cap * 64);
     if (e != cudaSuccess) {
         set_error("%s (%d)", "mixed-precision workspace allocation failed", (int)e);
         return QLP_ERR_NOMEM;
@@ -295,28 +275,31 @@ int mixed_init(qlp_ctx* c)
         return QLP_ERR_CUDA;
     }
     cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    solve_init_attributes<float>();
     m->ready = true;
     return QLP_OK;
 }
 
-int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st, cudaEvent_t* ev)
+int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, double regparam, cudaStream_t st,
+                        cudaEvent_t* ev)
 {
-    int rc = mixed_init(c);
+    int rc = mixed_init(slot);
     if (rc != QLP_OK) return rc;
-    MixedWork* m = mw_of(c);
-    Work& w = c->w;
-    const SrcOpts& so = c->so;
-    const int N_cap = c->N_cap;
-    const int Mc = c->M_cap;
+    MixedWork* m = mw_of(slot);
+    Work& w = slot.w;
+    const int N_cap = sd.n_mask;
+    const int Mc = slot.M_cap;
     int n = 0;
 
-    // D = L'^T C^-1 d (FP64)
-    launch_D(w, c->sd.n_mask, Mc, st);
-    // X, flags
+    // D = L^T P^T (C^-1 d), FP64
+    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, st);
+    op_LTw(w, N_cap, m->M_cap, m->t, m->part, w.D, st);
+    // L'32, then X and the block flags
+    launch_psf32(sd, w, m->L32, m->ld32, m->M_cap, st);
     cudaMemsetAsync(m->nz, 0, (size_t)(m->M_cap / TC_TILE) * m->nkb_cap, st);
     {
         dim3 g(m->K_cap / 32, m->M_cap / 32);
-        k_convert_x<<<g, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.cvec, m->X_hi, m->X_lo, m->K_cap, m->nz, m->nkb_cap);
+        k_convert_x<<<g, 256, 0, st>>>(w.gs, m->L32, m->ld32, w.cvec, m->X_hi, m->X_lo, m->K_cap, m->nz, m->nkb_cap);
         n++;
     }
     if (ev) cudaEventRecord(ev[3], st);
@@ -332,11 +315,11 @@ int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st, cudaEvent_
                                                                 m->F32, m->R32, m->ld32, so.regularization);
     n++;
     if (so.regularization) {
-        n += launch_cholesky_t<float>(m->R32, m->ld32, Mc, w.gs, 1, st);
+        n += launch_cholesky_t<float>(m->R32, m->ld32, Mc, w.gs, 1, st, m->linvR);
         k_logdet_t<float><<<1, 1024, 0, st>>>(m->R32, m->ld32, w.gs, w.out, 1);
         n++;
     }
-    n += launch_cholesky_t<float>(m->F32, m->ld32, Mc, w.gs, 0, st);
+    n += launch_cholesky_t<float>(m->F32, m->ld32, Mc, w.gs, 0, st, m->linvF);
     k_logdet_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, w.out, 0);
     n++;
     // s = F^-1 D with two FP64 refinement sweeps
@@ -344,19 +327,22 @@ int run_inversion_mixed(qlp_ctx* c, double regparam, cudaStream_t st, cudaEvent_
     n++;
     const int refine = 2;
     for (int it = 0; it <= refine; it++) {
-        k_solve_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, m->r, m->z, m->y);
+        k_solve_t<float><<<1, 1024, solve_smem_bytes<float>(Mc), st>>>(m->F32, m->ld32, m->linvF, w.gs, m->r, m->z,
+                                                                      Mc);
         k_axpy<<<(Mc + 255) / 256, 256, 0, st>>>(w.gs, m->z, w.s);
         n += 2;
         if (it == refine) break;
-        int blocks = (N_cap + 7) / 8;
-        if (blocks > 152 * 16) blocks = 152 * 16;
-        k_gemv_rows<<<blocks, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.s, m->u);
-        dim3 g((Mc + 127) / 128, (N_cap + RC_CHUNK - 1) / RC_CHUNK);
-        k_gemv_cols_partial<<<g, 128, 0, st>>>(w.gs, w.Lpsf, w.ldL, m->u, w.cvec, m->part, m->M_cap);
-        k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->part, m->M_cap, w.active_index, so.snx,
-                                                                  so.sny, regparam, so.regularization, w.s, m->r);
-        n += 3;
+        op_Ls(w, N_cap, w.s, m->t, st);
+        op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, st);
+        op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, st);
+        op_LTw(w, N_cap, m->M_cap, m->t, m->part, m->v, st);
+        k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, so.snx, so.sny,
+                                                                  regparam, so.regularization, w.s, m->r);
+        n++;
     }
+    // model image P L s in FP64 for chi^2
+    op_Ls(w, N_cap, w.s, m->t, st);
+    op_conv(sd, w, N_cap, false, m->t, nullptr, w.model, st);
     count_launches(n);
     return QLP_OK;
 }

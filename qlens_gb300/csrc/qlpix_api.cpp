@@ -177,6 +177,13 @@ int qlp_set_lens_model(qlp_ctx* c, const qlp_lens* lenses, int nlens, const qlp_
     return QLP_OK;
 }
 
+int qlp_set_batch_slots(qlp_ctx* c, int slots)
+{
+    if (!c || slots < 1 || slots > QLP_MAX_SLOTS) return fail(QLP_ERR_ARG, "bad slot count");
+    c->max_slots = slots;
+    return QLP_OK;
+}
+
 int qlp_n_params(const qlp_ctx* c)
 {
     if (!c) return 0;

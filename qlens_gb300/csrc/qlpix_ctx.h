@@ -6,12 +6,34 @@
 #include "qlpix_internal.h"
 
 #define QLP_N_STAGES 6
+#define QLP_MAX_SLOTS 32
+
+namespace qlpix {
+
+// One evaluation lane: a stream and the full per-evaluation workspace.  A
+// batch spreads its instances over several slots so that the sequential
+// parts of one evaluation (Cholesky pivots, triangular solves) overlap the
+// parallel parts of others.
+struct Slot {
+    cudaStream_t stream = nullptr;
+    Work w{};
+    void* mixed = nullptr;          // mixed-precision workspace (mixed.cu)
+    int M_cap = 0;                  // capacity in source cells (multiple of 64)
+    int N_cap = 0;                  // capacity in masked pixels
+    int nsub_cap = 0;
+    int snx_cap = 0, sny_cap = 0;
+    bool fp64_mats = false;         // F and R in FP64 allocated
+    cudaEvent_t done = nullptr;
+};
+
+}  // namespace qlpix
 
 struct qlp_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int precision = QLP_FP64;
+    int max_slots = 16;
 
     // lens model
     std::vector<qlp_lens> lenses;
@@ -33,18 +55,17 @@ struct qlp_ctx {
     // extra masks for batched evaluation (device mpix lists, concatenated)
     std::vector<int> mask_off, mask_cnt;
     int* d_inst_mpix = nullptr;
-    int max_inst_src = 0;                 // largest source grid requested by a batch (cells)
 
     qlpix::StaticData sd{};
     qlpix::SrcOpts so{};
-    qlpix::Work w{};
-    int M_cap = 0;                        // workspace capacity in source cells (multiple of 64)
-    int N_cap = 0;                        // workspace capacity in masked pixels
-    int nsub_cap = 0;
+    std::vector<qlpix::Slot> slots;       // slots[0] serves qlp_eval
 
-    void* mixed = nullptr;                // mixed-precision workspace (mixed.cu)
-    qlpix::EvalOut* h_out = nullptr;      // pinned
+    qlpix::EvalOut* h_out = nullptr;      // pinned, one per batch instance
+    int h_out_cap = 0;
+    qlpix::EvalOut* d_res = nullptr;
+    int d_res_cap = 0;
     cudaEvent_t ev[QLP_N_STAGES + 1] = {};
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<cudaEvent_t> ev_pool;     // (QLP_N_STAGES+1) per batched instance
     float stage_ms[QLP_N_STAGES] = {};
     float device_ms = 0;
@@ -64,4 +85,9 @@ int ctx_dump_Lpsf(qlp_ctx* c, int rows, double* out);
 int make_lens_rec(LensRec& L, int type, int plane, const double* p);
 int n_params_of(int type);
 void set_error(const char* fmt, const char* a, int code);
+// mixed.cu
+int mixed_init(Slot& slot);
+void mixed_free(Slot& slot);
+int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, double regparam, cudaStream_t st,
+                        cudaEvent_t* ev);
 }  // namespace qlpix

@@ -97,6 +97,7 @@ struct Work {
     double* s;   double* tmp;          // M
     double* model;                     // N
     double* partial;                   // reduction scratch
+    double* linv;                      // 64x64 inverse of the current diagonal Cholesky block
     GridState* gs;
     EvalOut* out;
 };
@@ -107,16 +108,24 @@ void launch_grid(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t 
 void launch_locate(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_build_L(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
+void launch_rowpix(const StaticData& sd, Work& w, cudaStream_t st);
 void launch_psf(const StaticData& sd, const SrcOpts& so, Work& w, int M_max, cudaStream_t st);
+void launch_psf32(const StaticData& sd, Work& w, float* out, int ld, int M_max, cudaStream_t st);
+void op_Ls(Work& w, int N_cap, const double* s, double* t, cudaStream_t st);
+void op_conv(const StaticData& sd, Work& w, int N_cap, bool transpose, const double* in, const double* scale_in,
+             double* out, cudaStream_t st);
+void op_LTw(Work& w, int N_cap, int M_cap, const double* v, double* part, double* out, cudaStream_t st);
+int ltw_chunks(int N_cap);
 void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st);
 void launch_D(Work& w, int N_max, int M_max, cudaStream_t st);
 void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st);
 void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regparam, cudaStream_t st);
-int  launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, cudaStream_t st);
+int  launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, double* linv,
+                          cudaStream_t st);
 void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st);
 void launch_solve_fp64(Work& w, int M_max, cudaStream_t st);
 void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max,
-                       double regparam, cudaStream_t st);
+                       double regparam, cudaStream_t st, bool model_ready = false);
 void init_kernel_attributes();
 long long kernel_launch_counter();
 void count_launches(int n);

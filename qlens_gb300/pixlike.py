@@ -48,6 +48,7 @@ def load_library(build_if_missing=False):
     L.qlp_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     L.qlp_eval.argtypes = [C.c_void_p, P(C.c_double), C.c_double, P(abi.qlp_result)]
     L.qlp_n_params.argtypes = [C.c_void_p]
+    L.qlp_set_batch_slots.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_instance_masks.argtypes = [C.c_void_p, P(C.c_ubyte), C.c_int]
     L.qlp_eval_batch.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(abi.qlp_instance), C.c_int,
                                  P(abi.qlp_result)]
@@ -153,6 +154,9 @@ class PixelLikelihood:
 
     def set_stream(self, stream_ptr):
         self._check(self.lib.qlp_set_stream(self.ctx, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def set_batch_slots(self, n):
+        self._check(self.lib.qlp_set_batch_slots(self.ctx, int(n)))
 
     def set_lens_model(self, spec, zfac=None, beta=None):
         self.lens_spec = spec
