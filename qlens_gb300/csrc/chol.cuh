@@ -89,6 +89,123 @@ __global__ void __launch_bounds__(256) k_potrf_t(T* __restrict__ A, int ld, int 
     for (int idx = threadIdx.x; idx < CB * CB; idx += blockDim.x) Lk[idx] = X[idx / CB][idx % CB];
 }
 
+// ---------------------------------------------------------------------------
+// FP32 kernels with the factor rows in registers.
+// ---------------------------------------------------------------------------
+
+// One warp factors the 64x64 diagonal tile: lane l holds rows l and l+32 in
+// registers; pivot and column values travel by shuffle.  Fully unrolled.
+static __global__ void __launch_bounds__(32) k_potrf_warp(float* __restrict__ A, int ld, int k, GridState* gs, int which)
+{
+    const int nblk = cpad64(gs->M) / CB;
+    if (k >= nblk) return;
+    const int o = k * CB;
+    const int lane = threadIdx.x;
+    float a0[CB], a1[CB];
+    const float* r0 = A + (size_t)(o + lane) * ld + o;
+    const float* r1 = A + (size_t)(o + lane + 32) * ld + o;
+    #pragma unroll
+    for (int c = 0; c < CB; c++) {
+        a0[c] = (c <= lane) ? r0[c] : 0.f;
+        a1[c] = (c <= lane + 32) ? r1[c] : 0.f;
+    }
+    #pragma unroll
+    for (int j = 0; j < CB; j++) {
+        const float dv = __shfl_sync(0xffffffffu, (j < 32) ? a0[j] : a1[j], j & 31);
+        if (lane == 0 && dv < 0.f) {
+            int* flag = which ? &gs->not_spd_R : &gs->not_spd_F;
+            if (*flag == 0) *flag = o + j + 1;
+        }
+        const float sd = sqrtf(fabsf(dv));
+        const float rinv = 1.0f / sd;
+        if (j < 32) {
+            if (lane > j) a0[j] *= rinv;
+            else if (lane == j) a0[j] = sd;
+        }
+        if (lane + 32 > j) a1[j] *= rinv;
+        else if (lane + 32 == j) a1[j] = sd;
+        #pragma unroll
+        for (int c = j + 1; c < CB; c++) {
+            const float vc = __shfl_sync(0xffffffffu, (c < 32) ? a0[j] : a1[j], c & 31);
+            if (c < 32 && c <= lane) a0[c] -= a0[j] * vc;
+            if (c <= lane + 32) a1[c] -= a1[j] * vc;
+        }
+    }
+    float* w0 = A + (size_t)(o + lane) * ld + o;
+    float* w1 = A + (size_t)(o + lane + 32) * ld + o;
+    #pragma unroll
+    for (int c = 0; c < CB; c++) {
+        if (c <= lane) w0[c] = a0[c];
+        if (c <= lane + 32) w1[c] = a1[c];
+    }
+}
+
+// Tiles below the diagonal: X L_kk^T = A_ik by forward substitution, one
+// thread per row of the tile with the row in registers, L_kk in shared memory.
+static __global__ void __launch_bounds__(CB) k_trsm_rows(float* __restrict__ A, int ld, int k, const GridState* __restrict__ gs)
+{
+    __shared__ float Lk[CB][CB + 1];
+    const int nblk = cpad64(gs->M) / CB;
+    const int i = k + 1 + blockIdx.x;
+    if (i >= nblk) return;
+    const int o = k * CB, ro = i * CB;
+    for (int idx = threadIdx.x; idx < CB * CB; idx += blockDim.x) {
+        const int r = idx / CB, c = idx % CB;
+        Lk[r][c] = (c <= r) ? A[(size_t)(o + r) * ld + o + c] : 0.f;
+    }
+    float x[CB];
+    float* row = A + (size_t)(ro + threadIdx.x) * ld + o;
+    #pragma unroll
+    for (int c = 0; c < CB; c++) x[c] = row[c];
+    __syncthreads();
+    #pragma unroll
+    for (int c = 0; c < CB; c++) {
+        float a0 = x[c], a1 = 0.f, a2 = 0.f, a3 = 0.f;   // four independent chains
+        #pragma unroll
+        for (int m = 0; m + 3 < c; m += 4) {
+            a0 -= x[m] * Lk[c][m];
+            a1 -= x[m + 1] * Lk[c][m + 1];
+            a2 -= x[m + 2] * Lk[c][m + 2];
+            a3 -= x[m + 3] * Lk[c][m + 3];
+        }
+        #pragma unroll
+        for (int m = c & ~3; m < c; m++) a0 -= x[m] * Lk[c][m];
+        x[c] = ((a0 + a1) + (a2 + a3)) / Lk[c][c];
+    }
+    #pragma unroll
+    for (int c = 0; c < CB; c++) row[c] = x[c];
+}
+
+// Inverses of all diagonal factors at once (after the factorisation, off its
+// critical path): thread t of block k computes column t of L_kk^-1.
+template <typename T>
+__global__ void __launch_bounds__(CB) k_diag_inverse(const T* __restrict__ A, int ld, const GridState* __restrict__ gs,
+                                                     T* __restrict__ Linv)
+{
+    __shared__ T Lk[CB][CB + 1];
+    const int nblk = cpad64(gs->M) / CB;
+    const int k = blockIdx.x;
+    if (k >= nblk) return;
+    const int o = k * CB;
+    for (int idx = threadIdx.x; idx < CB * CB; idx += blockDim.x) {
+        const int r = idx / CB, c = idx % CB;
+        Lk[r][c] = (c <= r) ? A[(size_t)(o + r) * ld + o + c] : T(0);
+    }
+    __syncthreads();
+    const int t = threadIdx.x;
+    T x[CB];
+    #pragma unroll
+    for (int i = 0; i < CB; i++) {
+        T acc = (i == t) ? T(1) : T(0);
+        #pragma unroll
+        for (int m = 0; m < i; m++) acc -= Lk[i][m] * x[m];
+        x[i] = (i < t) ? T(0) : acc / Lk[i][i];
+    }
+    T* Lo = Linv + (size_t)k * CB * CB;
+    #pragma unroll
+    for (int i = 0; i < CB; i++) Lo[i * CB + t] = x[i];
+}
+
 // Tiles below the diagonal: X = A_ik L_kk^-T = A_ik Linv^T, a 64x64x64 GEMM
 // per block row (the triangular solve through the explicit inverse of the
 // small diagonal factor, as blocked GPU Cholesky codes commonly do).
@@ -353,6 +470,28 @@ template <typename T>
 void solve_init_attributes()
 {
     cudaFuncSetAttribute(k_solve_t<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+// FP32 blocked Cholesky with the register kernels, then the diagonal inverses.
+inline int launch_cholesky_f32(float* A, int ld, int M_cap, const GridState* gs, int which, cudaStream_t st,
+                               float* Linv)
+{
+    const int nbm = (M_cap + CB - 1) / CB;
+    int n = 0;
+    for (int k = 0; k < nbm; k++) {
+        const int rem = nbm - k - 1;
+        k_potrf_warp<<<1, 32, 0, st>>>(A, ld, k, const_cast<GridState*>(gs), which);
+        n++;
+        if (rem > 0) {
+            k_trsm_rows<<<rem, CB, 0, st>>>(A, ld, k, gs);
+            k_chol_update_t<float><<<rem * (rem + 1) / 2, 256, 0, st>>>(A, ld, k, gs);
+            n += 2;
+        }
+    }
+    k_diag_inverse<float><<<nbm, CB, 0, st>>>(A, ld, gs, Linv);
+    n++;
+    count_launches(n);
+    return n;
 }
 
 }  // namespace qlpix

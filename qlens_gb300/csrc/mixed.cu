@@ -275,9 +275,34 @@ int mixed_init(Slot& c)
         return QLP_ERR_CUDA;
     }
     cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    cudaFuncSetAttribute(k_chol_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM);
     solve_init_attributes<float>();
     m->ready = true;
     return QLP_OK;
+}
+
+// FP32 blocked Cholesky for the mixed path: shared-memory potrf of each 64x64
+// diagonal tile, per-row triangular solve of the tiles below it, the trailing
+// update on the tensor cores, then all diagonal inverses in one launch.
+static int cholesky_mixed(float* A, int ld, int M_cap, GridState* gs, int which, cudaStream_t st, float* Linv)
+{
+    const int nbm = (M_cap + CB - 1) / CB;
+    int n = 0;
+    for (int k = 0; k < nbm; k++) {
+        const int rem = nbm - k - 1;
+        k_potrf_t<float><<<1, 256, 0, st>>>(A, ld, k, gs, which, nullptr);
+        n++;
+        if (rem > 0) {
+            k_trsm_rows<<<rem, CB, 0, st>>>(A, ld, k, gs);
+            const int nt = (rem * CB + TC_TILE - 1) / TC_TILE;
+            k_chol_update_tc<<<nt * (nt + 1) / 2, 128, UPD_SMEM, st>>>(A, ld, k, gs);
+            n += 2;
+        }
+    }
+    k_diag_inverse<float><<<nbm, CB, 0, st>>>(A, ld, gs, Linv);
+    n++;
+    count_launches(n);
+    return n;
 }
 
 int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, double regparam, cudaStream_t st,
@@ -315,11 +340,11 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, dou
                                                                 m->F32, m->R32, m->ld32, so.regularization);
     n++;
     if (so.regularization) {
-        n += launch_cholesky_t<float>(m->R32, m->ld32, Mc, w.gs, 1, st, m->linvR);
+        n += cholesky_mixed(m->R32, m->ld32, Mc, w.gs, 1, st, m->linvR);
         k_logdet_t<float><<<1, 1024, 0, st>>>(m->R32, m->ld32, w.gs, w.out, 1);
         n++;
     }
-    n += launch_cholesky_t<float>(m->F32, m->ld32, Mc, w.gs, 0, st, m->linvF);
+    n += cholesky_mixed(m->F32, m->ld32, Mc, w.gs, 0, st, m->linvF);
     k_logdet_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, w.out, 0);
     n++;
     // s = F^-1 D with two FP64 refinement sweeps
