@@ -199,6 +199,25 @@ int qlp_last_device_time(qlp_ctx* ctx, float* ms);
 /* Number of kernel launches issued by the last qlp_eval / qlp_eval_batch. */
 long long qlp_last_launch_count(const qlp_ctx* ctx);
 
+/* No counterpart in the reference (QLens allocates its matrices on every
+ * call).  For callers that cannot call cudaMalloc -- a host application that
+ * owns the GPU memory budget and only hands this library buffers it already
+ * allocated, or a latency-critical loop that cannot afford the implicit
+ * synchronisation of cudaMalloc/cudaFree -- this factors an SPD matrix
+ * without allocating anything: F (n x n, row-major, leading dimension ld,
+ * lower triangle read), D (n) and the outputs s (n) = F^-1 D and logdet
+ * (1 double, = log det F) are caller-owned DEVICE buffers on the current
+ * device.  The only scratch is a static device array sized for
+ * n <= 512 (about 2.1 MB per GPU, held until the process exits); larger n
+ * returns QLP_ERR_ARG.  The first call on each device looks up that array's
+ * address, so make it before any stream capture.  The call runs on `stream`
+ * (cudaStream_t as void*, NULL = default stream) and waits for it; every
+ * call shares the one array, so calls that overlap on the GPU (other host
+ * threads, other streams) race -- serialise them.  Returns QLP_ERR_NOT_SPD
+ * if a pivot is not positive. */
+int qlp_spd_solve_logdet_noalloc(const double* F, int n, int ld, const double* D, double* s, double* logdet,
+                                 void* stream);
+
 /* Message of the last error on this thread ("" if none). */
 const char* qlp_last_error(void);
 

@@ -28,6 +28,7 @@ UNITS = [
     ("psf.cu", ["--fmad=false"]),
     ("linalg.cu", []),
     ("sparseops.cu", []),
+    ("noalloc.cu", []),
     ("mixed.cu", []),
     ("ctx.cpp", []),
     ("qlpix_api.cpp", []),

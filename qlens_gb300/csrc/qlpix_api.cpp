@@ -102,6 +102,11 @@ static cudaError_t dalloc(T** p, size_t n)
 
 }  // namespace qlpix
 
+namespace qlpix {
+int spd_solve_logdet_noalloc(const double* F, int n, int ld, const double* D, double* s, double* logdet,
+                             void* stream, std::string& err);
+}
+
 using namespace qlpix;
 
 static int fail(int code, const char* msg)
@@ -250,6 +255,15 @@ int qlp_last_device_time(qlp_ctx* c, float* ms)
     if (!c || !ms) return fail(QLP_ERR_ARG, "bad arguments");
     *ms = c->device_ms;
     return QLP_OK;
+}
+
+int qlp_spd_solve_logdet_noalloc(const double* F, int n, int ld, const double* D, double* s, double* logdet,
+                                 void* stream)
+{
+    std::string err;
+    int rc = spd_solve_logdet_noalloc(F, n, ld, D, s, logdet, stream, err);
+    if (rc != QLP_OK) t_err = err;
+    return rc;
 }
 
 void qlp_destroy(qlp_ctx* c)

@@ -59,6 +59,8 @@ def load_library(build_if_missing=False):
     L.qlp_last_device_time.argtypes = [C.c_void_p, P(C.c_float)]
     L.qlp_last_launch_count.restype = C.c_longlong
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
+    L.qlp_spd_solve_logdet_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p]
     L.qlp_last_error.restype = C.c_char_p
     L.qlp_destroy.argtypes = [C.c_void_p]
     _lib = L
