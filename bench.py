@@ -33,6 +33,9 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_syrk_tc launch on cfg2 (ncu, GB300)
+SYRK_TC_DRAM_BYTES_CFG2 = 118.647e6 + 6.535e6
+
 METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 at |ΔlogL|<0.1"
 UNIT = "evals/s"
 
@@ -90,6 +93,19 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def reduce_over_ranks(values, dist, device="cuda"):
+    """Slowest rank decides: element-wise max of the timing values over ranks."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_evals(batch, steps, world):
+    """Evaluations of the whole job: every rank evaluates its own batches."""
+    return batch * steps * world
 
 
 def make_context(wl, precision):
@@ -235,11 +251,9 @@ def main():
 
     # slowest rank decides
     if dist:
-        t = torch.tensor([dev_ms, wall, span_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms, wall, span_ms = t.tolist()
+        dev_ms, wall, span_ms = reduce_over_ranks([dev_ms, wall, span_ms], dist)
 
-    n_evals = B * args.steps * world
+    n_evals = whole_job_evals(B, args.steps, world)
     value = n_evals / (dev_ms / 1e3)
     e2e = n_evals / wall
     bad = [r for r in results if r["status"] != 0]
@@ -257,8 +271,10 @@ def main():
         peak = 1.25
         peak_note = "nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)"
         bound = "fp64"
+    # DRAM bytes of one k_syrk_tc launch on cfg2 from one ncu capture (profiles/k_syrk_tc_cfg2.md)
+    traffic = SYRK_TC_DRAM_BYTES_CFG2 if (precision == "mixed" and args.config == "cfg2") else None
     roofline = {"bound": bound, "kernel": "F = L'^T C^-1 L' (SYRK)", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_note, "algorithmic_flops_per_step": flops / args.steps}
 
     cpu = None
