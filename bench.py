@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_syrk_tc launch on cfg2 (ncu, GB300)
-SYRK_TC_DRAM_BYTES_CFG2 = 118.647e6 + 6.535e6
+SYRK_TC_DRAM_BYTES_CFG2 = 268.482e6 + 11.716e6
 
 METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 at |ΔlogL|<0.1"
 UNIT = "evals/s"
@@ -113,7 +113,7 @@ def make_context(wl, precision):
     prec = abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64
     pl = PixelLikelihood(wl.xvals, wl.yvals, wl.data, wl.mask, wl.psf, covinv=None, bg_noise=wl.noise,
                          nsplit=wl.nsplit, src_npixels=wl.src_npixels, regparam=wl.regparam, precision=prec)
-    pl.set_lens_model(wl.lenses)
+    pl.set_lens_model(wl.lenses, getattr(wl, "zfac", None), getattr(wl, "beta", None))
     return pl
 
 
@@ -137,7 +137,8 @@ def cpu_port_eval(wl, params, threads=None):
     o.npixels_x, o.npixels_y = wl.src_npixels
     o.regparam = wl.regparam
     t = time.perf_counter()
-    r = O.evaluate(img, psf, o, wl.lenses, lens_params=params)
+    planes = abi.make_planes(getattr(wl, "zfac", None), getattr(wl, "beta", None))
+    r = O.evaluate(img, psf, o, wl.lenses, lens_params=params, planes=planes)
     return time.perf_counter() - t, r
 
 
@@ -177,7 +178,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="qlpix", choices=["qlpix", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
     ap.add_argument("--batch", type=int, default=0, help="evaluations per step (default per precision)")
     ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])

@@ -20,6 +20,7 @@ SOURCES = [os.path.join(HERE, "qlpix_oracle.c"), os.path.join(HERE, "nfw_oracle.
 def build(force=False):
     """Compile the oracle with gcc (OpenMP, no fused multiply-adds)."""
     deps = SOURCES + [os.path.join(HERE, "qlpix_oracle.h"),
+                      os.path.join(os.path.dirname(HERE), "qlens_gb300", "csrc", "patterson_rule.h"),
                       os.path.join(os.path.dirname(HERE), "include", "qlpix.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB

@@ -54,6 +54,8 @@ GRAB(G_nsplits, ImagePixelGrid, int**, nsplits)
 GRAB(G_subsrc, ImagePixelGrid, lensvector***, subpixel_center_sourcepts)
 GRAB(G_act_i, ImagePixelGrid, int*, active_image_pixel_i)
 GRAB(G_act_j, ImagePixelGrid, int*, active_image_pixel_j)
+GRAB(G_zfac, ImagePixelGrid, double*, imggrid_zfactors)
+GRAB(G_beta, ImagePixelGrid, double**, imggrid_betafactors)
 
 static std::string g_out;
 
@@ -143,6 +145,20 @@ int main(int argc, char** argv)
 	sg->create_pixel_grid(&lens, sxmin, sxmax, symin, symax, snx, sny);
 	sg->set_image_pixel_grid(g);
 	lens.regparam_ptr = &(sg->regparam);
+	// lens-plane factors the image grid ray-traces with (lenscalc.cpp:81-113)
+	{
+		const int nz = lens.n_lens_redshifts;
+		double* zf = g->*grab(G_zfac());
+		double** bf = g->*grab(G_beta());
+		std::vector<double> zv, bv;
+		for (int i = 0; i < nz; i++) zv.push_back(zf ? zf[i] : 1.0);
+		for (int i = 1; i < nz; i++)
+			for (int j = 0; j < i; j++) bv.push_back(bf[i - 1][j]);
+		dumpd("zfactors", zv); dumpd("betafactors", bv);
+		std::vector<int> lp(lens.nlens);
+		for (int k = 0; k < lens.nlens; k++) lp[k] = lens.lens_redshift_idx[k];
+		dumpi("lens_plane", lp);
+	}
 	bool** in_mask = g->*grab(G_in_mask());
 	int** nsplits = g->*grab(G_nsplits());
 	lensvector*** subsrc = g->*grab(G_subsrc());

@@ -71,7 +71,9 @@ __device__ __forceinline__ void sple_deflection(const LensRec& L, double x, doub
 #include "nfw_device.cuh"
 namespace qlpix {
 
-// LensProfile::deflection (profile.cpp:1782-1805); Shear::deflection (models.cpp:2266-2272)
+// LensProfile::deflection (profile.cpp:1782-1805); Shear::deflection (models.cpp:2266-2272).
+// NFW = false compiles the kernel without the quadrature (no NFW lens in the model).
+template <bool NFW>
 __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
 {
     if (L.type == QLP_LENS_SHEAR) {
@@ -89,7 +91,7 @@ __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, doub
         x = xp;
     }
     double ax, ay;
-    if (L.type == QLP_LENS_SPLE) sple_deflection(L, x, y, ax, ay);
+    if (!NFW || L.type == QLP_LENS_SPLE) sple_deflection(L, x, y, ax, ay);
     else nfw_deflection(L, x, y, ax, ay);
     if (rot) {
         double xp = ax * L.costheta - ay * L.sintheta;
@@ -100,6 +102,7 @@ __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, doub
 }
 
 // QLens::deflection + QLens::find_sourcept (lenscalc.cpp:81-113, 325-330)
+template <bool NFW>
 __device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, double y, double& bx, double& by)
 {
     double defx = 0, defy = 0;
@@ -118,7 +121,7 @@ __device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, dou
             for (int k = 0; k < lm.nlens; k++) {
                 if (lm.lens[k].plane != i) continue;
                 double ax, ay;
-                lens_deflection(lm.lens[k], xi, yi, ax, ay);
+                lens_deflection<NFW>(lm.lens[k], xi, yi, ax, ay);
                 dsx[i] += ax; dsy[i] += ay;
             }
             dsx[i] *= lm.zfac[i];

@@ -13,6 +13,7 @@
 
 namespace qlpix {
 
+template <bool NFW>
 __global__ void __launch_bounds__(256) k_raytrace(StaticData sd, LensModel lm, double* __restrict__ spx,
                                                   double* __restrict__ spy)
 {
@@ -27,7 +28,7 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd, LensModel lm, d
         double px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
         double py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
         double bx, by;
-        find_sourcept(lm, px, py, bx, by);
+        find_sourcept<NFW>(lm, px, py, bx, by);
         spx[t] = bx;
         spy[t] = by;
     }
@@ -37,7 +38,10 @@ void launch_raytrace(const StaticData& sd, const LensModel& lm, Work& w, cudaStr
 {
     if (sd.n_sub == 0) return;
     int blocks = (sd.n_sub + 255) / 256;
-    k_raytrace<<<blocks, 256, 0, st>>>(sd, lm, w.spx, w.spy);
+    bool nfw = false;
+    for (int k = 0; k < lm.nlens; k++) nfw |= (lm.lens[k].type == QLP_LENS_NFW);
+    if (nfw) k_raytrace<true><<<blocks, 256, 0, st>>>(sd, lm, w.spx, w.spy);
+    else k_raytrace<false><<<blocks, 256, 0, st>>>(sd, lm, w.spx, w.spy);
     count_launches(1);
 }
 

@@ -11,6 +11,11 @@ mask, split factor, PSF size, source-grid size -- follow the configurations:
         power law alpha in [0.9,1.2], b in [1,1.5], q in [0.6,0.95], shear in [0,0.1], sigma 0.01
   cfg3  100x100 @ 0.05", per-instance circle r in [1.5,3.0]", 2x2 split, 11x11 Gaussian PSF,
         source side in [20,64], SIE+shear (b,q,phi,x0,y0,gamma,phi_gamma) + log lambda
+  cfg4  200x200 @ 0.04", r < 4.5" (the whole frame), 4x4 split (~640k rays), 21x21 Airy-like PSF,
+        48x48 source, SIE host + elliptical NFW ks in [0.05,0.5], rs in [2,20]", q in [0.5,1]
+  cfg5  300x300 @ 0.03", annulus 0.3"-3.5", 4x4 split, 31x31 Airy-like PSF, 48x48 source; two lens
+        planes: SIE + shear at z=0.5, NFW subhalo (ks in [0.05,0.3], rs in [0.05,0.3]") at z=0.8,
+        source at z=2 (plane factors: the reference's own for those redshifts)
 """
 import math
 
@@ -113,7 +118,7 @@ class Workload:
     """Everything needed to construct a PixelLikelihood and draw parameters."""
 
     def __init__(self, name, xvals, yvals, data, mask, psf, noise, nsplit, src_npixels, lenses, regparam,
-                 draw, instance_masks=None, instance_src=None):
+                 draw, instance_masks=None, instance_src=None, zfac=None, beta=None):
         self.name = name
         self.xvals, self.yvals, self.data, self.mask, self.psf = xvals, yvals, data, mask, psf
         self.noise = noise
@@ -124,6 +129,7 @@ class Workload:
         self.draw = draw
         self.instance_masks = instance_masks
         self.instance_src = instance_src
+        self.zfac, self.beta = zfac, beta
 
     @property
     def n_mask(self):
@@ -213,4 +219,71 @@ def cfg3(seed=3, n_instances=64):
                     instance_masks=masks, instance_src=np.stack([sides, sides], 1))
 
 
-CONFIGS = {"cfg1": cfg1, "cfg2": cfg2, "cfg3": cfg3}
+def cfg4(seed=4):
+    xv = pixel_corners(200, -4.0, 4.0)
+    yv = pixel_corners(200, -4.0, 4.0)
+    psf = airy_psf(21, 0.04, 0.1)
+    data = mock_image(xv, yv, psf, 0.01, seed, lens=(1.2, 0.8, 30.0, 0.0, 0.0), nsplit=2,
+                      source=(1.0, 0.2, 1.5, 0.75, 20.0, 0.04, -0.02))
+    mask = annulus_mask(xv, yv, 0.0, 4.5)
+    lenses = [dict(type="sple", params=[1.2, 1.0, 0.0, 0.8, 30.0, 0.0, 0.0]),
+              dict(type="nfw", params=[0.2, 8.0, 0.7, 40.0, 0.3, -0.2])]
+
+    def draw(rng, n):
+        p = np.zeros((n, 13))
+        p[:, 0] = rng.uniform(1.0, 1.4, n)      # SIE b
+        p[:, 1] = 1.0
+        p[:, 3] = rng.uniform(0.6, 0.95, n)     # SIE q
+        p[:, 4] = rng.uniform(0.0, 180.0, n)
+        p[:, 7] = rng.uniform(0.05, 0.5, n)     # NFW ks
+        p[:, 8] = rng.uniform(2.0, 20.0, n)     # NFW rs
+        p[:, 9] = rng.uniform(0.5, 1.0, n)      # NFW q
+        p[:, 10] = rng.uniform(0.0, 180.0, n)   # NFW theta
+        p[:, 11] = 0.3 + rng.uniform(-0.5, 0.5, n)
+        p[:, 12] = -0.2 + rng.uniform(-0.5, 0.5, n)
+        return p
+
+    return Workload("cfg4: 200x200 @0.04\", r<4.5\", 4x4 split, 21x21 Airy PSF, 48x48 source, SIE + elliptical NFW",
+                    xv, yv, data, mask, psf, 0.01, 4, (48, 48), lenses, 10.0, draw)
+
+
+# QLens's own plane factors for lens planes at z = 0.5 and 0.8 and a source at
+# z = 2 (default cosmology; the twoplane golden case records the same numbers)
+CFG5_ZFAC = [1.0, 1.0]
+CFG5_BETA = [[0.50757349]]
+
+
+def cfg5(seed=5):
+    xv = pixel_corners(300, -4.5, 4.5)
+    yv = pixel_corners(300, -4.5, 4.5)
+    psf = airy_psf(31, 0.03, 0.08)
+    data = mock_image(xv, yv, psf, 0.01, seed, lens=(1.2, 0.8, 30.0, 0.05, 10.0), nsplit=2,
+                      source=(1.0, 0.2, 1.5, 0.75, 20.0, 0.04, -0.02))
+    mask = annulus_mask(xv, yv, 0.3, 3.5)
+    lenses = [dict(type="sple", params=[1.2, 1.0, 0.0, 0.8, 30.0, 0.0, 0.0], plane=0),
+              dict(type="shear", params=[0.05, 10.0, 0.0, 0.0], plane=0),
+              dict(type="nfw", params=[0.1, 0.1, 0.8, 0.0, 0.9, 0.6], plane=1)]
+
+    def draw(rng, n):
+        p = np.zeros((n, 17))
+        p[:, 0] = rng.uniform(1.0, 1.4, n)
+        p[:, 1] = 1.0
+        p[:, 3] = rng.uniform(0.6, 0.95, n)
+        p[:, 4] = rng.uniform(0.0, 180.0, n)
+        p[:, 7] = rng.uniform(0.0, 0.1, n)
+        p[:, 8] = rng.uniform(0.0, 180.0, n)
+        p[:, 11] = rng.uniform(0.05, 0.3, n)    # subhalo ks
+        p[:, 12] = rng.uniform(0.05, 0.3, n)    # subhalo rs
+        p[:, 13] = rng.uniform(0.5, 1.0, n)
+        p[:, 14] = rng.uniform(0.0, 180.0, n)
+        ang = rng.uniform(0, 2 * math.pi, n)
+        p[:, 15] = 1.2 * np.cos(ang)            # on the Einstein ring
+        p[:, 16] = 1.2 * np.sin(ang)
+        return p
+
+    return Workload("cfg5: 300x300 @0.03\", annulus 0.3-3.5\", 4x4 split, 31x31 Airy PSF, 48x48 source, "
+                    "two planes (SIE+shear z=0.5, NFW subhalo z=0.8)",
+                    xv, yv, data, mask, psf, 0.01, 4, (48, 48), lenses, 10.0, draw, zfac=CFG5_ZFAC, beta=CFG5_BETA)
+
+
+CONFIGS = {"cfg1": cfg1, "cfg2": cfg2, "cfg3": cfg3, "cfg4": cfg4, "cfg5": cfg5}

@@ -19,8 +19,10 @@ tests/golden/<case>.npz.  The .npz holds:
   -2 log(evidence) as returned by QLens::invert_image_surface_brightness_map.
 
 The lens configuration is stored in the library's own parameter convention
-(SPLE: b, alpha, s, q, theta_deg, xc, yc; SHEAR: shear, theta_deg, xc, yc),
-which is the same convention the QLens 'lens' command uses.
+(SPLE: b, alpha, s, q, theta_deg, xc, yc; SHEAR: shear, theta_deg, xc, yc;
+NFW: ks, rs, q, theta_deg, xc, yc), which is the same convention the QLens
+'lens' command uses, with each lens's redshift plane; the plane factors the
+reference ray-traced with are stored as zfactors / betafactors.
 """
 import json
 import os
@@ -161,12 +163,80 @@ inversion_method dense
         dense_rows=-1,
         full_F=True,
     ),
+    # elliptical NFW perturber (numerical deflection: adaptive Gauss-Patterson
+    # quadrature, profile.cpp:2359-2375) beside an SIE host and shear
+    "nfw": dict(
+        script="""random_seed 11
+grid -1.5 1.5 -1.5 1.5
+img_npixels 30 30
+emode 1
+lens sple 0.9 1 0 0.8 15 0 0 shear=0.04 -30
+lens nfw 0.35 1.8 0.65 40 0.45 -0.3
+source sersic 2 0.12 1.3 0.85 5 0.03 0.02
+psf_width 0.05
+bg_pixel_noise 0.02
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0.2 1.5
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 12 12
+fit regularization curvature
+regparam 8
+imgpixel_nsplit 3
+split_imgpixels on
+inversion_method dense
+""",
+        lenses=[dict(type="sple", params=[0.9, 1.0, 0.0, 0.8, 15.0, 0.0, 0.0]),
+                dict(type="shear", params=[0.04, -30.0, 0.0, 0.0]),
+                dict(type="nfw", params=[0.35, 1.8, 0.65, 40.0, 0.45, -0.3])],
+        dense_rows=-1,
+        full_F=True,
+    ),
+    # two lens planes: SIE + shear at z=0.5, elliptical NFW at z=0.8, source
+    # at z=2 (multi-plane recursion, lenscalc.cpp:81-113)
+    "twoplane": dict(
+        script="""random_seed 13
+zsrc 2
+zlens 0.5
+grid -1.5 1.5 -1.5 1.5
+img_npixels 30 30
+emode 1
+lens sple 0.85 1 0 0.75 -20 0 0 shear=0.05 35
+lens nfw 0.5 1.2 0.7 -50 -0.35 0.25 z=0.8
+source sersic 2 0.12 1.3 0.85 5 0.03 0.02
+psf_width 0.05
+bg_pixel_noise 0.02
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0.2 1.5
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 12 12
+fit regularization curvature
+regparam 8
+imgpixel_nsplit 3
+split_imgpixels on
+inversion_method dense
+""",
+        lenses=[dict(type="sple", params=[0.85, 1.0, 0.0, 0.75, -20.0, 0.0, 0.0], plane=0),
+                dict(type="shear", params=[0.05, 35.0, 0.0, 0.0], plane=0),
+                dict(type="nfw", params=[0.5, 1.2, 0.7, -50.0, -0.35, 0.25], plane=1)],
+        dense_rows=-1,
+        full_F=True,
+    ),
 }
 
-ARRAYS_F64 = ["xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
+ARRAYS_F64 = ["zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
               "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
               "F_diag", "F_packed_upper", "s", "model"]
-ARRAYS_I32 = ["masked_pixels", "active_index", "active_pixels", "L_rowptr", "L_index", "R_index"]
+ARRAYS_I32 = ["lens_plane", "masked_pixels", "active_index", "active_pixels", "L_rowptr", "L_index", "R_index"]
 ARRAYS_U8 = ["mask"]
 
 

@@ -7,7 +7,7 @@ import numpy as np
 from qlens_gb300 import abi
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["tiny_sie", "fixed_grid", "powerlaw", "cfg1"]
+CASES = ["tiny_sie", "fixed_grid", "powerlaw", "nfw", "twoplane", "cfg1"]
 
 
 class Golden:
@@ -41,3 +41,19 @@ class Golden:
 
     def params(self):
         return abi.flat_params(self.lenses)
+
+    def zbeta(self):
+        """(zfactors, betafactors rows) the reference ray-traced this case with,
+        or (None, None) for a single lens plane."""
+        zf = self.arr.get("zfactors")
+        if zf is None or len(zf) <= 1:
+            return None, None
+        bf = list(self.arr["betafactors"])
+        beta, k = [], 0
+        for i in range(1, len(zf)):
+            beta.append(bf[k:k + i])
+            k += i
+        return list(zf), beta
+
+    def planes(self):
+        return abi.make_planes(*self.zbeta())

@@ -20,7 +20,7 @@ M2_TOL = 2 * LOGL_TOL   # on -2 log(evidence)
 def _ctx(g, precision):
     from qlens_gb300 import PixelLikelihood
     pl = PixelLikelihood.from_opts(g.image, g.psf, g.opts, precision=precision)
-    pl.set_lens_model(g.lenses)
+    pl.set_lens_model(g.lenses, *g.zbeta())
     return pl
 
 

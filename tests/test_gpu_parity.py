@@ -26,9 +26,22 @@ def _gpu():
 def _run(g, params=None, precision=0):
     PL = _gpu()
     pl = PL.from_opts(g.image, g.psf, g.opts, precision=precision)
-    pl.set_lens_model(g.lenses)
+    pl.set_lens_model(g.lenses, *g.zbeta())
     r = pl.invert_image_surface_brightness_map(params)
     return pl, r
+
+
+def _srcpt_tol(g):
+    """Bound on |source point difference| / coordinate scale.
+
+    SPLE and shear: a few ulp (CUDA's and glibc's atan / atanh / pow differ in
+    the last bit).  NFW: QLens's convergence kappa = 2 ks (1 - F(x)) / (x^2 - 1),
+    F = atan(sqrt(x^2-1))/sqrt(x^2-1) or atanh(sqrt(1-x^2))/sqrt(1-x^2), cancels
+    as x^2 -> 1 (the reference switches to its series only within 1e-5 of 1),
+    so a one-ulp difference in atan / atanh becomes up to ~1e5 ulp of kappa at
+    quadrature nodes near the scale radius; the integrals average it down
+    (measured: 1.5e-14 of the coordinate scale)."""
+    return 1e-12 if any(l["type"] == "nfw" for l in g.lenses) else 1e-14
 
 
 def _rel(a, b):
@@ -60,7 +73,7 @@ def test_golden_lensing_matrix(name):
     # beta = theta - alpha: a last-bit difference of alpha is an absolute error
     # on the scale of the coordinates, so bound it against that scale
     err = np.abs(d["srcpt"] - ref_sp)
-    assert err.max() <= 1e-14 * np.abs(ref_sp).max()
+    assert err.max() <= _srcpt_tol(g) * np.abs(ref_sp).max()
     same = np.mean(d["srcpt"] == ref_sp)
     print("%s: %.4f%% of source-point coordinates bit-identical" % (name, 100 * same))
     # identical L sparsity and indices
@@ -68,7 +81,7 @@ def test_golden_lensing_matrix(name):
     assert np.array_equal(d["L_rowptr"], g.arr["L_rowptr"])
     assert np.array_equal(d["L_index"], g.arr["L_index"])
     # a last-bit change of a source point moves a weight by ~|dw/dx| ulp(x) ~ 1e-15
-    assert np.allclose(d["L_value"], g.arr["L_value"], rtol=1e-12, atol=1e-13)
+    assert np.allclose(d["L_value"], g.arr["L_value"], rtol=1e-12, atol=1e-13 * _srcpt_tol(g) / 1e-14)
     assert np.allclose(d["s"], g.arr["s"], rtol=1e-6, atol=1e-9 * np.abs(g.arr["s"]).max())
     assert np.allclose(d["model"], g.arr["model"], rtol=1e-6, atol=1e-9 * np.abs(g.arr["model"]).max())
     M = r["n_active_src"]
@@ -84,7 +97,7 @@ def test_random_parameters_vs_oracle():
     rng = np.random.default_rng(11)
     PL = _gpu()
     pl = PL.from_opts(g.image, g.psf, g.opts)
-    pl.set_lens_model(g.lenses)
+    pl.set_lens_model(g.lenses, *g.zbeta())
     base = np.array(g.params())
     for trial in range(6):
         p = base.copy()
@@ -99,6 +112,38 @@ def test_random_parameters_vs_oracle():
         assert r["n_active_src"] == ro["n_active_src"] and r["L_nnz"] == ro["L_nnz"]
         assert _rel(r["m2logev"], ro["m2logev"]) < REL, (trial, r["m2logev"], ro["m2logev"])
         assert np.array_equal(pl.dump(g.arr["srcpt_x"].size, r)["L_index"], O.get("L_index"))
+    pl.close()
+
+
+@pytest.mark.parametrize("name", ["nfw", "twoplane"])
+def test_random_nfw_parameters_vs_oracle(name):
+    """Elliptical (and one spherical) NFW by Gauss-Patterson quadrature, single
+    and two lens planes, against the oracle on the same parameter vectors."""
+    from oracle import oracle as O
+    g = Golden(name)
+    rng = np.random.default_rng(23)
+    PL = _gpu()
+    pl = PL.from_opts(g.image, g.psf, g.opts)
+    pl.set_lens_model(g.lenses, *g.zbeta())
+    base = np.array(g.params())
+    n_sub = g.arr["srcpt_x"].size
+    for trial in range(5):
+        p = base.copy()
+        p[11] *= rng.uniform(0.5, 1.5)               # ks
+        p[12] *= rng.uniform(0.6, 1.6)               # rs
+        p[13] = 1.0 if trial == 4 else rng.uniform(0.5, 0.95)   # q (1: spherical branch)
+        p[14] += rng.uniform(-40, 40)                # theta
+        p[15] += rng.uniform(-0.1, 0.1)              # xc
+        p[16] += rng.uniform(-0.1, 0.1)              # yc
+        r = pl.invert_image_surface_brightness_map(p)
+        ro = O.evaluate(g.image, g.psf, g.opts, g.lenses, lens_params=p, planes=g.planes())
+        assert r["status"] == ro["status"] == 0
+        assert r["n_active_src"] == ro["n_active_src"] and r["L_nnz"] == ro["L_nnz"]
+        assert _rel(r["m2logev"], ro["m2logev"]) < REL, (trial, r["m2logev"], ro["m2logev"])
+        d = pl.dump(n_sub, r)
+        sp = O.get("srcpt")
+        assert np.abs(d["srcpt"] - sp).max() <= _srcpt_tol(g) * np.abs(sp).max()
+        assert np.array_equal(d["L_index"], O.get("L_index"))
     pl.close()
 
 

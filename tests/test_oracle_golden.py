@@ -16,7 +16,7 @@ from oracle import oracle as O
 @pytest.fixture(scope="module", params=CASES)
 def case(request):
     g = Golden(request.param)
-    r = O.evaluate(g.image, g.psf, g.opts, g.lenses)
+    r = O.evaluate(g.image, g.psf, g.opts, g.lenses, planes=g.planes())
     return g, r
 
 
@@ -79,7 +79,7 @@ def test_missing_data_sentinel():
     saved = img.surface_brightness
     img.surface_brightness = None
     try:
-        r = O.evaluate(g.image, g.psf, g.opts, g.lenses)
+        r = O.evaluate(g.image, g.psf, g.opts, g.lenses, planes=g.planes())
     finally:
         img.surface_brightness = saved
     assert r["m2logev"] == -1e30
@@ -88,12 +88,12 @@ def test_missing_data_sentinel():
 def test_grid_too_small_sentinel():
     g = Golden("tiny_sie")
     g.opts.npixels_x = 1
-    r = O.evaluate(g.image, g.psf, g.opts, g.lenses)
+    r = O.evaluate(g.image, g.psf, g.opts, g.lenses, planes=g.planes())
     assert r["m2logev"] == 2e30
 
 
 def test_no_source_pixels_sentinel():
     g = Golden("fixed_grid")
     g.opts.xmin, g.opts.xmax, g.opts.ymin, g.opts.ymax = 50.0, 51.0, 50.0, 51.0
-    r = O.evaluate(g.image, g.psf, g.opts, g.lenses)
+    r = O.evaluate(g.image, g.psf, g.opts, g.lenses, planes=g.planes())
     assert r["m2logev"] == 2e30 and r["n_active_src"] == 0
