@@ -30,6 +30,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# one hardware work queue per concurrent evaluation slot (the default of 8
+# would serialise streams beyond the eighth); must precede CUDA initialisation
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
 
@@ -180,6 +183,8 @@ def main():
     ap.add_argument("--impl", default="qlpix", choices=["qlpix", "reference"])
     ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
     ap.add_argument("--batch", type=int, default=0, help="evaluations per step (default per precision)")
+    ap.add_argument("--slots", type=int, default=0, help="concurrent evaluation slots (default min(batch, 32))")
+    ap.add_argument("--no-graphs", action="store_true", help="launch kernel by kernel instead of replaying graphs")
     ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -213,7 +218,9 @@ def main():
     except Exception:
         precision = "fp64"
         pl.set_precision(abi.QLP_FP64)
-    B = args.batch or (16 if precision == "mixed" else 2)
+    B = args.batch or (32 if precision == "mixed" else 4)
+    pl.set_batch_slots(args.slots or min(B, 32))
+    pl.set_graphs(not args.no_graphs)
     stream = torch.cuda.current_stream()
     pl.set_stream(stream.cuda_stream)
 
@@ -230,8 +237,8 @@ def main():
     clocks = ClockSampler(local_rank)
     clocks.start()
     dev_ms = 0.0
-    stage = np.zeros(6)
     launches = 0
+    h2d = d2h = 0
     results = []
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -241,8 +248,10 @@ def main():
     for k in range(args.steps):
         res = pl.eval_batch(pinned[args.warmup + k].numpy())
         dev_ms += pl.last_device_ms()
-        stage += np.array(pl.stage_times())
         launches += pl.last_launch_count()
+        hb, db = pl.last_transfer_bytes()
+        h2d += hb
+        d2h += db
         results.extend(res)
     e1.record(stream)
     torch.cuda.synchronize()
@@ -259,10 +268,22 @@ def main():
     e2e = n_evals / wall
     bad = [r for r in results if r["status"] != 0]
 
-    # roofline of the dominant kernel: the F = L'^T C^-1 L' contraction
+    # Stage breakdown and the SYRK's own duration: a few evaluations after the
+    # timed region, one at a time and launched kernel by kernel, with CUDA
+    # events around each stage on the evaluation's stream (inside a batch the
+    # stages of concurrent evaluations overlap, so they are not separable).
+    iso = wl.draw(np.random.default_rng(777 + rank), 3)
+    stage = np.zeros(6)
+    iso_res = []
+    for p in iso:
+        iso_res.append(pl.invert_image_surface_brightness_map(p))
+        stage += np.array(pl.stage_times())
+    stage /= len(iso)
+
+    # roofline of the dominant tensor-core kernel: the F = L'^T C^-1 L' contraction
     peaks = _peaks()
     syrk_ms = stage[3]
-    flops = algorithmic_syrk_flops(results)
+    flops = algorithmic_syrk_flops(iso_res) / len(iso)
     achieved = flops / (syrk_ms / 1e3) / 1e12 if syrk_ms > 0 else None
     if precision == "mixed":
         peak = peaks.get("bf16_tflops", 1900.0)
@@ -276,7 +297,8 @@ def main():
     traffic = SYRK_TC_DRAM_BYTES_CFG2 if (precision == "mixed" and args.config == "cfg2") else None
     roofline = {"bound": bound, "kernel": "F = L'^T C^-1 L' (SYRK)", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "peak_source": peak_note, "algorithmic_flops_per_step": flops / args.steps}
+                "peak_source": peak_note, "algorithmic_flops_per_launch": flops,
+                "timing": "CUDA events around the SYRK launch of single evaluations after the timed region"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -293,16 +315,18 @@ def main():
             "dtype": "f32-tensor+f64" if precision == "mixed" else "f64",
             "data": "synthetic (seeded mock image; parameters drawn from the prior box)",
             "config": {**wl.describe(), "batch_per_step": B, "precision": precision,
+                       "slots": args.slots or min(B, 32),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set (dense L' %.0f MB) exceeds the 129 MB L2" % (
                            8e-6 * max(r["n_active_pixels"] for r in results) * max(r["n_active_src"] for r in results))},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(B * batches[0].shape[1] * 8),
-                    "d2h_bytes_per_step": int(B * 72)},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d // args.steps),
+                    "d2h_bytes_per_step": int(d2h // args.steps)},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clk,
-            "stage_ms_per_eval": [x / (B * args.steps) for x in stage],
+            "stage_ms_single_eval": [float(x) for x in stage],
+            "graphs": not args.no_graphs,
             "failed_evals": len(bad),
             "stream_span_ms": span_ms,
         }

@@ -151,10 +151,19 @@ int qlp_set_stream(qlp_ctx* ctx, void* stream);
 int qlp_eval(qlp_ctx* ctx, const double* lens_params, double regparam, qlp_result* out);
 
 /* Maximum number of evaluations of one qlp_eval_batch that run concurrently,
- * each on its own stream with its own workspace (default 16, at most 32).
+ * each on its own stream with its own workspace (default 16, at most 64).
  * More slots hide the sequential parts of each evaluation behind the others
- * at the cost of one workspace per slot. */
+ * at the cost of one workspace per slot (about 0.5 GB for a 200x200 image,
+ * 4x4 split and a 64x64 source grid in QLP_MIXED). */
 int qlp_set_batch_slots(qlp_ctx* ctx, int slots);
+
+/* on = 1 (default): qlp_eval_batch captures each slot's launch sequence once
+ * as a CUDA graph (per precision, mask and source-grid size) and replays it
+ * for every evaluation, so one evaluation costs the host a parameter upload
+ * and one graph launch instead of ~800 kernel launches.  on = 0: kernels are
+ * launched one by one and qlp_stage_times reports the batch's stages.
+ * No counterpart in the reference (it has no device launches). */
+int qlp_set_graphs(qlp_ctx* ctx, int on);
 
 /* Number of doubles in one lens-parameter vector for the current model. */
 int qlp_n_params(const qlp_ctx* ctx);
@@ -185,10 +194,11 @@ int qlp_dump(qlp_ctx* ctx, double* srcpt_xy, int* L_rowptr, int* L_index, double
  * columns) of the last qlp_eval. */
 int qlp_dump_Lpsf(qlp_ctx* ctx, int rows, double* out);
 
-/* Milliseconds of device time per stage of the last qlp_eval or
- * qlp_eval_batch (CUDA events on the context's stream, summed over the
- * batch): [0] ray shooting, [1] grid + mapping + L, [2] PSF convolution and
- * D, [3] F = L'^T C^-1 L' (the SYRK), [4] regularisation, factorisations and
+/* Milliseconds of device time per stage of the last qlp_eval, or of the
+ * last qlp_eval_batch run with graphs off (CUDA events on each evaluation's
+ * stream, summed over the batch; zeros after a graph-replayed batch):
+ * [0] ray shooting, [1] grid + mapping + L, [2] PSF convolution and D,
+ * [3] F = L'^T C^-1 L' (the SYRK), [4] regularisation, factorisations and
  * solve, [5] model image, chi^2 and evidence.  n >= 6. */
 int qlp_stage_times(qlp_ctx* ctx, float* ms, int n);
 
@@ -196,8 +206,14 @@ int qlp_stage_times(qlp_ctx* ctx, float* ms, int n);
  * qlp_eval / qlp_eval_batch. */
 int qlp_last_device_time(qlp_ctx* ctx, float* ms);
 
-/* Number of kernel launches issued by the last qlp_eval / qlp_eval_batch. */
+/* Number of kernels run by the last qlp_eval / qlp_eval_batch (launched
+ * directly or replayed from a graph). */
 long long qlp_last_launch_count(const qlp_ctx* ctx);
+
+/* Bytes the last qlp_eval / qlp_eval_batch copied host -> device (the
+ * per-evaluation lens model and regularisation parameter) and device -> host
+ * (the per-evaluation results). */
+int qlp_last_transfer_bytes(const qlp_ctx* ctx, long long* h2d, long long* d2h);
 
 /* No counterpart in the reference (QLens allocates its matrices on every
  * call).  For callers that cannot call cudaMalloc -- a host application that

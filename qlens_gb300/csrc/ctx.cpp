@@ -45,13 +45,21 @@ static void free_work(Work& w)
 {
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
-                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out};
+                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
 
+static void drop_graph(Slot& s)
+{
+    if (s.graph) cudaGraphExecDestroy(s.graph);
+    s.graph = nullptr;
+    s.graph_gen = 0;
+}
+
 static void free_slot(Slot& s)
 {
+    drop_graph(s);
     mixed_free(s);
     free_work(s.w);
     s.M_cap = s.N_cap = s.nsub_cap = s.snx_cap = s.sny_cap = 0;
@@ -87,7 +95,7 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     const size_t part = std::max((size_t)((n_mask + 255) / 256 + 1) * Mc, (size_t)Mc * 4);
     CK(dalloc(&w.partial, part), "alloc");
     CK(dalloc(&w.linv, (size_t)Mc * 64), "alloc");
-    CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc");
+    CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc"); CK(dalloc(&w.ep, 1), "alloc");
     s.M_cap = Mc;
     s.N_cap = n_mask;
     s.nsub_cap = nsub;
@@ -115,6 +123,9 @@ static int ensure_slot(qlp_ctx* c, int k, int n_mask, int cells, int snx, int sn
     Slot& s = c->slots[k];
     if (!s.stream) CK(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "stream");
     if (!s.done) CK(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "event");
+    if (!s.side) CK(cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking), "stream");
+    if (!s.side_fork) CK(cudaEventCreateWithFlags(&s.side_fork, cudaEventDisableTiming), "event");
+    if (!s.side_join) CK(cudaEventCreateWithFlags(&s.side_join, cudaEventDisableTiming), "event");
     const int nsub = c->sd.nsub;
     if (s.N_cap >= n_mask && s.M_cap >= round64(std::max(cells, 64)) && s.snx_cap >= snx && s.sny_cap >= sny &&
         s.nsub_cap == nsub)
@@ -164,6 +175,13 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     sd.cov_inverse = cov_inverse;
     sd.xvals = c->d_xvals; sd.yvals = c->d_yvals; sd.data = c->d_data; sd.covinv = c->d_covinv;
     sd.mpix = c->d_mpix; sd.psf = c->d_psf;
+    {
+        double psum = 0, cmax = 0;
+        for (int t = 0; t < psf->nx * psf->ny; t++) psum += fabs(psf->matrix[t]);
+        for (int t = 0; t < npx; t++) cmax = std::max(cmax, covinv[t]);
+        const double bound = std::max(psum, 1e-30) * std::max(sqrt(cmax), 1e-30);
+        sd.fix_exp = std::max(0, std::min(100, 61 - (int)ceil(log2(bound))));
+    }
 
     SrcOpts& so = c->so;
     so.snx = opts->npixels_x; so.sny = opts->npixels_y;
@@ -188,11 +206,15 @@ void ctx_free(qlp_ctx* c)
         free_slot(s);
         if (s.stream) cudaStreamDestroy(s.stream);
         if (s.done) cudaEventDestroy(s.done);
+        if (s.side) cudaStreamDestroy(s.side);
+        if (s.side_fork) cudaEventDestroy(s.side_fork);
+        if (s.side_join) cudaEventDestroy(s.side_join);
     }
     c->slots.clear();
-    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix, c->d_res};
+    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);
+    if (c->h_ep) cudaFreeHost(c->h_ep);
     for (int i = 0; i <= QLP_N_STAGES; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
@@ -221,19 +243,30 @@ static int build_lens_model(qlp_ctx* c, const double* lens_params, LensModel& lm
     return QLP_OK;
 }
 
+static bool model_has_nfw(const qlp_ctx* c)
+{
+    for (const qlp_lens& l : c->lenses)
+        if (l.type == QLP_LENS_NFW) return true;
+    return false;
+}
+
 // The launch sequence of one evaluation on stream st with the workspace of
-// `slot`; sd / so select the mask and source grid.  ev (QLP_N_STAGES+1 events
-// or null) brackets the stages.
-static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const SrcOpts& so_in, const LensModel& lm,
-                        double regparam, cudaStream_t st, cudaEvent_t* ev)
+// `slot`; sd / so select the mask and source grid.  Everything that changes
+// between evaluations (lens model, regularisation parameter) is read from the
+// slot's EvalParams in device memory, so the sequence can be captured once
+// and replayed.  ev (QLP_N_STAGES+1 events, or null) brackets the stages.
+static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const SrcOpts& so_in, cudaStream_t st,
+                        cudaEvent_t* ev)
 {
     StaticData sd = sd_in;
     SrcOpts so = so_in;
     Work& w = slot.w;
     const int Mc = slot.M_cap;
     const int N_max = sd.n_mask;
+    const double* regp = regparam_dev(w);
+    cudaMemsetAsync(w.out, 0, sizeof(EvalOut), st);
     if (ev) cudaEventRecord(ev[0], st);
-    launch_raytrace(sd, lm, w, st);
+    launch_raytrace(sd, model_has_nfw(c), w, st);
     if (ev) cudaEventRecord(ev[1], st);
     launch_grid(sd, so, w, st);
     launch_locate(sd, so, w, st);
@@ -244,7 +277,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     launch_dvec(sd, w, N_max, st);
     const bool mixed = (c->precision == QLP_MIXED);
     if (mixed) {
-        int r = run_inversion_mixed(slot, sd, so, regparam, st, ev);
+        int r = run_inversion_mixed(slot, sd, so, regp, st, ev);
         if (r != QLP_OK) return r;
     } else {
         int r = ensure_fp64_mats(slot);
@@ -254,7 +287,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
         if (ev) cudaEventRecord(ev[3], st);
         launch_syrk_fp64(sd, w, N_max, Mc, st);
         if (ev) cudaEventRecord(ev[4], st);
-        launch_regularization(so, w, Mc, regparam, st);
+        launch_regularization(so, w, Mc, regp, st);
         if (so.regularization) {
             launch_cholesky_fp64(w.R, w.ldF, Mc, w.gs, 1, w.linv, st);
             launch_logdet(w.R, w.ldF, Mc, w, 1, st);
@@ -264,8 +297,66 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
         launch_solve_fp64(w, Mc, st);
     }
     if (ev) cudaEventRecord(ev[5], st);
-    launch_model_chi2(sd, so, w, N_max, Mc, regparam, st, mixed);
+    launch_model_chi2(sd, so, w, N_max, Mc, regp, st, mixed);
     if (ev) cudaEventRecord(ev[6], st);
+    return QLP_OK;
+}
+
+// Make the slot's workspace ready for the pipeline without allocating during
+// a stream capture.
+static int prepare_slot(qlp_ctx* c, Slot& s)
+{
+    if (c->precision == QLP_MIXED) return mixed_init(s);
+    return ensure_fp64_mats(s);
+}
+
+// Capture the slot's launch sequence for this (mask, source grid) as a graph.
+static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const int key[5])
+{
+    drop_graph(s);
+    int r = prepare_slot(c, s);
+    if (r != QLP_OK) return r;
+    const long long l0 = kernel_launch_counter();
+    CK(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal), "capture");
+    r = run_pipeline(c, s, sd, so, s.stream, nullptr);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s.stream, &g);
+    const long long n = kernel_launch_counter() - l0;
+    count_launches((int)-n);            // nothing ran yet: replays count them
+    if (r != QLP_OK) { if (g) cudaGraphDestroy(g); return r; }
+    if (e != cudaSuccess || !g) return cuda_fail(e, "stream capture");
+    e = cudaGraphInstantiate(&s.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { s.graph = nullptr; return cuda_fail(e, "graph instantiate"); }
+    for (int i = 0; i < 5; i++) s.graph_key[i] = key[i];
+    s.graph_gen = c->graph_gen;
+    s.graph_launches = n;
+    return QLP_OK;
+}
+
+// One evaluation on slot s: upload its parameters, run (replay or launch) the
+// sequence, copy its result to *h_dst -- all asynchronous on the slot stream.
+static int issue_eval(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, int mask_id,
+                      const EvalParams* h_ep, EvalOut* h_dst, cudaEvent_t* ev)
+{
+    CK(cudaMemcpyAsync(s.w.ep, h_ep, sizeof(EvalParams), cudaMemcpyHostToDevice, s.stream), "h2d");
+    if (c->use_graphs && ev == nullptr) {
+        const int key[5] = {c->precision, mask_id, so.snx, so.sny, model_has_nfw(c) ? 1 : 0};
+        bool ok = s.graph && s.graph_gen == c->graph_gen;
+        for (int i = 0; ok && i < 5; i++) ok = (s.graph_key[i] == key[i]);
+        if (!ok) {
+            int r = capture_graph(c, s, sd, so, key);
+            if (r != QLP_OK) return r;
+        }
+        CK(cudaGraphLaunch(s.graph, s.stream), "graph launch");
+        count_launches((int)s.graph_launches);
+    } else {
+        int r = prepare_slot(c, s);
+        if (r != QLP_OK) return r;
+        r = run_pipeline(c, s, sd, so, s.stream, ev);
+        if (r != QLP_OK) return r;
+    }
+    CK(cudaMemcpyAsync(h_dst, s.w.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, s.stream), "d2h");
     return QLP_OK;
 }
 
@@ -293,15 +384,17 @@ static int ensure_results(qlp_ctx* c, int n)
         CK(cudaMallocHost((void**)&c->h_out, sizeof(EvalOut) * n), "pinned");
         c->h_out_cap = n;
     }
-    if (c->d_res_cap < n) {
-        if (c->d_res) cudaFree(c->d_res);
-        c->d_res = nullptr;
-        CK(dalloc(&c->d_res, n), "alloc");
-        c->d_res_cap = n;
+    if (c->h_ep_cap < n) {
+        if (c->h_ep) cudaFreeHost(c->h_ep);
+        c->h_ep = nullptr;
+        CK(cudaMallocHost((void**)&c->h_ep, sizeof(EvalParams) * n), "pinned");
+        c->h_ep_cap = n;
     }
     return QLP_OK;
 }
 
+// Single evaluation: slot 0, launched directly (not replayed) so that the
+// stage events bracket each part of the pipeline.
 int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result* out)
 {
     memset(out, 0, sizeof(*out));
@@ -310,27 +403,26 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
         out->m2logev = 2e30; out->status = QLP_ERR_GRID_TOO_SMALL;
         return QLP_ERR_GRID_TOO_SMALL;
     }
-    LensModel lm;
-    int r = build_lens_model(c, lens_params, lm);
-    if (r != QLP_OK) { out->status = r; return r; }
-    if (regparam <= 0) regparam = c->opts.regparam;
-    r = ensure_results(c, 1);
+    int r = ensure_results(c, 1);
     if (r != QLP_OK) return r;
-    if (c->precision == QLP_MIXED) {
-        r = mixed_init(c->slots[0]);
-        if (r != QLP_OK) { out->status = r; return r; }
-    }
+    EvalParams& ep = c->h_ep[0];
+    r = build_lens_model(c, lens_params, ep.lm);
+    if (r != QLP_OK) { out->status = r; return r; }
+    ep.regparam = (regparam > 0) ? regparam : c->opts.regparam;
     Slot& s = c->slots[0];
     long long l0 = kernel_launch_counter();
     cudaStream_t st = c->stream;
-    s.w.out = c->d_res;
-    CK(cudaMemsetAsync(s.w.out, 0, sizeof(EvalOut), st), "memset");
-    r = run_pipeline(c, s, c->sd, c->so, lm, regparam, st, c->ev);
+    CK(cudaEventRecord(c->fork, st), "event");
+    CK(cudaStreamWaitEvent(s.stream, c->fork, 0), "wait");
+    r = issue_eval(c, s, c->sd, c->so, -1, &ep, &c->h_out[0], c->ev);
     if (r != QLP_OK) { out->status = r; return r; }
-    CK(cudaMemcpyAsync(c->h_out, c->d_res, sizeof(EvalOut), cudaMemcpyDeviceToHost, st), "d2h");
+    CK(cudaEventRecord(s.done, s.stream), "event");
+    CK(cudaStreamWaitEvent(st, s.done, 0), "wait");
     CK(cudaGetLastError(), "launch");
     CK(cudaStreamSynchronize(st), "eval");
     c->last_launches = kernel_launch_counter() - l0;
+    c->last_h2d = sizeof(EvalParams);
+    c->last_d2h = sizeof(EvalOut);
     for (int i = 0; i < QLP_N_STAGES; i++) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
     cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
     fill_result(c->h_out[0], out);
@@ -350,6 +442,7 @@ int ctx_set_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)
         c->mask_cnt.push_back((int)v.size());
         all.insert(all.end(), v.begin(), v.end());
     }
+    c->graph_gen++;                       // captured graphs hold the old mask pointers
     if (c->d_inst_mpix) { cudaFree(c->d_inst_mpix); c->d_inst_mpix = nullptr; }
     CK(dalloc(&c->d_inst_mpix, all.size()), "alloc");
     if (!all.empty())
@@ -393,37 +486,39 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
     }
     int r = ensure_results(c, n);
     if (r != QLP_OK) return r;
+    const bool timed = !c->use_graphs;     // direct launches record the stage events
     const int ne = QLP_N_STAGES + 1;
-    while ((int)c->ev_pool.size() < ne * n) {
+    while (timed && (int)c->ev_pool.size() < ne * n) {
         cudaEvent_t e;
         CK(cudaEventCreate(&e), "event");
         c->ev_pool.push_back(e);
     }
     cudaStream_t st0 = c->stream;
     long long l0 = kernel_launch_counter();
-    CK(cudaMemsetAsync(c->d_res, 0, sizeof(EvalOut) * n, st0), "memset");
     CK(cudaEventRecord(c->fork, st0), "event");
     for (int k = 0; k < S; k++) CK(cudaStreamWaitEvent(c->slots[k].stream, c->fork, 0), "wait");
     std::vector<int> pre(n, QLP_OK);
     int rc = QLP_OK;
     for (int i = 0; i < n; i++) {
         Slot& s = c->slots[i % S];
-        LensModel lm;
-        int ri = build_lens_model(c, params + (size_t)i * np, lm);
-        const double lam = (regparams && regparams[i] > 0) ? regparams[i] : c->opts.regparam;
+        EvalParams& ep = c->h_ep[i];
+        int ri = build_lens_model(c, params + (size_t)i * np, ep.lm);
+        ep.regparam = (regparams && regparams[i] > 0) ? regparams[i] : c->opts.regparam;
         StaticData sd = c->sd;
         SrcOpts so = c->so;
+        int mask_id = -1;
         if (inst) {
             if (inst[i].mask_id >= 0) {
-                sd.mpix = c->d_inst_mpix + c->mask_off[inst[i].mask_id];
-                sd.n_mask = c->mask_cnt[inst[i].mask_id];
+                mask_id = inst[i].mask_id;
+                sd.mpix = c->d_inst_mpix + c->mask_off[mask_id];
+                sd.n_mask = c->mask_cnt[mask_id];
                 sd.n_sub = sd.n_mask * sd.nsub;
             }
             if (inst[i].src_npixels_x > 0) { so.snx = inst[i].src_npixels_x; so.sny = inst[i].src_npixels_y; }
         }
-        s.w.out = c->d_res + i;
         if (ri == QLP_OK && (so.snx < 2 || so.sny < 2)) ri = QLP_ERR_GRID_TOO_SMALL;
-        if (ri == QLP_OK) ri = run_pipeline(c, s, sd, so, lm, lam, s.stream, &c->ev_pool[(size_t)ne * i]);
+        if (ri == QLP_OK)
+            ri = issue_eval(c, s, sd, so, mask_id, &ep, &c->h_out[i], timed ? &c->ev_pool[(size_t)ne * i] : nullptr);
         pre[i] = ri;
         if (ri != QLP_OK && rc == QLP_OK) rc = ri;
     }
@@ -432,12 +527,13 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         CK(cudaStreamWaitEvent(st0, c->slots[k].done, 0), "wait");
     }
     CK(cudaEventRecord(c->join, st0), "event");
-    CK(cudaMemcpyAsync(c->h_out, c->d_res, sizeof(EvalOut) * n, cudaMemcpyDeviceToHost, st0), "d2h");
     CK(cudaGetLastError(), "launch");
     CK(cudaStreamSynchronize(st0), "batch");
     c->last_launches = kernel_launch_counter() - l0;
+    c->last_h2d = (long long)n * sizeof(EvalParams);
+    c->last_d2h = (long long)n * sizeof(EvalOut);
     for (int k = 0; k < QLP_N_STAGES; k++) c->stage_ms[k] = 0;
-    for (int i = 0; i < n; i++) {
+    for (int i = 0; timed && i < n; i++) {
         if (pre[i] != QLP_OK) continue;
         for (int k = 0; k < QLP_N_STAGES; k++) {
             float t = 0;
@@ -447,12 +543,14 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
     }
     cudaEventElapsedTime(&c->device_ms, c->fork, c->join);
     for (int i = 0; i < n; i++) {
-        fill_result(c->h_out[i], &out[i]);
-        if (c->precision == QLP_MIXED) out[i].refine_iters = 2;
         if (pre[i] != QLP_OK) {
+            memset(&out[i], 0, sizeof(out[i]));
             out[i].status = pre[i];
             out[i].m2logev = (pre[i] == QLP_ERR_GRID_TOO_SMALL) ? 2e30 : 0;
+            continue;
         }
+        fill_result(c->h_out[i], &out[i]);
+        if (c->precision == QLP_MIXED) out[i].refine_iters = 2;
     }
     return rc;
 }

@@ -159,8 +159,10 @@ __device__ __forceinline__ int act_at(const int* ai, int snx, int sny, int i, in
 }
 
 __global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ ai, int snx, int sny,
-                      double regparam, double* __restrict__ F, double* __restrict__ R, int ldF, int do_reg)
+                      const double* __restrict__ regp, double* __restrict__ F, double* __restrict__ R, int ldF,
+                      int do_reg)
 {
+    const double regparam = *regp;
     const int M = gs->M, Mp = mpad64(M);
     const int ncell = snx * sny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
@@ -191,12 +193,12 @@ __global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ 
     }
 }
 
-void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regparam, cudaStream_t st)
+void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* regp, cudaStream_t st)
 {
     const int ncell = so.snx * so.sny;
     if (so.regularization) cudaMemsetAsync(w.R, 0, sizeof(double) * (size_t)w.ldF * w.ldF, st);
     int total = ncell + 64;
-    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regparam, w.F, w.R, w.ldF,
+    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regp, w.F, w.R, w.ldF,
                                                so.regularization);
     count_launches(1);
     (void)M_max;
@@ -248,8 +250,9 @@ __global__ void __launch_bounds__(256) k_model(const GridState* __restrict__ gs,
 __global__ void __launch_bounds__(1024) k_final(StaticData sd, SrcOpts so, const GridState* __restrict__ gs,
                                                 const int* __restrict__ rowidx, const double* __restrict__ model,
                                                 const double* __restrict__ s, const int* __restrict__ ai,
-                                                double regparam, EvalOut* out)
+                                                const double* __restrict__ regp, EvalOut* out)
 {
+    const double regparam = *regp;
     __shared__ double red[2][32];
     const int M = gs->M;
     double chi = 0, es = 0;
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd, SrcOpts so, const
     }
 }
 
-void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max, double regparam,
+void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max, const double* regp,
                        cudaStream_t st, bool model_ready)
 {
     (void)M_max;
@@ -319,7 +322,7 @@ void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_m
         if (blocks > 152 * 16) blocks = 152 * 16;
         k_model<<<blocks, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.s, w.model);
     }
-    k_final<<<1, 1024, 0, st>>>(sd, so, w.gs, w.rowidx, w.model, w.s, w.active_index, regparam, w.out);
+    k_final<<<1, 1024, 0, st>>>(sd, so, w.gs, w.rowidx, w.model, w.s, w.active_index, regp, w.out);
     count_launches(2);
 }
 

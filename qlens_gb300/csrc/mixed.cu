@@ -2,8 +2,8 @@
 // FP32 Cholesky of F and R, FP64 log det accumulation and FP64 iterative
 // refinement of the source amplitudes.
 //
-//   L'32   = P L accumulated in FP32 (psf.cu)                   only feeds F
-//   X      = (L'32 * sqrt(C^-1))^T split into TF32 hi + lo      k_convert_x
+//   X      = (P L sqrt(C^-1))^T, built column by column (one source cell
+//            per CTA, exact fixed-point sums), split into TF32 hi + lo  k_psf_x
 //   F32    = X X^T on tcgen05 (block-sparse over pixel blocks)   k_syrk_tc
 //   F32   += lambda R, R32 = R                                  k_reg32
 //   L_F L_F^T = F32, L_R L_R^T = R32 (FP32 blocked Cholesky)    chol.cuh
@@ -16,15 +16,24 @@
 // FP64; the mixed path's deviation from it is measured by the tests.
 #include <cuda.h>
 #include <cstring>
+#include <algorithm>
 #include "qlpix_ctx.h"
 #include "chol.cuh"
 #include "tc_syrk.cuh"
+#include "chol128.cuh"
 
 namespace qlpix {
 
 struct MixedWork {
-    float* L32 = nullptr;    // N_cap x ld32 PSF-convolved L, FP32
     double* t = nullptr;     // N (image-plane scratch)
+    // L by source cell (CSC of the merged pre-PSF rows), for k_psf_x
+    int* colcnt = nullptr;   // M_cap + 1 counts, then the column pointers
+    int* cursor = nullptr;   // M_cap
+    int* colrow = nullptr;   // nnz_cap
+    float* colval = nullptr; // nnz_cap
+    float* sqc = nullptr;    // N_cap: sqrt(C^-1) per active row
+    int nnz_cap = 0;
+    int chunk = 0;           // image rows per k_psf_x accumulator
     float* X_hi = nullptr;
     float* X_lo = nullptr;
     int K_cap = 0;           // columns of X (image pixels), multiple of 32
@@ -40,8 +49,12 @@ struct MixedWork {
     double* z = nullptr;     // M
     double* y = nullptr;     // M (solve scratch)
     double* part = nullptr;
-    float* linvF = nullptr;  // inverses of the 64x64 diagonal Cholesky blocks
-    float* linvR = nullptr;
+    float* linvF = nullptr;  // per 128-block of F: inverse of its diagonal factor, then its transpose
+    float* linv128 = nullptr; // the same for R's current diagonal block
+    float* yf = nullptr;     // M_cap: forward-solve result
+    float* zf = nullptr;     // M_cap: backward-solve result (FP32 copy read by other CTAs)
+    int* flags = nullptr;    // 2 x nb: per-block "published" flags of the two sweeps
+    int nb = 0;              // 128-blocks of M_cap
     CUtensorMap map_hi, map_lo;
     bool ready = false;
 };
@@ -81,7 +94,18 @@ static int make_map(CUtensorMap* map, float* base, int rows, int cols)
 }
 
 // ---------------------------------------------------------------------------
-// X = (L' sqrt(c))^T as TF32 hi + lo, and the nonzero flags of 128x32 blocks.
+// X = (P L sqrt(C^-1))^T as TF32 hi + lo, and the nonzero flags of its
+// 128-cell x 32-pixel blocks, built one source cell (one row of X) at a time.
+//
+// Row s of X is the PSF-convolved image of source cell s: every pixel q that
+// sees s (column s of the pre-PSF L) spreads L[q][s] over its PSF neighbours
+// p with weight psf[k][l] (the transpose of QLens's gather,
+// pixelgrid.cpp:14126-14168), scaled by sqrt(C^-1) of p.  The sums are
+// accumulated as 64-bit fixed point in shared memory, so they are exact and
+// independent of the order the atomics land in (the result is the same bits
+// every run); each product is formed in FP32 and rounded once to the
+// fixed-point grid 2^-fix_exp, far below FP32 resolution.  X's rows are
+// written contiguously, no dense L' is stored, and L is read once per cell.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float to_tf32(float f)
 {
@@ -90,41 +114,125 @@ __device__ __forceinline__ float to_tf32(float f)
     return __uint_as_float(u);
 }
 
-__global__ void __launch_bounds__(256) k_convert_x(const GridState* __restrict__ gs, const float* __restrict__ L,
-                                                   int ldL, const double* __restrict__ cvec, float* __restrict__ Xh,
-                                                   float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
-                                                   int nkb_cap)
+// column counts of the merged pre-PSF L and sqrt(C^-1) per active row
+__global__ void k_csc_count(const GridState* __restrict__ gs, const int* __restrict__ rowptr,
+                            const int* __restrict__ cidx, const int* __restrict__ ccnt,
+                            const double* __restrict__ cvec, int* __restrict__ colcnt, float* __restrict__ sqc)
 {
-    __shared__ float th[32][33];
-    __shared__ float tl[32][33];
+    const int N = gs->N;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const int b = rowptr[r], n = ccnt[r];
+        for (int e = 0; e < n; e++) atomicAdd(&colcnt[cidx[b + e]], 1);
+        sqc[r] = sqrtf((float)cvec[r]);
+    }
+}
+
+// exclusive scan of colcnt[0..M) in place (colcnt[M] = total), cursor = starts
+__global__ void __launch_bounds__(1024) k_csc_scan(const GridState* __restrict__ gs, int* __restrict__ colcnt,
+                                                   int* __restrict__ cursor)
+{
+    __shared__ int part[1024];
+    const int M = gs->M;
+    const int per = (M + 1023) / 1024;
+    const int a = threadIdx.x * per, b = min(a + per, M);
+    int sum = 0;
+    for (int i = a; i < b; i++) sum += colcnt[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {     // Hillis-Steele inclusive scan
+        int v = (threadIdx.x >= off) ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = part[threadIdx.x] - sum;
+    for (int i = a; i < b; i++) {
+        const int c = colcnt[i];
+        colcnt[i] = run;
+        cursor[i] = run;
+        run += c;
+    }
+    if (threadIdx.x == 1023) colcnt[M] = part[1023];
+}
+
+__global__ void k_csc_fill(const GridState* __restrict__ gs, const int* __restrict__ rowptr,
+                           const int* __restrict__ cidx, const double* __restrict__ cval,
+                           const int* __restrict__ ccnt, int* __restrict__ cursor, int* __restrict__ colrow,
+                           float* __restrict__ colval)
+{
+    const int N = gs->N;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const int b = rowptr[r], n = ccnt[r];
+        for (int e = 0; e < n; e++) {
+            const int pos = atomicAdd(&cursor[cidx[b + e]], 1);
+            colrow[pos] = r;
+            colval[pos] = (float)cval[b + e];
+        }
+    }
+}
+
+// grid (M_cap cells, image-row chunks); chunk rows of 64-bit accumulators
+__global__ void __launch_bounds__(256) k_psf_x(StaticData sd, const GridState* __restrict__ gs,
+                                               const int* __restrict__ colptr, const int* __restrict__ colrow,
+                                               const float* __restrict__ colval, const int* __restrict__ rowpix,
+                                               const int* __restrict__ pixindex, const float* __restrict__ sqc,
+                                               int chunk, float* __restrict__ Xh, float* __restrict__ Xl,
+                                               int K_cap, unsigned char* __restrict__ nz, int nkb_cap)
+{
+    extern __shared__ __align__(16) unsigned char psfx_smem[];
+    long long* acc = reinterpret_cast<long long*>(psfx_smem);
+    float* tpsf = reinterpret_cast<float*>(acc + chunk);
     const int N = gs->N, M = gs->M;
     const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
     const int Np = (N + TC_KB - 1) / TC_KB * TC_KB;
-    const int p0 = blockIdx.x * 32, a0 = blockIdx.y * 32;
-    if (p0 >= Np || a0 >= Mp) return;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
-    __shared__ float sq[32];
-    if (threadIdx.x < 32) sq[threadIdx.x] = (p0 + threadIdx.x < N) ? (float)sqrt(cvec[p0 + threadIdx.x]) : 0.0f;
+    const int s = blockIdx.x;
+    const int r0 = blockIdx.y * chunk, r1 = min(r0 + chunk, Np);
+    if (s >= Mp || r0 >= Np) return;
+    const int nT = sd.pnx * sd.pny;
+    const float scale = ldexpf(1.0f, sd.fix_exp), inv = ldexpf(1.0f, -sd.fix_exp);
+    for (int i = threadIdx.x; i < r1 - r0; i += blockDim.x) acc[i] = 0;
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) tpsf[t] = (float)sd.psf[t];
     __syncthreads();
-    bool any = false;
-    for (int k = ty; k < 32; k += 8) {
-        const int p = p0 + k, a = a0 + tx;
-        float x = 0;
-        if (p < N && a < M) x = L[(size_t)p * ldL + a] * sq[k];
-        const float h = to_tf32(x);
-        const float l = to_tf32(x - h);   // exact: h is x rounded to fewer bits
-        th[k][tx] = h;
-        tl[k][tx] = l;
-        any |= (x != 0.0f);
+    if (s < M) {
+        const int b = colptr[s], n = colptr[s + 1] - b;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        const int nxh = sd.pnx / 2, nyh = sd.pny / 2;
+        for (int e = warp; e < n; e += nw) {
+            const int q = colrow[b + e];
+            const float v = colval[b + e];
+            const int pix = rowpix[q];
+            const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
+            for (int t = lane; t < nT; t += 32) {
+                const int pk = t / sd.pny, pl = t - pk * sd.pny;
+                const int ii = iq - nxh + pk, jj = jq - nyh + pl;
+                if (ii < 0 || ii >= sd.nx || jj < 0 || jj >= sd.ny) continue;
+                const int r = pixindex[ii * sd.ny + jj];
+                if (r < r0 || r >= r1) continue;            // inactive (-1) or another chunk
+                const float x = tpsf[t] * v * sqc[r];
+                atomicAdd(reinterpret_cast<unsigned long long*>(&acc[r - r0]),
+                          (unsigned long long)__float2ll_rn(x * scale));
+            }
+        }
     }
     __syncthreads();
-    for (int k = ty; k < 32; k += 8) {
-        const int a = a0 + k, p = p0 + tx;
-        Xh[(size_t)a * K_cap + p] = th[tx][k];
-        Xl[(size_t)a * K_cap + p] = tl[tx][k];
+    // write row s of X for pixels [r0, r1): hi = x rounded to TF32, lo = the
+    // TF32 rounding of the exact remainder; one warp covers one 32-pixel block
+    const int span = r1 - r0;
+    for (int i0 = 0; i0 < span; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        float h = 0.0f, l = 0.0f;
+        if (i < span) {
+            const long long a = acc[i];
+            h = to_tf32((float)a * inv);
+            const long long rem = a - __float2ll_rn(h * scale);
+            l = to_tf32((float)rem * inv);
+            Xh[(size_t)s * K_cap + r0 + i] = h;
+            Xl[(size_t)s * K_cap + r0 + i] = l;
+        }
+        const unsigned any = __ballot_sync(0xffffffffu, (h != 0.0f) || (l != 0.0f));
+        if ((threadIdx.x & 31) == 0 && any && i < span)
+            nz[(size_t)(s / TC_TILE) * nkb_cap + (r0 + i) / TC_KB] = 1;
     }
-    const int anyb = __syncthreads_or(any ? 1 : 0);
-    if (threadIdx.x == 0 && anyb) nz[(size_t)(a0 / TC_TILE) * nkb_cap + p0 / TC_KB] = 1;
 }
 
 // F32 += lambda R; R32 = R; identity beyond M up to the 64-padding.
@@ -135,9 +243,11 @@ __device__ __forceinline__ int act_at32(const int* ai, int snx, int sny, int i, 
 }
 
 __global__ void k_reg32(const GridState* __restrict__ gs, const int* __restrict__ ai, int snx, int sny,
-                        double regparam, float* __restrict__ F, float* __restrict__ R, int ld, int do_reg)
+                        const double* __restrict__ regp, float* __restrict__ F, float* __restrict__ R, int ld,
+                        int do_reg)
 {
-    const int M = gs->M, Mp = (M + 63) & ~63;
+    const double regparam = *regp;
+    const int M = gs->M, Mp = (M + 127) & ~127;   // identity up to the 128-block padding
     const int ncell = snx * sny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
         if (c >= ncell) {
@@ -195,8 +305,10 @@ __global__ void k_axpy(const GridState* __restrict__ gs, const double* __restric
 // r = D - v - lambda R s   (v = L'^T C^-1 L' s; R applied by its stencil)
 __global__ void k_residual(const GridState* __restrict__ gs, const double* __restrict__ D,
                            const double* __restrict__ vv, const int* __restrict__ ai, int snx, int sny,
-                           double regparam, int do_reg, const double* __restrict__ s, double* __restrict__ r)
+                           const double* __restrict__ regp, int do_reg, const double* __restrict__ s,
+                           double* __restrict__ r)
 {
+    const double regparam = *regp;
     const int M = gs->M;
     const int ncell = snx * sny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
@@ -227,8 +339,9 @@ void mixed_free(Slot& c)
 {
     MixedWork* m = mw_of(c);
     if (!m) return;
-    void* ptrs[] = {m->L32, m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
-                    m->linvF, m->linvR};
+    void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
+                    m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
+                    m->sqc};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
     c.mixed = nullptr;
@@ -254,7 +367,13 @@ int mixed_init(Slot& c)
     A((void**)&m->nz, (size_t)(M_cap / TC_TILE) * m->nkb_cap);
     A((void**)&m->F32, sizeof(float) * (size_t)M_cap * M_cap);
     A((void**)&m->R32, sizeof(float) * (size_t)M_cap * M_cap);
-    A((void**)&m->L32, sizeof(float) * (size_t)c.N_cap * M_cap);
+    m->nnz_cap = 3 * c.N_cap * c.nsub_cap;
+    m->chunk = std::min(K_cap, 24576);
+    A((void**)&m->colcnt, sizeof(int) * (size_t)(M_cap + 1));
+    A((void**)&m->cursor, sizeof(int) * (size_t)M_cap);
+    A((void**)&m->colrow, sizeof(int) * (size_t)m->nnz_cap);
+    A((void**)&m->colval, sizeof(float) * (size_t)m->nnz_cap);
+    A((void**)&m->sqc, sizeof(float) * (size_t)(c.N_cap + 64));
     A((void**)&m->t, sizeof(double) * (size_t)(c.N_cap + 64));
     A((void**)&m->u, sizeof(double) * (size_t)(c.N_cap + 64));
     A((void**)&m->v, sizeof(double) * M_cap);
@@ -262,8 +381,12 @@ int mixed_init(Slot& c)
     A((void**)&m->z, sizeof(double) * M_cap);
     A((void**)&m->y, sizeof(double) * M_cap);
     A((void**)&m->part, sizeof(double) * (size_t)M_cap * (ltw_chunks(c.N_cap) + 1));
-    A((void**)&m->linvF, sizeof(float) * (size_t)M_cap * 64);
-    A((void**)&m->linvR, sizeof(float) * (size_t)M_cap * 64);
+    m->nb = M_cap / C2;
+    A((void**)&m->linvF, sizeof(float) * (size_t)m->nb * 2 * C2 * C2);
+    A((void**)&m->linv128, sizeof(float) * 2 * C2 * C2);
+    A((void**)&m->yf, sizeof(float) * (size_t)M_cap);
+    A((void**)&m->zf, sizeof(float) * (size_t)M_cap);
+    A((void**)&m->flags, sizeof(int) * (size_t)2 * m->nb);
     if (e != cudaSuccess) {
         set_error("%s (%d)", "mixed-precision workspace allocation failed", (int)e);
         return QLP_ERR_NOMEM;
@@ -274,38 +397,41 @@ int mixed_init(Slot& c)
         set_error("%s (%d)", "cuTensorMapEncodeTiled unavailable or failed", 0);
         return QLP_ERR_CUDA;
     }
+    cudaFuncSetAttribute(k_psf_x, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
+    cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
     cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     cudaFuncSetAttribute(k_chol_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM);
-    solve_init_attributes<float>();
     m->ready = true;
     return QLP_OK;
 }
 
-// FP32 blocked Cholesky for the mixed path: shared-memory potrf of each 64x64
-// diagonal tile, per-row triangular solve of the tiles below it, the trailing
-// update on the tensor cores, then all diagonal inverses in one launch.
-static int cholesky_mixed(float* A, int ld, int M_cap, GridState* gs, int which, cudaStream_t st, float* Linv)
+// FP32 blocked Cholesky for the mixed path (chol128.cuh): per 128-column step
+// the diagonal factor and its inverse in one CTA, the panel solve and the
+// trailing update on the tensor cores.  band: 128-blocks below the diagonal
+// that can be nonzero (the whole matrix for F).  The inverse of diagonal
+// block k goes to linv + k * linv_stride (stride 0: one scratch block).
+static int cholesky_mixed(float* A, int ld, int M_cap128, GridState* gs, int which, int band, float* linv,
+                          size_t linv_stride, cudaStream_t st)
 {
-    const int nbm = (M_cap + CB - 1) / CB;
+    const int nb = M_cap128 / C2;
     int n = 0;
-    for (int k = 0; k < nbm; k++) {
-        const int rem = nbm - k - 1;
-        k_potrf_t<float><<<1, 256, 0, st>>>(A, ld, k, gs, which, nullptr);
+    for (int k = 0; k < nb; k++) {
+        float* lk = linv + (size_t)k * linv_stride;
+        k_potrf128<<<1, 256, P128_SMEM, st>>>(A, ld, k, gs, which, lk);
         n++;
-        if (rem > 0) {
-            k_trsm_rows<<<rem, CB, 0, st>>>(A, ld, k, gs);
-            const int nt = (rem * CB + TC_TILE - 1) / TC_TILE;
-            k_chol_update_tc<<<nt * (nt + 1) / 2, 128, UPD_SMEM, st>>>(A, ld, k, gs);
-            n += 2;
-        }
+        const int rem = nb - k - 1;
+        if (rem == 0) break;
+        const int bt = std::min(rem, band);
+        k_chol_tile128<<<bt, 128, T128_SMEM, st>>>(A, ld, k, gs, 1, lk, band);
+        k_chol_tile128<<<bt * (bt + 1) / 2, 128, T128_SMEM, st>>>(A, ld, k, gs, 0, lk, band);
+        n += 2;
     }
-    k_diag_inverse<float><<<nbm, CB, 0, st>>>(A, ld, gs, Linv);
-    n++;
     count_launches(n);
     return n;
 }
 
-int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, double regparam, cudaStream_t st,
+int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, cudaStream_t st,
                         cudaEvent_t* ev)
 {
     int rc = mixed_init(slot);
@@ -319,13 +445,25 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, dou
     // D = L^T P^T (C^-1 d), FP64
     op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, st);
     op_LTw(w, N_cap, m->M_cap, m->t, m->part, w.D, st);
-    // L'32, then X and the block flags
-    launch_psf32(sd, w, m->L32, m->ld32, m->M_cap, st);
+    // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
     cudaMemsetAsync(m->nz, 0, (size_t)(m->M_cap / TC_TILE) * m->nkb_cap, st);
+    cudaMemsetAsync(m->colcnt, 0, sizeof(int) * (size_t)(m->M_cap + 1), st);
     {
-        dim3 g(m->K_cap / 32, m->M_cap / 32);
-        k_convert_x<<<g, 256, 0, st>>>(w.gs, m->L32, m->ld32, w.cvec, m->X_hi, m->X_lo, m->K_cap, m->nz, m->nkb_cap);
-        n++;
+        const int rb = std::min((N_cap + 255) / 256, 152 * 8);
+        k_csc_count<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, w.cvec, m->colcnt, m->sqc);
+        k_csc_scan<<<1, 1024, 0, st>>>(w.gs, m->colcnt, m->cursor);
+        k_csc_fill<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.cval, w.ccnt, m->cursor, m->colrow,
+                                                    m->colval);
+        // accumulator rows per CTA: all pixels if they fit beside the PSF in 227 KB
+        const int nT = sd.pnx * sd.pny;
+        const int fit = (int)(((227 * 1024 - sizeof(float) * (size_t)nT) / sizeof(long long)) & ~(size_t)31);
+        const int chunk = std::max(32, std::min(m->chunk, fit));
+        const int nchunk = (m->K_cap + chunk - 1) / chunk;
+        const size_t smem = sizeof(long long) * (size_t)chunk + sizeof(float) * (size_t)nT;
+        k_psf_x<<<dim3(m->M_cap, nchunk), 256, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
+                                                            w.pixindex, m->sqc, chunk, m->X_hi, m->X_lo,
+                                                            m->K_cap, m->nz, m->nkb_cap);
+        n += 4;
     }
     if (ev) cudaEventRecord(ev[3], st);
     {
@@ -336,33 +474,43 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, dou
     }
     if (ev) cudaEventRecord(ev[4], st);
     if (so.regularization) cudaMemsetAsync(m->R32, 0, sizeof(float) * (size_t)m->ld32 * m->ld32, st);
-    k_reg32<<<(so.snx * so.sny + 64 + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regparam,
+    k_reg32<<<(so.snx * so.sny + 128 + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regp,
                                                                 m->F32, m->R32, m->ld32, so.regularization);
     n++;
     if (so.regularization) {
-        n += cholesky_mixed(m->R32, m->ld32, Mc, w.gs, 1, st, m->linvR);
-        k_logdet_t<float><<<1, 1024, 0, st>>>(m->R32, m->ld32, w.gs, w.out, 1);
+        // R's factorisation (log det R only) runs on the slot's second stream,
+        // beside F's.  R couples a cell to cells at most two grid rows
+        // (2 snx active indices) away, so its factor stays within that band.
+        cudaEventRecord(slot.side_fork, st);
+        cudaStreamWaitEvent(slot.side, slot.side_fork, 0);
+        const int band_R = (2 * so.snx - 1) / C2 + 1;
+        n += cholesky_mixed(m->R32, m->ld32, m->M_cap, w.gs, 1, band_R, m->linv128, 0, slot.side);
+        k_logdet_t<float><<<1, 1024, 0, slot.side>>>(m->R32, m->ld32, w.gs, w.out, 1);
         n++;
+        cudaEventRecord(slot.side_join, slot.side);
     }
-    n += cholesky_mixed(m->F32, m->ld32, Mc, w.gs, 0, st, m->linvF);
+    n += cholesky_mixed(m->F32, m->ld32, m->M_cap, w.gs, 0, 1 << 20, m->linvF, (size_t)2 * C2 * C2, st);
     k_logdet_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, w.out, 0);
     n++;
+    if (so.regularization) cudaStreamWaitEvent(st, slot.side_join, 0);
     // s = F^-1 D with two FP64 refinement sweeps
     k_copy_init<<<(Mc + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->r, w.s);
     n++;
     const int refine = 2;
     for (int it = 0; it <= refine; it++) {
-        k_solve_t<float><<<1, 1024, solve_smem_bytes<float>(Mc), st>>>(m->F32, m->ld32, m->linvF, w.gs, m->r, m->z,
-                                                                      Mc);
+        cudaMemsetAsync(m->flags, 0, sizeof(int) * (size_t)2 * m->nb, st);
+        k_trsv128_fwd<<<m->nb, 256, 0, st>>>(m->F32, m->ld32, m->linvF, w.gs, m->r, m->yf, m->flags);
+        k_trsv128_bwd<<<m->nb, 256, 0, st>>>(m->F32, m->ld32, m->linvF, w.gs, m->yf, m->zf, m->z,
+                                              m->flags + m->nb);
         k_axpy<<<(Mc + 255) / 256, 256, 0, st>>>(w.gs, m->z, w.s);
-        n += 2;
+        n += 3;
         if (it == refine) break;
         op_Ls(w, N_cap, w.s, m->t, st);
         op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, st);
         op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, st);
         op_LTw(w, N_cap, m->M_cap, m->t, m->part, m->v, st);
         k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, so.snx, so.sny,
-                                                                  regparam, so.regularization, w.s, m->r);
+                                                                  regp, so.regularization, w.s, m->r);
         n++;
     }
     // model image P L s in FP64 for chi^2

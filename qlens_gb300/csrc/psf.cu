@@ -10,10 +10,9 @@
 // accumulates in shared memory; taps are separated by __syncwarp so the
 // per-entry order is the reference's.  Built with --fmad=false.
 //
-// The accumulator type is a template parameter: double for the plain path
-// (bit-exact rows), float for the mixed-precision path, whose dense L' only
-// feeds the TF32 tensor-core SYRK (every FP64 product of the mixed path goes
-// through the sparse operators of sparseops.cu instead).
+// The accumulator type is a template parameter; the plain path instantiates
+// double (bit-exact rows).  The mixed path builds its TF32 operand column by
+// column instead (k_psf_x, mixed.cu).
 #include "qlpix_internal.h"
 
 namespace qlpix {
@@ -107,7 +106,6 @@ __global__ void k_rowpix(StaticData sd, const int* __restrict__ rowidx, int* __r
 void psf_init_attributes()
 {
     cudaFuncSetAttribute(k_psf<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_psf<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
 template <typename T>
@@ -143,12 +141,6 @@ void launch_psf(const StaticData& sd, const SrcOpts& so, Work& w, int M_max, cud
 {
     (void)so;
     launch_psf_t<double>(sd, w, w.Lpsf, w.ldL, M_max, st);
-    count_launches(1);
-}
-
-void launch_psf32(const StaticData& sd, Work& w, float* out, int ld, int M_max, cudaStream_t st)
-{
-    launch_psf_t<float>(sd, w, out, ld, M_max, st);
     count_launches(1);
 }
 

@@ -189,6 +189,21 @@ int qlp_set_batch_slots(qlp_ctx* c, int slots)
     return QLP_OK;
 }
 
+int qlp_set_graphs(qlp_ctx* c, int on)
+{
+    if (!c) return fail(QLP_ERR_ARG, "null context");
+    c->use_graphs = on ? 1 : 0;
+    return QLP_OK;
+}
+
+int qlp_last_transfer_bytes(const qlp_ctx* c, long long* h2d, long long* d2h)
+{
+    if (!c || !h2d || !d2h) return fail(QLP_ERR_ARG, "bad arguments");
+    *h2d = c->last_h2d;
+    *d2h = c->last_d2h;
+    return QLP_OK;
+}
+
 int qlp_n_params(const qlp_ctx* c)
 {
     if (!c) return 0;

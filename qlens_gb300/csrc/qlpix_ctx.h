@@ -6,7 +6,7 @@
 #include "qlpix_internal.h"
 
 #define QLP_N_STAGES 6
-#define QLP_MAX_SLOTS 32
+#define QLP_MAX_SLOTS 64
 
 namespace qlpix {
 
@@ -24,6 +24,15 @@ struct Slot {
     int snx_cap = 0, sny_cap = 0;
     bool fp64_mats = false;         // F and R in FP64 allocated
     cudaEvent_t done = nullptr;
+    // second stream of the slot: R's factorisation runs beside F's
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
+    // the launch sequence captured as a CUDA graph, valid for one
+    // (precision, mask, source grid, NFW) combination and graph generation
+    cudaGraphExec_t graph = nullptr;
+    int graph_key[5] = {0, 0, 0, 0, 0};
+    long long graph_gen = 0;
+    long long graph_launches = 0;   // kernels per replay
 };
 
 }  // namespace qlpix
@@ -62,11 +71,14 @@ struct qlp_ctx {
 
     qlpix::EvalOut* h_out = nullptr;      // pinned, one per batch instance
     int h_out_cap = 0;
-    qlpix::EvalOut* d_res = nullptr;
-    int d_res_cap = 0;
     cudaEvent_t ev[QLP_N_STAGES + 1] = {};
     cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<cudaEvent_t> ev_pool;     // (QLP_N_STAGES+1) per batched instance
+    qlpix::EvalParams* h_ep = nullptr;    // pinned, one per batch instance
+    int h_ep_cap = 0;
+    int use_graphs = 1;                   // batched evaluation replays captured graphs
+    long long graph_gen = 1;              // bumped whenever captured graphs go stale
+    long long last_h2d = 0, last_d2h = 0; // bytes moved by the last call
     float stage_ms[QLP_N_STAGES] = {};
     float device_ms = 0;
     long long last_launches = 0;
@@ -88,6 +100,6 @@ void set_error(const char* fmt, const char* a, int code);
 // mixed.cu
 int mixed_init(Slot& slot);
 void mixed_free(Slot& slot);
-int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, double regparam, cudaStream_t st,
+int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, cudaStream_t st,
                         cudaEvent_t* ev);
 }  // namespace qlpix

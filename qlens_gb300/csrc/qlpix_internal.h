@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stddef.h>
 #include "../../include/qlpix.h"
 
 namespace qlpix {
@@ -27,6 +28,15 @@ struct LensModel {
     double zfac[QLP_MAX_PLANES];
     double beta[QLP_MAX_PLANES][QLP_MAX_PLANES];
     LensRec lens[QLP_MAX_LENSES];
+};
+
+// What changes from one evaluation to the next: the lens model (meta
+// parameters computed on the host) and the regularisation parameter.  Kept in
+// device memory, one copy per slot, so that one captured launch sequence (a
+// CUDA graph) serves every evaluation a slot runs.
+struct EvalParams {
+    LensModel lm;
+    double regparam;
 };
 
 // Source-grid state computed on the device each evaluation.
@@ -60,6 +70,9 @@ struct StaticData {            // per-context, uploaded once
     const double* covinv;      // nx*ny (filled with cov_inverse when uniform)
     const int* mpix;           // n_mask: i*ny+j, j-outer / i-inner order
     const double* psf;         // pnx*pny
+    // fixed-point scale of the mixed path's L' accumulation: 2^fix_exp keeps
+    // sum|psf| * max sqrt(C^-1) (a bound on every |L' sqrt(C^-1)| entry) below 2^61
+    int fix_exp;
 };
 
 struct SrcOpts {
@@ -99,18 +112,24 @@ struct Work {
     double* partial;                   // reduction scratch
     double* linv;                      // 64x64 inverse of the current diagonal Cholesky block
     GridState* gs;
-    EvalOut* out;
+    EvalOut* out;                      // this slot's result (copied to the host after each evaluation)
+    EvalParams* ep;                    // this slot's per-evaluation parameters
 };
 
+// Device address of the regularisation parameter of a slot's EvalParams.
+inline const double* regparam_dev(const Work& w)
+{
+    return reinterpret_cast<const double*>(reinterpret_cast<const char*>(w.ep) + offsetof(EvalParams, regparam));
+}
+
 // ---- kernels (launch wrappers implemented in the .cu files) ----
-void launch_raytrace(const StaticData& sd, const LensModel& lm, Work& w, cudaStream_t st);
+void launch_raytrace(const StaticData& sd, bool nfw, Work& w, cudaStream_t st);
 void launch_grid(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_locate(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_build_L(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_rowpix(const StaticData& sd, Work& w, cudaStream_t st);
 void launch_psf(const StaticData& sd, const SrcOpts& so, Work& w, int M_max, cudaStream_t st);
-void launch_psf32(const StaticData& sd, Work& w, float* out, int ld, int M_max, cudaStream_t st);
 void op_Ls(Work& w, int N_cap, const double* s, double* t, cudaStream_t st);
 void op_conv(const StaticData& sd, Work& w, int N_cap, bool transpose, const double* in, const double* scale_in,
              double* out, cudaStream_t st);
@@ -119,13 +138,13 @@ int ltw_chunks(int N_cap);
 void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st);
 void launch_D(Work& w, int N_max, int M_max, cudaStream_t st);
 void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st);
-void launch_regularization(const SrcOpts& so, Work& w, int M_max, double regparam, cudaStream_t st);
+void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* regp, cudaStream_t st);
 int  launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, double* linv,
                           cudaStream_t st);
 void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st);
 void launch_solve_fp64(Work& w, int M_max, cudaStream_t st);
 void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max,
-                       double regparam, cudaStream_t st, bool model_ready = false);
+                       const double* regp, cudaStream_t st, bool model_ready = false);
 void init_kernel_attributes();
 long long kernel_launch_counter();
 void count_launches(int n);

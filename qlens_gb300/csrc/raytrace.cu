@@ -14,9 +14,17 @@
 namespace qlpix {
 
 template <bool NFW>
-__global__ void __launch_bounds__(256) k_raytrace(StaticData sd, LensModel lm, double* __restrict__ spx,
-                                                  double* __restrict__ spy)
+__global__ void __launch_bounds__(256) k_raytrace(StaticData sd, const EvalParams* __restrict__ ep,
+                                                  double* __restrict__ spx, double* __restrict__ spy)
 {
+    // the lens model of this evaluation, staged in shared memory
+    __shared__ __align__(16) LensModel lm;
+    {
+        const double* src = reinterpret_cast<const double*>(&ep->lm);
+        double* dst = reinterpret_cast<double*>(&lm);
+        for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
     const int ns = sd.nsplit, nsub = sd.nsub;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < sd.n_sub; t += gridDim.x * blockDim.x) {
         int m = t / nsub, k = t - m * nsub;
@@ -34,14 +42,13 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd, LensModel lm, d
     }
 }
 
-void launch_raytrace(const StaticData& sd, const LensModel& lm, Work& w, cudaStream_t st)
+// nfw: the model has an NFW lens (selects the kernel with the quadrature)
+void launch_raytrace(const StaticData& sd, bool nfw, Work& w, cudaStream_t st)
 {
     if (sd.n_sub == 0) return;
     int blocks = (sd.n_sub + 255) / 256;
-    bool nfw = false;
-    for (int k = 0; k < lm.nlens; k++) nfw |= (lm.lens[k].type == QLP_LENS_NFW);
-    if (nfw) k_raytrace<true><<<blocks, 256, 0, st>>>(sd, lm, w.spx, w.spy);
-    else k_raytrace<false><<<blocks, 256, 0, st>>>(sd, lm, w.spx, w.spy);
+    if (nfw) k_raytrace<true><<<blocks, 256, 0, st>>>(sd, w.ep, w.spx, w.spy);
+    else k_raytrace<false><<<blocks, 256, 0, st>>>(sd, w.ep, w.spx, w.spy);
     count_launches(1);
 }
 

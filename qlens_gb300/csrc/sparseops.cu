@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) k_conv(StaticData sd, const GridState* __
 }
 
 // partial[chunk][s] = sum over the chunk's rows r (in order) of cval * w[r]
-#define LTW_CHUNK 256
+#define LTW_CHUNK 64
 __global__ void __launch_bounds__(32) k_LTw_chunk(const GridState* __restrict__ gs, const int* __restrict__ rowptr,
                                                   const int* __restrict__ cidx, const double* __restrict__ cval,
                                                   const int* __restrict__ ccnt, const double* __restrict__ w,

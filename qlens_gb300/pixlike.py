@@ -59,6 +59,8 @@ def load_library(build_if_missing=False):
     L.qlp_last_device_time.argtypes = [C.c_void_p, P(C.c_float)]
     L.qlp_last_launch_count.restype = C.c_longlong
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
+    L.qlp_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_last_transfer_bytes.argtypes = [C.c_void_p, P(C.c_longlong), P(C.c_longlong)]
     L.qlp_spd_solve_logdet_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p]
     L.qlp_last_error.restype = C.c_char_p
@@ -159,6 +161,16 @@ class PixelLikelihood:
 
     def set_batch_slots(self, n):
         self._check(self.lib.qlp_set_batch_slots(self.ctx, int(n)))
+
+    def set_graphs(self, on):
+        """Replay captured CUDA graphs in eval_batch (default) or launch kernel by kernel."""
+        self._check(self.lib.qlp_set_graphs(self.ctx, 1 if on else 0))
+
+    def last_transfer_bytes(self):
+        """(host->device, device->host) bytes moved by the last call."""
+        h, d = C.c_longlong(), C.c_longlong()
+        self._check(self.lib.qlp_last_transfer_bytes(self.ctx, C.byref(h), C.byref(d)))
+        return h.value, d.value
 
     def set_lens_model(self, spec, zfac=None, beta=None):
         self.lens_spec = spec
