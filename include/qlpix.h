@@ -56,6 +56,9 @@ extern "C" {
 #define QLP_MAX_PARAMS 8
 
 /* ---- precision modes ---- */
+#define QLP_NFW_QUADRATURE 0  /* NFW deflection by QLens's adaptive Gauss-Patterson quadrature */
+#define QLP_NFW_SURROGATE  1  /* the trained MLP, quadrature where its error bound is exceeded */
+
 #define QLP_FP64  0  /* plain FP64 everywhere */
 #define QLP_MIXED 1  /* FP32-class tensor-core SYRK + Cholesky, FP64 refinement/logdet/sums */
 
@@ -115,7 +118,26 @@ typedef struct {
     long long L_nnz;      /* nonzeros of the pre-PSF L */
     int status;
     int refine_iters;     /* FP64 refinement sweeps used (mixed precision) */
+    int nfw_fallbacks;    /* rays that took the NFW quadrature instead of the surrogate */
 } qlp_result;
+
+/* Training of the NFW deflection surrogate (qlp_nfw_surrogate_train). */
+typedef struct {
+    int n_train;                 /* quadrature samples to train on (default 1 << 20) */
+    int batch;                   /* samples per Adam step (default 16384) */
+    int steps;                   /* Adam steps (default 30000) */
+    double lr;                   /* peak learning rate: 2 % warm-up, cosine decay to 0.1 % (default 3e-3) */
+    unsigned long long seed;     /* samples and initial weights (default 1) */
+} qlp_surrogate_opts;
+
+typedef struct {
+    double final_loss;           /* weighted mean squared error of the last training batch */
+    double val_max_rel;          /* largest relative error of G_0, G_1 on the validation grid */
+    double val_mean_rel;         /* mean over the grid cells of their largest relative error */
+    double cells_below_1e5;      /* fraction of cells whose bound is <= 1e-5 */
+    double train_ms;             /* wall time of sample generation, training and validation */
+    int n_params, n_train, steps;
+} qlp_surrogate_report;
 
 /* Per-instance description for batched evaluation (uneven masks / grids). */
 typedef struct {
@@ -205,6 +227,37 @@ int qlp_stage_times(qlp_ctx* ctx, float* ms, int n);
 /* Device time in milliseconds from the first to the last kernel of the last
  * qlp_eval / qlp_eval_batch. */
 int qlp_last_device_time(qlp_ctx* ctx, float* ms);
+
+/* ---- learned NFW deflection (no counterpart in the reference: QLens
+ * always integrates, LensProfile::deflection_numerical, profile.cpp:2359) ----
+ * Defaults for qlp_nfw_surrogate_train. */
+void qlp_surrogate_defaults(qlp_surrogate_opts* opts);
+
+/* Train the NFW deflection surrogate on `device` (once per process and device;
+ * every context on that device shares it): samples from the GPU quadrature,
+ * Adam on the project's own forward/backward kernels, then the per-cell error
+ * bounds from the tensor-core inference path.  rep may be NULL. */
+int qlp_nfw_surrogate_train(int device, const qlp_surrogate_opts* opts, qlp_surrogate_report* rep);
+
+/* QLP_NFW_QUADRATURE (default) or QLP_NFW_SURROGATE (needs a trained
+ * surrogate on the context's device).  threshold_arcsec: a ray whose bound on
+ * the surrogate's deflection error exceeds it takes the quadrature (<= 0
+ * gives 2e-5; at 1e-4 the NFW golden case moves |log L| by up to 0.11).
+ * Applies to NFW lenses with q < 1. */
+int qlp_set_nfw_mode(qlp_ctx* ctx, int mode, double threshold_arcsec);
+
+/* Test hooks of the surrogate.  qlp_surrogate_grad_check: one forward and
+ * backward pass of the training kernels (params [50306], x [batch][3],
+ * t [batch][2], both as the network sees them) -> loss and grad [50306].
+ * qlp_surrogate_eval: the network through the inference path at n points
+ * (log R, phi, q) [n][3] -> t [n][2] = log(G/B), with the quadrature's G [n][2],
+ * the baselines B [n] and the relative error bound of each point's cell [n]
+ * (infinite outside the trained domain) for the same points (G, B, bound may
+ * be NULL). */
+int qlp_surrogate_grad_check(int device, const float* params, const float* x, const float* t, int batch,
+                             double* loss, float* grad);
+int qlp_surrogate_eval(int device, const double* rho_phi_q, int n, double* t, double* G, double* B,
+                       double* bound);
 
 /* Number of kernels run by the last qlp_eval / qlp_eval_batch (launched
  * directly or replayed from a graph). */

@@ -1,4 +1,5 @@
-"""Python loader for the C oracle (oracle/qlpix_oracle.c).
+"""Python loader for the C oracle (oracle/qlpix_oracle.c, nfw_oracle.c,
+mlp_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
 baseline legs of bench.py as the checker.  The product never imports it.
@@ -14,7 +15,8 @@ from qlens_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqlpix_oracle.so")
-SOURCES = [os.path.join(HERE, "qlpix_oracle.c"), os.path.join(HERE, "nfw_oracle.c")]
+SOURCES = [os.path.join(HERE, "qlpix_oracle.c"), os.path.join(HERE, "nfw_oracle.c"),
+           os.path.join(HERE, "mlp_oracle.c")]
 
 
 def build(force=False):
@@ -48,6 +50,11 @@ def lib():
         _lib.oracle_get.restype = C.c_long
         _lib.oracle_get.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
         _lib.oracle_threads.restype = C.c_int
+        _lib.oracle_mlp_n_params.restype = C.c_int
+        _lib.oracle_mlp_loss_grad.restype = C.c_double
+        _lib.oracle_mlp_loss_grad.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double)]
     return _lib
 
 
@@ -84,3 +91,18 @@ def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.
 
 def threads():
     return lib().oracle_threads()
+
+
+def mlp_loss_grad(params, x, t):
+    """Surrogate network in double precision (mlp_oracle.c): returns
+    (loss, dloss/dparams, outputs) for params [n_params], x [n][3], t [n][2]."""
+    L = lib()
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    assert p.shape == (L.oracle_mlp_n_params(),)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    g = np.empty_like(p)
+    y = np.empty((x.shape[0], 2))
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    loss = L.oracle_mlp_loss_grad(dp(p), x.shape[0], dp(x), dp(t), dp(g), dp(y))
+    return loss, g, y

@@ -23,6 +23,9 @@ QLP_MAX_PARAMS = 8
 QLP_FP64 = 0
 QLP_MIXED = 1
 
+QLP_NFW_QUADRATURE = 0
+QLP_NFW_SURROGATE = 1
+
 LENS_TYPES = {"sple": QLP_LENS_SPLE, "shear": QLP_LENS_SHEAR, "nfw": QLP_LENS_NFW}
 N_PARAMS = {QLP_LENS_SPLE: 7, QLP_LENS_SHEAR: 4, QLP_LENS_NFW: 6}
 
@@ -63,7 +66,21 @@ class qlp_result(C.Structure):
     _fields_ = [("m2logev", C.c_double), ("chisq0", C.c_double), ("logdet_F", C.c_double),
                 ("logdet_R", C.c_double), ("Es_times_two", C.c_double), ("regterms", C.c_double),
                 ("n_active_pixels", C.c_int), ("n_active_src", C.c_int), ("L_nnz", C.c_longlong),
-                ("status", C.c_int), ("refine_iters", C.c_int)]
+                ("status", C.c_int), ("refine_iters", C.c_int), ("nfw_fallbacks", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class qlp_surrogate_opts(C.Structure):
+    _fields_ = [("n_train", C.c_int), ("batch", C.c_int), ("steps", C.c_int), ("lr", C.c_double),
+                ("seed", C.c_ulonglong)]
+
+
+class qlp_surrogate_report(C.Structure):
+    _fields_ = [("final_loss", C.c_double), ("val_max_rel", C.c_double), ("val_mean_rel", C.c_double),
+                ("cells_below_1e5", C.c_double), ("train_ms", C.c_double), ("n_params", C.c_int),
+                ("n_train", C.c_int), ("steps", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -30,10 +30,11 @@ UNITS = [
     ("sparseops.cu", []),
     ("noalloc.cu", []),
     ("mixed.cu", []),
+    ("surrogate.cu", ["--fmad=false"]),
     ("ctx.cpp", []),
     ("qlpix_api.cpp", []),
 ]
-HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_syrk.cuh"]
+HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_common.cuh", "tc_syrk.cuh"]
 
 
 def _newer(src, obj, deps):

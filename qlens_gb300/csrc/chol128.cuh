@@ -21,7 +21,7 @@
 // negative pivot is recorded and sqrt(|d|) used; the first such pivot is
 // reported through GridState::not_spd_F / not_spd_R.
 #pragma once
-#include "tc_syrk.cuh"
+#include "tc_common.cuh"
 
 namespace qlpix {
 

@@ -45,7 +45,8 @@ static void free_work(Work& w)
 {
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
-                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep};
+                    w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep,
+                    w.fb_ray, w.fb_xy, w.fb_count};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
@@ -96,6 +97,7 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     CK(dalloc(&w.partial, part), "alloc");
     CK(dalloc(&w.linv, (size_t)Mc * 64), "alloc");
     CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc"); CK(dalloc(&w.ep, 1), "alloc");
+    CK(dalloc(&w.fb_ray, n_sub), "alloc"); CK(dalloc(&w.fb_xy, 2 * n_sub), "alloc"); CK(dalloc(&w.fb_count, 1), "alloc");
     s.M_cap = Mc;
     s.N_cap = n_mask;
     s.nsub_cap = nsub;
@@ -266,7 +268,18 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     const double* regp = regparam_dev(w);
     cudaMemsetAsync(w.out, 0, sizeof(EvalOut), st);
     if (ev) cudaEventRecord(ev[0], st);
-    launch_raytrace(sd, model_has_nfw(c), w, st);
+    if (c->nfw_mode == QLP_NFW_SURROGATE && model_has_nfw(c)) {
+        // a single NFW lens on the last plane: its quadrature fallbacks can run
+        // afterwards in their own kernel (nothing downstream needs them)
+        int defer = -1, n_nfw = 0;
+        for (int k = 0; k < (int)c->lenses.size(); k++)
+            if (c->lenses[k].type == QLP_LENS_NFW) { n_nfw++; defer = k; }
+        if (n_nfw != 1 || c->lenses[defer].plane != c->planes.n_planes - 1) defer = -1;
+        int r = launch_raytrace_sur(sd, w, c->nfw_threshold, defer, st);
+        if (r != QLP_OK) return r;
+    } else {
+        launch_raytrace(sd, model_has_nfw(c), w, st);
+    }
     if (ev) cudaEventRecord(ev[1], st);
     launch_grid(sd, so, w, st);
     launch_locate(sd, so, w, st);
@@ -311,7 +324,7 @@ static int prepare_slot(qlp_ctx* c, Slot& s)
 }
 
 // Capture the slot's launch sequence for this (mask, source grid) as a graph.
-static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const int key[5])
+static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const int key[6])
 {
     drop_graph(s);
     int r = prepare_slot(c, s);
@@ -328,7 +341,7 @@ static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpt
     e = cudaGraphInstantiate(&s.graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { s.graph = nullptr; return cuda_fail(e, "graph instantiate"); }
-    for (int i = 0; i < 5; i++) s.graph_key[i] = key[i];
+    for (int i = 0; i < 6; i++) s.graph_key[i] = key[i];
     s.graph_gen = c->graph_gen;
     s.graph_launches = n;
     return QLP_OK;
@@ -341,9 +354,9 @@ static int issue_eval(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& 
 {
     CK(cudaMemcpyAsync(s.w.ep, h_ep, sizeof(EvalParams), cudaMemcpyHostToDevice, s.stream), "h2d");
     if (c->use_graphs && ev == nullptr) {
-        const int key[5] = {c->precision, mask_id, so.snx, so.sny, model_has_nfw(c) ? 1 : 0};
+        const int key[6] = {c->precision, mask_id, so.snx, so.sny, model_has_nfw(c) ? 1 : 0, c->nfw_mode};
         bool ok = s.graph && s.graph_gen == c->graph_gen;
-        for (int i = 0; ok && i < 5; i++) ok = (s.graph_key[i] == key[i]);
+        for (int i = 0; ok && i < 6; i++) ok = (s.graph_key[i] == key[i]);
         if (!ok) {
             int r = capture_graph(c, s, sd, so, key);
             if (r != QLP_OK) return r;
@@ -374,6 +387,7 @@ static void fill_result(const EvalOut& o, qlp_result* out)
     out->L_nnz = o.L_nnz;
     out->status = o.status;
     out->refine_iters = o.refine_iters;
+    out->nfw_fallbacks = o.pad;
 }
 
 static int ensure_results(qlp_ctx* c, int n)

@@ -401,7 +401,6 @@ int mixed_init(Slot& c)
     cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
     cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
     cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    cudaFuncSetAttribute(k_chol_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM);
     m->ready = true;
     return QLP_OK;
 }

@@ -68,20 +68,12 @@ static __device__ __noinline__ void nfw_node(const LensRec& L, double xsq, doubl
     f1 = t / (qfac * sq);
 }
 
-static __device__ void nfw_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+// The two Patterson integrals of LensIntegral::j_integral for lens-frame
+// (x^2, y^2): I_n = 0.5 * sum_level(w_j f_n(node_j)) at the level where that
+// integral converged to `tol` (QLens: 1e-3).  The deflection is
+// alpha_x = x sqrt(1-eps) I_0, alpha_y = y sqrt(1-eps) I_1.
+static __device__ void nfw_integrals(const LensRec& L, double xsq, double ysq, double tol, double& I0, double& I1)
 {
-    if (L.q == 1.0) {
-        double kapavg = nfw_kapavg_spherical_rsq(L.ks, L.rs, x * x + y * y);
-        dx = kapavg * x;
-        dy = kapavg * y;
-        return;
-    }
-    if ((fabs(x) < 1e-14) && (fabs(y) < 1e-14)) {
-        dx = 0;
-        dy = 0;
-        return;
-    }
-    const double xsq = x * x, ysq = y * y;
     double keep0[NFW_KEEP], keep1[NFW_KEEP];   // values at nodes of levels <= 5, slot (i+1)/8 - 1
     double r0 = 0, r1 = 0, old0, old1;
     bool done0 = false, done1 = false;
@@ -111,16 +103,35 @@ static __device__ void nfw_deflection(const LensRec& L, double x, double y, doub
         }
         if (!done0) {
             r0 = s0;
-            if ((level > 1) && (fabs(r0 - old0) < NFW_PAT_TOL * fabs(r0))) done0 = true;
+            if ((level > 1) && (fabs(r0 - old0) < tol * fabs(r0))) done0 = true;
         }
         if (!done1) {
             r1 = s1;
-            if ((level > 1) && (fabs(r1 - old1) < NFW_PAT_TOL * fabs(r1))) done1 = true;
+            if ((level > 1) && (fabs(r1 - old1) < tol * fabs(r1))) done1 = true;
         }
     } while (++level < QLP_PAT_LEVELS && !(done0 && done1));
+    I0 = 0.5 * r0;
+    I1 = 0.5 * r1;
+}
+
+static __device__ void nfw_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+{
+    if (L.q == 1.0) {
+        double kapavg = nfw_kapavg_spherical_rsq(L.ks, L.rs, x * x + y * y);
+        dx = kapavg * x;
+        dy = kapavg * y;
+        return;
+    }
+    if ((fabs(x) < 1e-14) && (fabs(y) < 1e-14)) {
+        dx = 0;
+        dy = 0;
+        return;
+    }
+    double I0, I1;
+    nfw_integrals(L, x * x, y * y, NFW_PAT_TOL, I0, I1);
     const double sqe = sqrt(1 - L.epsilon);
-    dx = x * (sqe * (0.5 * r0));
-    dy = y * (sqe * (0.5 * r1));
+    dx = x * (sqe * I0);
+    dy = y * (sqe * I1);
 }
 
 }  // namespace qlpix

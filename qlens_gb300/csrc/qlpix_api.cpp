@@ -204,6 +204,49 @@ int qlp_last_transfer_bytes(const qlp_ctx* c, long long* h2d, long long* d2h)
     return QLP_OK;
 }
 
+void qlp_surrogate_defaults(qlp_surrogate_opts* o)
+{
+    if (!o) return;
+    o->n_train = 1 << 20;
+    o->batch = 16384;
+    o->steps = 30000;
+    o->lr = 3e-3;
+    o->seed = 1;
+}
+
+int qlp_nfw_surrogate_train(int device, const qlp_surrogate_opts* opts, qlp_surrogate_report* rep)
+{
+    qlp_surrogate_opts d;
+    qlp_surrogate_defaults(&d);
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(QLP_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= n) return fail(QLP_ERR_ARG, "bad device");
+    return surrogate_train(device, opts ? opts : &d, rep);
+}
+
+int qlp_set_nfw_mode(qlp_ctx* c, int mode, double threshold_arcsec)
+{
+    if (!c || (mode != QLP_NFW_QUADRATURE && mode != QLP_NFW_SURROGATE)) return fail(QLP_ERR_ARG, "bad NFW mode");
+    if (mode == QLP_NFW_SURROGATE && !surrogate_ready(c->device))
+        return fail(QLP_ERR_ARG, "no trained NFW surrogate on this device (qlp_nfw_surrogate_train)");
+    c->nfw_mode = mode;
+    c->nfw_threshold = (threshold_arcsec > 0) ? threshold_arcsec : 2e-5;
+    return QLP_OK;
+}
+
+int qlp_surrogate_grad_check(int device, const float* params, const float* x, const float* t, int batch,
+                             double* loss, float* grad)
+{
+    if (!params || !x || !t || !loss || !grad || batch < 1) return fail(QLP_ERR_ARG, "bad arguments");
+    return surrogate_grad_check(device, params, x, t, batch, loss, grad);
+}
+
+int qlp_surrogate_eval(int device, const double* rpq, int n, double* t, double* G, double* B, double* bound)
+{
+    if (!rpq || !t || n < 1) return fail(QLP_ERR_ARG, "bad arguments");
+    return surrogate_eval(device, rpq, n, t, G, B, bound);
+}
+
 int qlp_n_params(const qlp_ctx* c)
 {
     if (!c) return 0;

@@ -30,7 +30,7 @@ struct Slot {
     // the launch sequence captured as a CUDA graph, valid for one
     // (precision, mask, source grid, NFW) combination and graph generation
     cudaGraphExec_t graph = nullptr;
-    int graph_key[5] = {0, 0, 0, 0, 0};
+    int graph_key[6] = {0, 0, 0, 0, 0, 0};
     long long graph_gen = 0;
     long long graph_launches = 0;   // kernels per replay
 };
@@ -77,6 +77,8 @@ struct qlp_ctx {
     qlpix::EvalParams* h_ep = nullptr;    // pinned, one per batch instance
     int h_ep_cap = 0;
     int use_graphs = 1;                   // batched evaluation replays captured graphs
+    int nfw_mode = QLP_NFW_QUADRATURE;    // NFW deflection: quadrature or trained surrogate
+    double nfw_threshold = 2e-5;          // surrogate error bound (arcsec) above which a ray falls back
     long long graph_gen = 1;              // bumped whenever captured graphs go stale
     long long last_h2d = 0, last_d2h = 0; // bytes moved by the last call
     float stage_ms[QLP_N_STAGES] = {};
@@ -102,4 +104,11 @@ int mixed_init(Slot& slot);
 void mixed_free(Slot& slot);
 int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, cudaStream_t st,
                         cudaEvent_t* ev);
+// surrogate.cu
+int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_report* rep);
+bool surrogate_ready(int device);
+int surrogate_grad_check(int device, const float* params, const float* x, const float* t, int batch, double* loss,
+                         float* grad);
+int surrogate_eval(int device, const double* rpq, int n, double* t_net, double* G_quad, double* B, double* bound);
+int launch_raytrace_sur(const StaticData& sd, Work& w, double thresh, int defer_lens, cudaStream_t st);
 }  // namespace qlpix

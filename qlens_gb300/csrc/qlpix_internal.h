@@ -53,7 +53,8 @@ struct GridState {
 // Scalars of one evaluation, written by the final assembly kernel.
 struct EvalOut {
     double chisq0, logdet_F, logdet_R, Es_times_two, regterms, m2logev;
-    int n_active_pixels, n_active_src, L_nnz, status, refine_iters, pad;
+    int n_active_pixels, n_active_src, L_nnz, status, refine_iters;
+    int pad;                           // rays that took the NFW quadrature instead of the surrogate
 };
 
 struct StaticData {            // per-context, uploaded once
@@ -114,6 +115,8 @@ struct Work {
     GridState* gs;
     EvalOut* out;                      // this slot's result (copied to the host after each evaluation)
     EvalParams* ep;                    // this slot's per-evaluation parameters
+    // rays whose NFW deflection the surrogate hands to the quadrature (n_sub capacity)
+    int* fb_ray;  double* fb_xy;  int* fb_count;
 };
 
 // Device address of the regularisation parameter of a slot's EvalParams.

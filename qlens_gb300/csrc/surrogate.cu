@@ -1,0 +1,1150 @@
+// surrogate.cu -- the learned part: an MLP surrogate of the elliptical NFW
+// deflection, trained on the GPU on output of the Gauss-Patterson quadrature
+// (nfw_device.cuh) and run on the tensor cores inside the ray shooting, with
+// the quadrature as fallback wherever the surrogate's error bound is exceeded.
+//
+// What is learned.  For the lens-frame point (x, y), the quadrature gives
+// alpha_x = x ks G_0(X, Y, q), alpha_y = y ks G_1(X, Y, q) with X = x/rs,
+// Y = y/rs (LensProfile::deflection_numerical, profile.cpp:2359-2375; G_n =
+// sqrt(1-eps) J_n / ks, eps = 1 - q^2, is dimensionless because
+// kappa(r^2; ks, rs) = ks kappa_hat(r^2/rs^2), models.cpp:978-984).  The
+// network maps the inputs (log R, phi, q), R = sqrt(X^2 + Y^2),
+// phi = atan2(|Y|, |X|) -- log rs is absorbed exactly by that scaling -- to
+// s_n = log(G_n / B) / (1 - q), B = the spherical mean convergence kapavg_hat
+// at the elliptical radius xi^2 = q X^2 + Y^2 / q (NFW::kapavg_spherical_rsq,
+// models.cpp:1001-1010, in FP64): log(G_n / B) is a bounded residual that
+// vanishes at q = 1 (where G_n = B exactly), so dividing by 1 - q leaves an
+// O(1) smooth target and makes the surrogate exact in the spherical limit.
+// Deflection only: the pixel likelihood ray-traces, it never needs the
+// Hessian.
+//
+// Network: 3 -> 4 x 128 tanh -> 2 (50,306 parameters, the layout of
+// oracle/mlp_oracle.c).  Training (k_sur_*): FP32 SIMT GEMMs for the
+// forward pass, the backward pass and the weight gradients (split over the
+// batch, reduced in a fixed order), Adam; the loss weights each sample by its
+// squared dimensionless deflection, since the error the gate tests is |alpha|
+// times the relative error.  Inference (sur_mlp_cta): 128 rays per CTA = the
+// 128 TMEM lanes; layer 0 (3 -> 128) on the CUDA cores, layers 1-3
+// (128 x 128) as tcgen05 kind::tf32 MMAs with the activations in TMEM
+// (A operand, TF32 hi + lo) and the weights TMA-loaded into shared memory
+// (B operand, hi + lo), 3xTF32; the output layer on the CUDA cores.
+//
+// Error bound.  After training the surrogate is compared with the quadrature
+// (tolerance 1e-10) on 32 jittered points of every cell of a 64 x 16 x 16 grid
+// over (log R, phi, q); three times the largest relative error of G_0, G_1 in
+// a cell is that cell's bound.  A ray uses the surrogate only if
+// ks |G| |(x, y)| times its cell's bound is below the gate (2e-5 arcsec by
+// default) and its inputs lie inside the trained domain; every other ray
+// takes the quadrature.
+#include <cuda.h>
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+#include "qlpix_ctx.h"
+#include "lens_device.cuh"
+#include "tc_common.cuh"
+
+namespace qlpix {
+
+#define SUR_H 128
+#define SUR_W0 0
+#define SUR_B0 (SUR_W0 + 3 * SUR_H)
+#define SUR_W1 (SUR_B0 + SUR_H)
+#define SUR_B1 (SUR_W1 + SUR_H * SUR_H)
+#define SUR_W2 (SUR_B1 + SUR_H)
+#define SUR_B2 (SUR_W2 + SUR_H * SUR_H)
+#define SUR_W3 (SUR_B2 + SUR_H)
+#define SUR_B3 (SUR_W3 + SUR_H * SUR_H)
+#define SUR_W4 (SUR_B3 + SUR_H)
+#define SUR_B4 (SUR_W4 + 2 * SUR_H)
+#define SUR_NP (SUR_B4 + 2)
+
+// trained domain
+#define SUR_RHO_LO (-9.210340371976184)   // log 1e-4
+#define SUR_RHO_HI (5.298317366548036)    // log 200
+#define SUR_Q_LO 0.45
+#define SUR_NB_RHO 64
+#define SUR_NB_PHI 16
+#define SUR_NB_Q 16
+#define SUR_NBINS (SUR_NB_RHO * SUR_NB_PHI * SUR_NB_Q)
+#define SUR_VAL_PER_BIN 32
+#define SUR_BOUND_SAFETY 3.0
+#define SUR_TARGET_TOL 1e-10
+
+// ---------------------------------------------------------------------------
+// shared pieces: inputs, baseline, activation
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sur_tanh(float x)
+{
+    return 1.0f - 2.0f / (1.0f + __expf(2.0f * x));
+}
+
+struct SurIn {
+    float f0, f1, f2;   // normalised inputs
+    int bin;            // error-bound cell, -1 outside the domain
+    double B;           // baseline
+};
+
+__host__ __device__ __forceinline__ int sur_cell(double rho, double phi, double q)
+{
+    if (!(rho >= SUR_RHO_LO && rho < SUR_RHO_HI && q >= SUR_Q_LO && q < 1.0)) return -1;
+    int ir = (int)((rho - SUR_RHO_LO) / (SUR_RHO_HI - SUR_RHO_LO) * SUR_NB_RHO);
+    int ip = (int)(phi / (0.5 * M_PI) * SUR_NB_PHI);
+    int iq = (int)((q - SUR_Q_LO) / (1.0 - SUR_Q_LO) * SUR_NB_Q);
+    ir = ir < 0 ? 0 : (ir >= SUR_NB_RHO ? SUR_NB_RHO - 1 : ir);
+    ip = ip < 0 ? 0 : (ip >= SUR_NB_PHI ? SUR_NB_PHI - 1 : ip);
+    iq = iq < 0 ? 0 : (iq >= SUR_NB_Q ? SUR_NB_Q - 1 : iq);
+    return (ir * SUR_NB_PHI + ip) * SUR_NB_Q + iq;
+}
+
+// X = x/rs, Y = y/rs in the lens frame (either sign), q < 1
+__device__ __forceinline__ SurIn sur_inputs(double X, double Y, double q)
+{
+    SurIn s;
+    const double ax = fabs(X), ay = fabs(Y);
+    const double R2 = ax * ax + ay * ay;
+    const double rho = 0.5 * log(R2);
+    const double phi = atan2(ay, ax);
+    const double hr = 0.5 * (SUR_RHO_HI - SUR_RHO_LO), mr = 0.5 * (SUR_RHO_HI + SUR_RHO_LO);
+    const double hq = 0.5 * (1.0 - SUR_Q_LO), mq = 0.5 * (1.0 + SUR_Q_LO);
+    // outside the domain (or at the centre) the network still runs on clamped
+    // inputs, but the ray takes the quadrature
+    s.f0 = (float)fmin(fmax((rho - mr) / hr, -2.0), 2.0);
+    s.f1 = (float)(phi * (4.0 / M_PI) - 1.0);
+    s.f2 = (float)fmin(fmax((q - mq) / hq, -2.0), 2.0);
+    s.bin = sur_cell(rho, phi, q);
+    s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, q * ax * ax + ay * ay / q);
+    return s;
+}
+
+__device__ __forceinline__ uint64_t sur_hash(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double sur_unif(uint64_t seed, uint64_t i, int j)
+{
+    return (double)(sur_hash(seed * 0x100000001B3ull + i * 4 + j) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// One sample at (rho, phi, q): network inputs, the quadrature's G_0, G_1
+// (tolerance 1e-10) and the baseline.
+__device__ void sur_point(double rho, double phi, double q, float* f, double* G, double* B)
+{
+    const double R = exp(rho);
+    const double X = R * cos(phi), Y = R * sin(phi);
+    LensRec L;
+    memset(&L, 0, sizeof(L));
+    L.type = QLP_LENS_NFW;
+    L.ks = 1.0; L.rs = 1.0; L.q = q; L.qsq = q * q; L.epsilon = 1 - L.qsq;
+    double I0, I1;
+    nfw_integrals(L, X * X, Y * Y, SUR_TARGET_TOL, I0, I1);
+    const double sqe = sqrt(1 - L.epsilon);
+    G[0] = sqe * I0;
+    G[1] = sqe * I1;
+    const SurIn s = sur_inputs(X, Y, q);
+    f[0] = s.f0; f[1] = s.f1; f[2] = s.f2;
+    *B = s.B;
+}
+
+// Samples: mode 0 uniform over the domain, mode 1 SUR_VAL_PER_BIN jittered
+// points per error-bound cell (sample i belongs to cell i / SUR_VAL_PER_BIN).
+// Writes the inputs X [n][3], the raw targets T [n][2] (s_0, s_1), when G is
+// not null G [n][2], the baselines Bv [n] and q [n], and when Wt is not null
+// the squared dimensionless deflection (the training weight before scaling).
+__global__ void k_sur_samples(int n, uint64_t seed, int mode, float* __restrict__ Xf, float* __restrict__ Tf,
+                              double* __restrict__ G, double* __restrict__ Bv, double* __restrict__ Qv,
+                              float* __restrict__ Wt)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double rho, phi, q;
+        const double u0 = sur_unif(seed, i, 0), u1 = sur_unif(seed, i, 1), u2 = sur_unif(seed, i, 2);
+        if (mode == 0) {
+            rho = SUR_RHO_LO + u0 * (SUR_RHO_HI - SUR_RHO_LO);
+            phi = u1 * 0.5 * M_PI;
+            q = SUR_Q_LO + u2 * (1.0 - SUR_Q_LO);
+        } else {
+            const int b = i / SUR_VAL_PER_BIN;
+            const int iq = b % SUR_NB_Q, ip = (b / SUR_NB_Q) % SUR_NB_PHI, ir = b / (SUR_NB_Q * SUR_NB_PHI);
+            rho = SUR_RHO_LO + (ir + u0) * (SUR_RHO_HI - SUR_RHO_LO) / SUR_NB_RHO;
+            phi = (ip + u1) * 0.5 * M_PI / SUR_NB_PHI;
+            q = SUR_Q_LO + (iq + u2) * (1.0 - SUR_Q_LO) / SUR_NB_Q;
+        }
+        if (q >= 1.0) q = 0.999999;
+        float f[3];
+        double g[2], b;
+        sur_point(rho, phi, q, f, g, &b);
+        Xf[3 * (size_t)i] = f[0]; Xf[3 * (size_t)i + 1] = f[1]; Xf[3 * (size_t)i + 2] = f[2];
+        Tf[2 * (size_t)i] = (float)(log(g[0] / b) / (1.0 - q));
+        Tf[2 * (size_t)i + 1] = (float)(log(g[1] / b) / (1.0 - q));
+        if (G) { G[2 * (size_t)i] = g[0]; G[2 * (size_t)i + 1] = g[1]; Bv[i] = b; Qv[i] = q; }
+        if (Wt) {   // |alpha| / (ks rs) squared: where an error in G matters most
+            const double R = exp(rho), c = cos(phi), sn = sin(phi);
+            Wt[i] = (float)(R * R * (g[0] * g[0] * c * c + g[1] * g[1] * sn * sn));
+        }
+    }
+}
+
+// given points (rho, phi, q): inputs, quadrature G and baselines
+__global__ void k_sur_points(int n, const double* __restrict__ rpq, float* __restrict__ Xf, double* __restrict__ G,
+                             double* __restrict__ Bv)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double q = rpq[3 * (size_t)i + 2];
+        if (q >= 1.0) q = 0.999999;
+        float f[3];
+        double g[2], b;
+        sur_point(rpq[3 * (size_t)i], rpq[3 * (size_t)i + 1], q, f, g, &b);
+        Xf[3 * (size_t)i] = f[0]; Xf[3 * (size_t)i + 1] = f[1]; Xf[3 * (size_t)i + 2] = f[2];
+        G[2 * (size_t)i] = g[0]; G[2 * (size_t)i + 1] = g[1];
+        Bv[i] = b;
+    }
+}
+
+// targets to zero mean, unit variance per output; weights to wfloor + wscale w
+__global__ void k_sur_affine(int n, float* __restrict__ T, float mu0, float mu1, float is0, float is1,
+                             float* __restrict__ Wt, float wscale, float wfloor)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        T[2 * (size_t)i] = (T[2 * (size_t)i] - mu0) * is0;
+        T[2 * (size_t)i + 1] = (T[2 * (size_t)i + 1] - mu1) * is1;
+        Wt[i] = wfloor + Wt[i] * wscale;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// training: FP32 SIMT GEMM C[M][N] = op(A)[M][K] op(B)[K][N] with generic
+// strides, 64x64 tiles, 256 threads, 4x4 outputs per thread, and epilogues
+//   EPI_STORE      C = acc
+//   EPI_TANH       C = tanh(acc + bias)       hidden layer, forward
+//   EPI_BIAS       C = acc + bias             output layer, forward
+//   EPI_DTANH      C = acc * (1 - Aux^2)      backward through tanh
+// gridDim.z > 1 splits K: split z writes C + z * M * N.
+// ---------------------------------------------------------------------------
+#define EPI_STORE 0
+#define EPI_TANH 1
+#define EPI_BIAS 2
+#define EPI_DTANH 3
+
+template <int EPI>
+__global__ void __launch_bounds__(256) k_sur_gemm(int M, int N, int K, const float* __restrict__ A, int a_rs, int a_cs,
+                                                  const float* __restrict__ B, int b_rs, int b_cs,
+                                                  float* __restrict__ C, const float* __restrict__ bias,
+                                                  const float* __restrict__ aux)
+{
+    __shared__ float As[16][64 + 4];
+    __shared__ float Bs[16][64 + 4];
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int ksplit = (K + gridDim.z - 1) / gridDim.z;
+    const int kbeg = blockIdx.z * ksplit, kend = min(K, kbeg + ksplit);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[4][4] = {};
+    for (int k0 = kbeg; k0 < kend; k0 += 16) {
+        for (int e = threadIdx.x; e < 16 * 64; e += 256) {
+            const int kk = e >> 6, mm = e & 63;
+            const int gm = m0 + mm, gk = k0 + kk;
+            As[kk][mm] = (gm < M && gk < kend) ? A[(size_t)gm * a_rs + (size_t)gk * a_cs] : 0.f;
+            const int gn = n0 + mm;
+            Bs[kk][mm] = (gn < N && gk < kend) ? B[(size_t)gk * b_rs + (size_t)gn * b_cs] : 0.f;
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int kk = 0; kk < 16; kk++) {
+            float a[4], b[4];
+            #pragma unroll
+            for (int u = 0; u < 4; u++) { a[u] = As[kk][ty * 4 + u]; b[u] = Bs[kk][tx * 4 + u]; }
+            #pragma unroll
+            for (int u = 0; u < 4; u++)
+                #pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] = __fmaf_rn(a[u], b[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+    float* Cz = C + (size_t)blockIdx.z * M * N;
+    #pragma unroll
+    for (int u = 0; u < 4; u++)
+        #pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const int gm = m0 + ty * 4 + u, gn = n0 + tx * 4 + v;
+            if (gm >= M || gn >= N) continue;
+            float x = acc[u][v];
+            if (EPI == EPI_TANH) x = sur_tanh(x + bias[gn]);
+            else if (EPI == EPI_BIAS) x = x + bias[gn];
+            else if (EPI == EPI_DTANH) { const float a = aux[(size_t)gm * N + gn]; x = x * (1.f - a * a); }
+            Cz[(size_t)gm * N + gn] = x;
+        }
+}
+
+// out[i] = sum_z part[z][i] in order (deterministic split-K reduction)
+__global__ void k_sur_reduce(int n, int nz, const float* __restrict__ part, float* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int z = 0; z < nz; z++) s += part[(size_t)z * n + i];
+        out[i] = s;
+    }
+}
+
+// bias gradients: column sums of D [rows][n], one block per column, fixed order
+__global__ void __launch_bounds__(256) k_sur_colsum(int rows, int n, const float* __restrict__ D, float* __restrict__ out)
+{
+    __shared__ float red[256];
+    const int c = blockIdx.x;
+    float s = 0.f;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) s += D[(size_t)r * n + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = red[0];
+}
+
+// output-layer gradient dL/dy = 2 w (y - t) / batch (w = 1 without weights);
+// per-block partial sums of w (y - t)^2
+__global__ void __launch_bounds__(256) k_sur_mse(int batch, const float* __restrict__ Y, const float* __restrict__ T,
+                                                 const float* __restrict__ W, float* __restrict__ dY,
+                                                 double* __restrict__ part)
+{
+    __shared__ double red[256];
+    double s = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * batch; i += gridDim.x * blockDim.x) {
+        const float w = W ? W[i >> 1] : 1.f;
+        const float e = Y[i] - T[i];
+        dY[i] = 2.f * w * e / batch;
+        s += (double)w * e * e;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_sur_adam(int n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                           float* __restrict__ m2, float lr, float b1, float b2, float c1, float c2)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float a = b1 * m1[i] + (1.f - b1) * gi;
+        const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+        m1[i] = a;
+        m2[i] = b;
+        p[i] -= lr * (a * c1) / (sqrtf(b * c2) + 1e-8f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// inference on the tensor cores
+// ---------------------------------------------------------------------------
+struct SurMaps {
+    CUtensorMap m[6];     // layer 1..3, hi then lo: [128 out][128 in] FP32, 32x128 boxes, 128-byte swizzle
+};
+#define SUR_SMALL (3 * SUR_H + 4 * SUR_H + 2 * SUR_H + 2)   // W0, b0..b3, W4, b4
+#define SUR_TILE (SUR_H * 32 * 4)                            // 16 KB: 128 rows x 32 K
+#define SUR_SMEM (8 * SUR_TILE + 1024 + SUR_SMALL * 4)
+
+__device__ __forceinline__ void mma_tf32_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_32cols(uint32_t taddr, const float* v)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
+        "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
+        "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
+        "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
+        "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+        : "memory");
+}
+
+__device__ __forceinline__ float tf32_round(float f)
+{
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(f));
+    return __uint_as_float(u);
+}
+
+// Per-CTA state of the tensor-core MLP.
+struct SurCta {
+    unsigned char* tiles;   // 8 x 16 KB, 1024-aligned
+    float* small;           // SUR_SMALL floats
+    uint64_t* tma_bar;
+    uint64_t* mma_bar;
+    volatile int* abort;
+    uint32_t tmem;          // 512 columns: D [0,128), A_hi [128,256), A_lo [256,384)
+    uint32_t phase;         // completed layers (mbarrier parity)
+};
+
+// All 128 threads call this with their ray's inputs; returns the network's
+// two outputs.  ok is cleared if a bounded wait ran out.
+__device__ void sur_mlp_cta(SurCta& S, const SurMaps& maps, float f0, float f1, float f2, float& t0, float& t1,
+                            bool& ok)
+{
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t lane_base = ((uint32_t)(warp * 32)) << 16;
+    const float* W0 = S.small;
+    const float* bb = S.small + 3 * SUR_H;          // b0, b1, b2, b3
+    const float* W4 = S.small + 7 * SUR_H;
+    const float* b4 = S.small + 9 * SUR_H;
+    // layer 0 on the CUDA cores, straight into TMEM as the next A operand (hi, lo)
+    #pragma unroll 1
+    for (int c = 0; c < SUR_H; c += 32) {
+        float hi[32], lo[32];
+        #pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int u = c + j;
+            const float h =
+                sur_tanh(__fmaf_rn(W0[2 * SUR_H + u], f2, __fmaf_rn(W0[SUR_H + u], f1, __fmaf_rn(W0[u], f0, bb[u]))));
+            hi[j] = tf32_round(h);
+            lo[j] = tf32_round(h - hi[j]);
+        }
+        tmem_st_32cols(S.tmem + lane_base + 128 + c, hi);
+        tmem_st_32cols(S.tmem + lane_base + 256 + c, lo);
+    }
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    float o0 = 0.f, o1 = 0.f;
+    for (int l = 1; l <= 3; l++) {
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            mbar_expect_tx(S.tma_bar, 8 * SUR_TILE);
+            for (int kb = 0; kb < 4; kb++) {
+                tma_load_2d(&maps.m[2 * (l - 1)], S.tma_bar, S.tiles + (kb * 2 + 0) * SUR_TILE, kb * 32, 0);
+                tma_load_2d(&maps.m[2 * (l - 1) + 1], S.tma_bar, S.tiles + (kb * 2 + 1) * SUR_TILE, kb * 32, 0);
+            }
+        }
+        if (tid == 32) {
+            const bool w = mbar_wait_bounded(S.tma_bar, S.phase & 1, S.abort, false);
+            tc_fence_after();
+            if (w) {
+                const uint32_t idesc = idesc_tf32_128x128();
+                for (int kb = 0; kb < 4; kb++) {
+                    const uint64_t b_hi = sdesc_sw128(smem_u32(S.tiles + (kb * 2 + 0) * SUR_TILE));
+                    const uint64_t b_lo = sdesc_sw128(smem_u32(S.tiles + (kb * 2 + 1) * SUR_TILE));
+                    #pragma unroll
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint32_t ka = (uint32_t)(kb * 32 + kk * 8);
+                        const uint64_t off = (uint64_t)((kk * 32) >> 4);
+                        mma_tf32_ta(S.tmem, S.tmem + 128 + ka, b_hi + off, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32_ta(S.tmem, S.tmem + 128 + ka, b_lo + off, idesc, 1u);
+                        mma_tf32_ta(S.tmem, S.tmem + 256 + ka, b_hi + off, idesc, 1u);
+                    }
+                }
+            }
+            mma_commit(S.mma_bar);
+        }
+        __syncwarp();
+        const bool done = mbar_wait_bounded(S.mma_bar, S.phase & 1, S.abort, false);
+        tc_fence_after();
+        S.phase++;
+        if (!done || *S.abort) ok = false;
+        // epilogue: bias, tanh; layers 1-2 back into TMEM, layer 3 into the output layer
+        const float* bl = bb + l * SUR_H;
+        #pragma unroll 1
+        for (int c = 0; c < SUR_H; c += 32) {
+            float v[32];
+            tmem_ld_32cols(S.tmem + lane_base + c, v);
+            #pragma unroll
+            for (int j = 0; j < 32; j++) v[j] = sur_tanh(v[j] + bl[c + j]);
+            if (l < 3) {
+                float hi[32], lo[32];
+                #pragma unroll
+                for (int j = 0; j < 32; j++) { hi[j] = tf32_round(v[j]); lo[j] = tf32_round(v[j] - hi[j]); }
+                tmem_st_32cols(S.tmem + lane_base + 128 + c, hi);
+                tmem_st_32cols(S.tmem + lane_base + 256 + c, lo);
+            } else {
+                #pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    o0 = __fmaf_rn(v[j], W4[2 * (c + j)], o0);
+                    o1 = __fmaf_rn(v[j], W4[2 * (c + j) + 1], o1);
+                }
+            }
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    t0 = o0 + b4[0];
+    t1 = o1 + b4[1];
+}
+
+__device__ __forceinline__ void sur_cta_begin(SurCta& S, unsigned char* smem_raw, const float* __restrict__ small_g,
+                                              uint64_t* tma_bar, uint64_t* mma_bar, uint32_t* tmem_slot,
+                                              volatile int* abort)
+{
+    S.tiles = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    S.small = reinterpret_cast<float*>(S.tiles + 8 * SUR_TILE);
+    S.tma_bar = tma_bar;
+    S.mma_bar = mma_bar;
+    S.abort = abort;
+    S.phase = 0;
+    for (int i = threadIdx.x; i < SUR_SMALL; i += blockDim.x) S.small[i] = small_g[i];
+    if (threadIdx.x == 0) {
+        mbar_init(tma_bar, 1);
+        mbar_init(mma_bar, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if ((threadIdx.x >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    S.tmem = *tmem_slot;
+}
+
+__device__ __forceinline__ void sur_cta_end(SurCta& S)
+{
+    tc_fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(512) : "memory");
+    }
+}
+
+// Batch inference for the error-bound table and the tests: T[i] = net(X[i]).
+__global__ void __launch_bounds__(128, 1) k_sur_infer(int n, const float* __restrict__ X, float* __restrict__ T,
+                                                      const __grid_constant__ SurMaps maps,
+                                                      const float* __restrict__ small_g, int* status)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint64_t tma_bar, mma_bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    SurCta S;
+    sur_cta_begin(S, smem_raw, small_g, &tma_bar, &mma_bar, &tmem_slot, &abort_flag);
+    const int i = blockIdx.x * 128 + threadIdx.x;
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+    if (i < n) { f0 = X[3 * (size_t)i]; f1 = X[3 * (size_t)i + 1]; f2 = X[3 * (size_t)i + 2]; }
+    float t0, t1;
+    bool ok = true;
+    sur_mlp_cta(S, maps, f0, f1, f2, t0, t1, ok);
+    if (i < n) { T[2 * (size_t)i] = t0; T[2 * (size_t)i + 1] = t1; }
+    if (!ok && threadIdx.x == 0) atomicExch(status, QLP_ERR_TIMEOUT);
+    sur_cta_end(S);
+}
+
+// Ray shooting with NFW lenses on the surrogate: k_raytrace's lens equation
+// (QLens::find_sourcept, lenscalc.cpp:81-113), 128 rays per CTA.  At every
+// NFW lens with q < 1 all 128 threads run the network together (unless no
+// ray of the CTA can pass the gate, then none does); a ray whose bound
+// exceeds `thresh` (or whose inputs leave the domain) takes the quadrature
+// instead -- right here, or, for the lens `defer_lens` (the only NFW lens, on
+// the last plane), later in k_nfw_fallback at full occupancy (its lens-frame
+// position is queued and its contribution left out here).  out->pad counts
+// the fallbacks.
+__global__ void __launch_bounds__(128, 1) k_raytrace_sur(StaticData sd, const EvalParams* __restrict__ ep,
+                                                         double* __restrict__ spx, double* __restrict__ spy,
+                                                         const __grid_constant__ SurMaps maps,
+                                                         const float* __restrict__ small_g,
+                                                         const float* __restrict__ bound, double thresh,
+                                                         int defer_lens, int* __restrict__ fb_count,
+                                                         int* __restrict__ fb_ray, double* __restrict__ fb_xy,
+                                                         GridState* gs, EvalOut* out)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint64_t tma_bar, mma_bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    __shared__ __align__(16) LensModel lm;
+    __shared__ int n_fb;
+    {
+        const double* src = reinterpret_cast<const double*>(&ep->lm);
+        double* dst = reinterpret_cast<double*>(&lm);
+        for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
+        if (threadIdx.x == 0) n_fb = 0;
+    }
+    SurCta S;
+    sur_cta_begin(S, smem_raw, small_g, &tma_bar, &mma_bar, &tmem_slot, &abort_flag);
+    const int t = blockIdx.x * 128 + threadIdx.x;
+    const bool valid = t < sd.n_sub;
+    double px = 0, py = 0;
+    if (valid) {
+        const int ns = sd.nsplit, nsub = sd.nsub;
+        const int m = t / nsub, k = t - m * nsub;
+        const int pix = sd.mpix[m];
+        const int i = pix / sd.ny, j = pix - i * sd.ny;
+        const int ii = k / ns, jj = k - ii * ns;
+        const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
+        const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
+        px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
+        py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
+    }
+    bool ok = true;
+    int fb = 0;
+    double defx = 0, defy = 0;
+    double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
+    for (int p = 0; p < lm.n_planes; p++) {
+        dsx[p] = 0; dsy[p] = 0;
+        if (lm.zfac[p] == 0.0) continue;
+        double xi = px, yi = py;
+        for (int jp = 0; jp < p; jp++) {
+            xi -= lm.beta[p - 1][jp] * dsx[jp];
+            yi -= lm.beta[p - 1][jp] * dsy[jp];
+        }
+        for (int k = 0; k < lm.nlens; k++) {
+            const LensRec& L = lm.lens[k];
+            if (L.plane != p) continue;
+            double ax, ay;
+            if (L.type == QLP_LENS_NFW && L.q != 1.0) {
+                // LensProfile::deflection: shift, rotate, deflect, rotate back
+                double x = xi - L.xc, y = yi - L.yc;
+                const bool rot = (L.sintheta != 0);
+                if (rot) {
+                    const double xp = x * L.costheta + y * L.sintheta;
+                    y = -x * L.sintheta + y * L.costheta;
+                    x = xp;
+                }
+                const SurIn in = sur_inputs(x / L.rs, y / L.rs, L.q);
+                const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
+                // before the network: |alpha| ~ ks B |(x, y)| (G is within a few
+                // tens of percent of B), so a CTA none of whose rays can pass the
+                // gate skips the network and sends every ray to the quadrature
+                const bool maybe = valid && !centre && in.bin >= 0 &&
+                                   L.ks * in.B * sqrt(x * x + y * y) * (double)bound[in.bin] <= 1.5 * thresh;
+                double bx = 0, by = 0;
+                bool use = false;
+                if (__syncthreads_or(maybe)) {
+                    float t0, t1;
+                    sur_mlp_cta(S, maps, in.f0, in.f1, in.f2, t0, t1, ok);
+                    const double G0 = in.B * exp((1.0 - L.q) * t0), G1 = in.B * exp((1.0 - L.q) * t1);
+                    bx = x * L.ks * G0;
+                    by = y * L.ks * G1;
+                    const double mag = sqrt(bx * bx + by * by);
+                    use = ok && !centre && in.bin >= 0 && mag * (double)bound[in.bin] <= thresh;
+                }
+                if (!use && valid) {
+                    fb++;
+                    if (k == defer_lens) {
+                        const int e = atomicAdd(fb_count, 1);
+                        fb_ray[e] = t;
+                        fb_xy[2 * (size_t)e] = x;
+                        fb_xy[2 * (size_t)e + 1] = y;
+                        bx = 0; by = 0;
+                    } else {
+                        nfw_deflection(L, x, y, bx, by);
+                    }
+                }
+                if (rot) {
+                    const double xp = bx * L.costheta - by * L.sintheta;
+                    by = bx * L.sintheta + by * L.costheta;
+                    bx = xp;
+                }
+                ax = bx; ay = by;
+            } else {
+                lens_deflection<true>(L, xi, yi, ax, ay);
+            }
+            dsx[p] += ax; dsy[p] += ay;
+        }
+        dsx[p] *= lm.zfac[p];
+        dsy[p] *= lm.zfac[p];
+        defx += dsx[p];
+        defy += dsy[p];
+    }
+    if (valid) {
+        spx[t] = px - defx;
+        spy[t] = py - defy;
+    }
+    if (fb) atomicAdd(&n_fb, fb);
+    sur_cta_end(S);
+    if (threadIdx.x == 0) {
+        if (n_fb) atomicAdd(&out->pad, n_fb);
+        if (!ok) atomicExch(&gs->status, QLP_ERR_TIMEOUT);
+    }
+}
+
+// The queued fallbacks of k_raytrace_sur: quadrature deflection of lens
+// `lens` at the queued lens-frame points, rotated back, scaled by its plane's
+// factor and subtracted from the rays' source points.
+__global__ void k_nfw_fallback(const EvalParams* __restrict__ ep, int lens, const int* __restrict__ fb_count,
+                               const int* __restrict__ fb_ray, const double* __restrict__ fb_xy,
+                               double* __restrict__ spx, double* __restrict__ spy)
+{
+    const int n = *fb_count;
+    const LensRec& L = ep->lm.lens[lens];
+    const double z = ep->lm.zfac[L.plane];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        double bx, by;
+        nfw_deflection(L, fb_xy[2 * (size_t)e], fb_xy[2 * (size_t)e + 1], bx, by);
+        if (L.sintheta != 0) {
+            const double xp = bx * L.costheta - by * L.sintheta;
+            by = bx * L.sintheta + by * L.costheta;
+            bx = xp;
+        }
+        const int t = fb_ray[e];
+        spx[t] -= z * bx;
+        spy[t] -= z * by;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side: one trained network per device, shared by every context
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFnS)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+struct SurState {
+    bool ready = false;
+    float* params = nullptr;   // training layout
+    float* wt = nullptr;       // [3 layers][hi, lo][128 out][128 in]
+    float* small = nullptr;    // SUR_SMALL
+    float* bound = nullptr;    // SUR_NBINS
+    SurMaps maps;
+    qlp_surrogate_report rep{};
+};
+static std::mutex g_sur_mu;
+static SurState g_sur[64];
+
+// [l][out][in] hi/lo copies of layers 1-3 and the small parameters for
+// inference, with the target normalisation folded into the output layer
+__global__ void k_sur_prep(const float* __restrict__ p, float* __restrict__ wt, float* __restrict__ small, float mu0,
+                           float mu1, float sg0, float sg1)
+{
+    const int n = 3 * SUR_H * SUR_H;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int l = e / (SUR_H * SUR_H), r = e % (SUR_H * SUR_H), o = r / SUR_H, i = r % SUR_H;
+        const float w = p[SUR_W1 + l * (SUR_H * SUR_H + SUR_H) + i * SUR_H + o];
+        const float h = tf32_round(w);
+        wt[(size_t)(2 * l) * SUR_H * SUR_H + o * SUR_H + i] = h;
+        wt[(size_t)(2 * l + 1) * SUR_H * SUR_H + o * SUR_H + i] = tf32_round(w - h);
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < SUR_SMALL; e += gridDim.x * blockDim.x) {
+        float v;
+        if (e < 3 * SUR_H) v = p[SUR_W0 + e];
+        else if (e < 7 * SUR_H) {
+            const int l = (e - 3 * SUR_H) / SUR_H, u = (e - 3 * SUR_H) % SUR_H;
+            v = p[SUR_B0 + l * (SUR_H * SUR_H + SUR_H) + u];
+        } else if (e < 9 * SUR_H) v = p[SUR_W4 + (e - 7 * SUR_H)] * (((e - 7 * SUR_H) & 1) ? sg1 : sg0);
+        else v = p[SUR_B4 + (e - 9 * SUR_H)] * ((e & 1) ? sg1 : sg0) + ((e & 1) ? mu1 : mu0);   // un-normalised s
+        small[e] = v;
+    }
+}
+
+// per-cell bound: SUR_BOUND_SAFETY x the largest relative error of G_0, G_1 among the cell's samples
+__global__ void k_sur_bound(int nbins, const float* __restrict__ Tnet, const double* __restrict__ G,
+                            const double* __restrict__ Bv, const double* __restrict__ Qv, float* __restrict__ bound,
+                            double* __restrict__ stats)
+{
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
+        double mx = 0;
+        for (int s = 0; s < SUR_VAL_PER_BIN; s++) {
+            const size_t i = (size_t)b * SUR_VAL_PER_BIN + s;
+            for (int o = 0; o < 2; o++) {
+                const double g = Bv[i] * exp((1.0 - Qv[i]) * Tnet[2 * i + o]);
+                const double e = fabs(g - G[2 * i + o]) / fabs(G[2 * i + o]);
+                mx = fmax(mx, e);
+            }
+        }
+        bound[b] = (float)(SUR_BOUND_SAFETY * mx);
+        stats[b] = mx;
+    }
+}
+
+static int sur_maps(SurState& st)
+{
+    static EncodeTiledFnS enc = nullptr;
+    if (!enc) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return QLP_ERR_CUDA;
+        enc = (EncodeTiledFnS)p;
+    }
+    for (int k = 0; k < 6; k++) {
+        cuuint64_t dims[2] = {SUR_H, SUR_H};
+        cuuint64_t strides[1] = {SUR_H * sizeof(float)};
+        cuuint32_t box[2] = {32, SUR_H};
+        cuuint32_t estr[2] = {1, 1};
+        if (enc(&st.maps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, st.wt + (size_t)k * SUR_H * SUR_H, dims, strides,
+                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return QLP_ERR_CUDA;
+    }
+    return QLP_OK;
+}
+
+#define SCK(x)                                                                    \
+    do {                                                                          \
+        cudaError_t e__ = (x);                                                    \
+        if (e__ != cudaSuccess) {                                                 \
+            set_error("%s (%d)", "surrogate: CUDA error", (int)e__);              \
+            rc = QLP_ERR_CUDA;                                                    \
+            goto done;                                                            \
+        }                                                                         \
+    } while (0)
+
+static const int g_dims[6] = {3, SUR_H, SUR_H, SUR_H, SUR_H, 2};
+
+static void sur_offsets(size_t* off, size_t* boff)
+{
+    size_t p = 0;
+    for (int l = 0; l < 5; l++) {
+        off[l] = p;
+        p += (size_t)g_dims[l] * g_dims[l + 1];
+        boff[l] = p;
+        p += g_dims[l + 1];
+    }
+}
+
+// One forward + backward pass of the training kernels: activations in act
+// (6 x bs x 128), gradient into grad.  W (per-sample loss weights) may be null.
+static void sur_fwd_bwd(cudaStream_t s, const float* P, const float* xb, const float* tb, const float* W, int bs,
+                        float* act, float* dz, float* dz2, float* gpart, int KS, float* grad, double* lpart,
+                        int mse_blocks)
+{
+    size_t off[5], boff[5];
+    sur_offsets(off, boff);
+    float* a[6];
+    for (int l = 0; l < 6; l++) a[l] = act + (size_t)l * bs * SUR_H;
+    const float* in = xb;
+    for (int l = 0; l < 5; l++) {
+        dim3 g((g_dims[l + 1] + 63) / 64, (bs + 63) / 64, 1);
+        if (l < 4)
+            k_sur_gemm<EPI_TANH><<<g, 256, 0, s>>>(bs, g_dims[l + 1], g_dims[l], in, g_dims[l], 1, P + off[l],
+                                                   g_dims[l + 1], 1, a[l + 1], P + boff[l], nullptr);
+        else
+            k_sur_gemm<EPI_BIAS><<<g, 256, 0, s>>>(bs, 2, SUR_H, in, SUR_H, 1, P + off[l], 2, 1, a[5], P + boff[l],
+                                                   nullptr);
+        in = a[l + 1];
+    }
+    k_sur_mse<<<mse_blocks, 256, 0, s>>>(bs, a[5], tb, W, dz, lpart);
+    // backward: dcur = dL/dz of layer l; weight gradient a[l]^T dcur, bias gradient colsum(dcur)
+    float* dcur = dz;
+    float* dnext = dz2;
+    for (int l = 4; l >= 0; l--) {
+        const float* al = (l == 0) ? xb : a[l];
+        const int ni = g_dims[l], no = g_dims[l + 1];
+        dim3 gw((no + 63) / 64, (ni + 63) / 64, KS);
+        k_sur_gemm<EPI_STORE><<<gw, 256, 0, s>>>(ni, no, bs, al, 1, ni, dcur, no, 1, gpart, nullptr, nullptr);
+        k_sur_reduce<<<(ni * no + 255) / 256, 256, 0, s>>>(ni * no, KS, gpart, grad + off[l]);
+        k_sur_colsum<<<no, 256, 0, s>>>(bs, no, dcur, grad + boff[l]);
+        if (l == 0) break;
+        // dz_prev = (dcur W_l^T) * (1 - a[l]^2)
+        dim3 gb((ni + 63) / 64, (bs + 63) / 64, 1);
+        k_sur_gemm<EPI_DTANH><<<gb, 256, 0, s>>>(bs, ni, no, dcur, no, 1, P + off[l], 1, no, dnext, nullptr, a[l]);
+        std::swap(dcur, dnext);
+    }
+}
+
+int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_report* rep)
+{
+    std::lock_guard<std::mutex> lock(g_sur_mu);
+    if (device < 0 || device >= 64) return QLP_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return QLP_ERR_NO_DEVICE;
+    SurState& st = g_sur[device];
+    const int ntr = std::max(o->n_train, 4096), bs = std::min(std::max(o->batch, 256), ntr);
+    const int steps = std::max(o->steps, 1);
+    const int nval = SUR_NBINS * SUR_VAL_PER_BIN;
+    const int KS = std::max(1, bs / 256);              // split-K for the weight gradients
+    const int mse_blocks = 64;
+    cudaStream_t s = nullptr;
+    float *X = nullptr, *T = nullptr, *Wtr = nullptr, *Xv = nullptr, *Tv = nullptr, *Tnet = nullptr, *act = nullptr;
+    float *dz = nullptr, *dz2 = nullptr, *grad = nullptr, *gpart = nullptr, *m1 = nullptr, *m2 = nullptr;
+    double *Gv = nullptr, *Bv = nullptr, *Qv = nullptr, *lpart = nullptr, *stats = nullptr;
+    int* dstatus = nullptr;
+    int rc = QLP_OK;
+    float mu[2] = {0.f, 0.f}, sg[2] = {1.f, 1.f};
+    double last_loss = 0;
+    size_t off[5], boff[5];
+    sur_offsets(off, boff);
+    const auto t_start = std::chrono::steady_clock::now();
+    SCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    if (!st.params) {
+        SCK(cudaMalloc(&st.params, sizeof(float) * SUR_NP));
+        SCK(cudaMalloc(&st.wt, sizeof(float) * 6 * SUR_H * SUR_H));
+        SCK(cudaMalloc(&st.small, sizeof(float) * SUR_SMALL));
+        SCK(cudaMalloc(&st.bound, sizeof(float) * SUR_NBINS));
+    }
+    st.ready = false;
+    SCK(cudaMalloc(&X, sizeof(float) * 3 * (size_t)ntr));
+    SCK(cudaMalloc(&T, sizeof(float) * 2 * (size_t)ntr));
+    SCK(cudaMalloc(&Wtr, sizeof(float) * (size_t)ntr));
+    SCK(cudaMalloc(&Xv, sizeof(float) * 3 * (size_t)nval));
+    SCK(cudaMalloc(&Tv, sizeof(float) * 2 * (size_t)nval));
+    SCK(cudaMalloc(&Tnet, sizeof(float) * 2 * (size_t)nval));
+    SCK(cudaMalloc(&Gv, sizeof(double) * 2 * (size_t)nval));
+    SCK(cudaMalloc(&Bv, sizeof(double) * (size_t)nval));
+    SCK(cudaMalloc(&Qv, sizeof(double) * (size_t)nval));
+    SCK(cudaMalloc(&act, sizeof(float) * 6 * (size_t)bs * SUR_H));
+    SCK(cudaMalloc(&dz, sizeof(float) * (size_t)bs * SUR_H));
+    SCK(cudaMalloc(&dz2, sizeof(float) * (size_t)bs * SUR_H));
+    SCK(cudaMalloc(&grad, sizeof(float) * SUR_NP));
+    SCK(cudaMalloc(&gpart, sizeof(float) * (size_t)KS * SUR_H * SUR_H));
+    SCK(cudaMalloc(&m1, sizeof(float) * SUR_NP));
+    SCK(cudaMalloc(&m2, sizeof(float) * SUR_NP));
+    SCK(cudaMalloc(&lpart, sizeof(double) * mse_blocks));
+    SCK(cudaMalloc(&stats, sizeof(double) * SUR_NBINS));
+    SCK(cudaMalloc(&dstatus, sizeof(int)));
+    SCK(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+    {   // Glorot-uniform initial weights, zero biases (host RNG, seeded)
+        std::vector<float> h(SUR_NP, 0.f);
+        uint64_t z = o->seed * 0x2545F4914F6CDD1Dull + 1;
+        auto rnd = [&]() { z ^= z << 13; z ^= z >> 7; z ^= z << 17; return (double)(z >> 11) / 9007199254740992.0; };
+        for (int l = 0; l < 5; l++) {
+            const double a = sqrt(6.0 / (g_dims[l] + g_dims[l + 1]));
+            for (size_t i = 0; i < (size_t)g_dims[l] * g_dims[l + 1]; i++) h[off[l] + i] = (float)((2 * rnd() - 1) * a);
+        }
+        SCK(cudaMemcpyAsync(st.params, h.data(), sizeof(float) * SUR_NP, cudaMemcpyHostToDevice, s));
+        SCK(cudaMemsetAsync(m1, 0, sizeof(float) * SUR_NP, s));
+        SCK(cudaMemsetAsync(m2, 0, sizeof(float) * SUR_NP, s));
+        SCK(cudaStreamSynchronize(s));
+    }
+    // training and validation samples from the quadrature
+    k_sur_samples<<<(ntr + 127) / 128, 128, 0, s>>>(ntr, o->seed, 0, X, T, nullptr, nullptr, nullptr, Wtr);
+    k_sur_samples<<<(nval + 127) / 128, 128, 0, s>>>(nval, o->seed ^ 0x5DEECE66Dull, 1, Xv, Tv, Gv, Bv, Qv,
+                                                      nullptr);
+    SCK(cudaGetLastError());
+    {   // target mean and spread, mean weight (host, double), then normalise on the device
+        std::vector<float> ht(2 * (size_t)ntr), hw(ntr);
+        SCK(cudaMemcpyAsync(ht.data(), T, sizeof(float) * ht.size(), cudaMemcpyDeviceToHost, s));
+        SCK(cudaMemcpyAsync(hw.data(), Wtr, sizeof(float) * hw.size(), cudaMemcpyDeviceToHost, s));
+        SCK(cudaStreamSynchronize(s));
+        double wmean = 0;
+        for (int i = 0; i < ntr; i++) wmean += hw[i];
+        wmean = std::max(wmean / ntr, 1e-30);
+        for (int o2 = 0; o2 < 2; o2++) {
+            double a = 0, b = 0;
+            for (int i = 0; i < ntr; i++) { const double v = ht[2 * (size_t)i + o2]; a += v; b += v * v; }
+            a /= ntr;
+            mu[o2] = (float)a;
+            sg[o2] = (float)std::max(sqrt(std::max(b / ntr - a * a, 0.0)), 1e-6);
+        }
+        // loss weight: 0.1 + 0.9 |alpha|^2 / mean |alpha|^2 -- the deflection
+        // error the gate tests is |alpha| times the relative error the loss sees
+        k_sur_affine<<<(ntr + 255) / 256, 256, 0, s>>>(ntr, T, mu[0], mu[1], 1.f / sg[0], 1.f / sg[1], Wtr,
+                                                        (float)(0.9 / wmean), 0.1f);
+    }
+    {
+        const float b1 = 0.9f, b2 = 0.999f;
+        double p1 = 1, p2 = 1;
+        for (int it = 0; it < steps; it++) {
+            const size_t base = ((size_t)it * bs) % (size_t)(ntr - bs + 1);
+            sur_fwd_bwd(s, st.params, X + 3 * base, T + 2 * base, Wtr + base, bs, act, dz, dz2, gpart, KS, grad,
+                        lpart, mse_blocks);
+            // Adam: linear warm-up over the first 2 % of the steps, then a
+            // cosine decay of the learning rate to 0.1 % of o->lr
+            p1 *= b1; p2 *= b2;
+            const double frac = (double)it / steps;
+            const double warm = std::min(1.0, (it + 1) / (0.02 * steps + 1));
+            const float lr = (float)(o->lr * warm * (0.001 + 0.999 * 0.5 * (1 + cos(M_PI * frac))));
+            k_sur_adam<<<(SUR_NP + 255) / 256, 256, 0, s>>>(SUR_NP, st.params, grad, m1, m2, lr, b1, b2,
+                                                            (float)(1.0 / (1 - p1)), (float)(1.0 / (1 - p2)));
+        }
+        double hp[64];
+        SCK(cudaMemcpyAsync(hp, lpart, sizeof(double) * mse_blocks, cudaMemcpyDeviceToHost, s));
+        SCK(cudaStreamSynchronize(s));
+        for (int b = 0; b < mse_blocks; b++) last_loss += hp[b];
+        last_loss /= bs;
+    }
+    SCK(cudaGetLastError());
+    // inference copies, then the error-bound table from the tensor-core path
+    k_sur_prep<<<64, 256, 0, s>>>(st.params, st.wt, st.small, mu[0], mu[1], sg[0], sg[1]);
+    SCK(cudaStreamSynchronize(s));
+    if (sur_maps(st) != QLP_OK) {
+        set_error("%s (%d)", "surrogate: tensor map encoding failed", 0);
+        rc = QLP_ERR_CUDA;
+        goto done;
+    }
+    SCK(cudaFuncSetAttribute(k_sur_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
+    SCK(cudaFuncSetAttribute(k_raytrace_sur, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
+    k_sur_infer<<<(nval + 127) / 128, 128, SUR_SMEM, s>>>(nval, Xv, Tnet, st.maps, st.small, dstatus);
+    k_sur_bound<<<(SUR_NBINS + 255) / 256, 256, 0, s>>>(SUR_NBINS, Tnet, Gv, Bv, Qv, st.bound, stats);
+    SCK(cudaGetLastError());
+    {
+        std::vector<double> hs(SUR_NBINS);
+        int hstat = 0;
+        SCK(cudaMemcpyAsync(hs.data(), stats, sizeof(double) * SUR_NBINS, cudaMemcpyDeviceToHost, s));
+        SCK(cudaMemcpyAsync(&hstat, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SCK(cudaStreamSynchronize(s));
+        if (hstat != 0) {
+            set_error("%s (%d)", "surrogate: tensor-core inference timed out", hstat);
+            rc = QLP_ERR_TIMEOUT;
+            goto done;
+        }
+        double mx = 0, sum = 0;
+        int below = 0;
+        for (double v : hs) { mx = std::max(mx, v); sum += v; below += (SUR_BOUND_SAFETY * v <= 1e-5); }
+        st.rep.final_loss = last_loss;
+        st.rep.val_max_rel = mx;
+        st.rep.val_mean_rel = sum / SUR_NBINS;
+        st.rep.cells_below_1e5 = (double)below / SUR_NBINS;
+        st.rep.n_params = SUR_NP;
+        st.rep.n_train = ntr;
+        st.rep.steps = steps;
+        st.rep.train_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+        st.ready = true;
+        if (rep) *rep = st.rep;
+    }
+done:
+    void* bufs[] = {X, T, Wtr, Xv, Tv, Tnet, Gv, Bv, Qv, act, dz, dz2, grad, gpart, m1, m2, lpart, stats, dstatus};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (s) cudaStreamDestroy(s);
+    return rc;
+}
+
+bool surrogate_ready(int device) { return device >= 0 && device < 64 && g_sur[device].ready; }
+
+// One forward + backward pass of the training kernels on a given batch and
+// parameter vector, unweighted (the gradient test).  grad: SUR_NP floats.
+int surrogate_grad_check(int device, const float* params, const float* x, const float* t, int batch, double* loss,
+                         float* grad_out)
+{
+    if (cudaSetDevice(device) != cudaSuccess) return QLP_ERR_NO_DEVICE;
+    const int bs = batch, KS = std::max(1, bs / 256), mse_blocks = 64;
+    float *P = nullptr, *X = nullptr, *T = nullptr, *act = nullptr, *dz = nullptr, *dz2 = nullptr, *grad = nullptr,
+          *gpart = nullptr;
+    double* lpart = nullptr;
+    int rc = QLP_OK;
+    double hp[64];
+    cudaStream_t s = nullptr;
+    SCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    SCK(cudaMalloc(&P, sizeof(float) * SUR_NP));
+    SCK(cudaMalloc(&X, sizeof(float) * 3 * (size_t)bs));
+    SCK(cudaMalloc(&T, sizeof(float) * 2 * (size_t)bs));
+    SCK(cudaMalloc(&act, sizeof(float) * 6 * (size_t)bs * SUR_H));
+    SCK(cudaMalloc(&dz, sizeof(float) * (size_t)bs * SUR_H));
+    SCK(cudaMalloc(&dz2, sizeof(float) * (size_t)bs * SUR_H));
+    SCK(cudaMalloc(&grad, sizeof(float) * SUR_NP));
+    SCK(cudaMalloc(&gpart, sizeof(float) * (size_t)KS * SUR_H * SUR_H));
+    SCK(cudaMalloc(&lpart, sizeof(double) * mse_blocks));
+    SCK(cudaMemcpyAsync(P, params, sizeof(float) * SUR_NP, cudaMemcpyHostToDevice, s));
+    SCK(cudaMemcpyAsync(X, x, sizeof(float) * 3 * (size_t)bs, cudaMemcpyHostToDevice, s));
+    SCK(cudaMemcpyAsync(T, t, sizeof(float) * 2 * (size_t)bs, cudaMemcpyHostToDevice, s));
+    sur_fwd_bwd(s, P, X, T, nullptr, bs, act, dz, dz2, gpart, KS, grad, lpart, mse_blocks);
+    SCK(cudaGetLastError());
+    SCK(cudaMemcpyAsync(hp, lpart, sizeof(double) * mse_blocks, cudaMemcpyDeviceToHost, s));
+    SCK(cudaMemcpyAsync(grad_out, grad, sizeof(float) * SUR_NP, cudaMemcpyDeviceToHost, s));
+    SCK(cudaStreamSynchronize(s));
+    {
+        double l = 0;
+        for (int b = 0; b < mse_blocks; b++) l += hp[b];
+        *loss = l / bs;
+    }
+done:
+    void* bufs[] = {P, X, T, act, dz, dz2, grad, gpart, lpart};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (s) cudaStreamDestroy(s);
+    return rc;
+}
+
+// At n points (rho, phi, q): t = log(G/B) through the tensor-core inference
+// path, the quadrature's G, the baselines and each point's cell bound.
+int surrogate_eval(int device, const double* rpq, int n, double* t_net, double* G_quad, double* B, double* bound_out)
+{
+    if (!surrogate_ready(device)) {
+        set_error("%s (%d)", "surrogate not trained on this device", device);
+        return QLP_ERR_ARG;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return QLP_ERR_NO_DEVICE;
+    SurState& st = g_sur[device];
+    int rc = QLP_OK;
+    cudaStream_t s = nullptr;
+    float *X = nullptr, *T = nullptr;
+    double *P = nullptr, *G = nullptr, *Bd = nullptr;
+    int* dstatus = nullptr;
+    int hstat = 0;
+    std::vector<float> ht(2 * (size_t)n), hb(SUR_NBINS);
+    SCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    SCK(cudaMalloc(&X, sizeof(float) * 3 * (size_t)n + 16));
+    SCK(cudaMalloc(&T, sizeof(float) * 2 * (size_t)n + 16));
+    SCK(cudaMalloc(&P, sizeof(double) * 3 * (size_t)n + 16));
+    SCK(cudaMalloc(&G, sizeof(double) * 2 * (size_t)n + 16));
+    SCK(cudaMalloc(&Bd, sizeof(double) * (size_t)n + 16));
+    SCK(cudaMalloc(&dstatus, sizeof(int)));
+    SCK(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
+    SCK(cudaMemcpyAsync(P, rpq, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s));
+    k_sur_points<<<(n + 127) / 128, 128, 0, s>>>(n, P, X, G, Bd);
+    k_sur_infer<<<(n + 127) / 128, 128, SUR_SMEM, s>>>(n, X, T, st.maps, st.small, dstatus);
+    SCK(cudaGetLastError());
+    SCK(cudaMemcpyAsync(ht.data(), T, sizeof(float) * 2 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    SCK(cudaMemcpyAsync(hb.data(), st.bound, sizeof(float) * SUR_NBINS, cudaMemcpyDeviceToHost, s));
+    if (G_quad) SCK(cudaMemcpyAsync(G_quad, G, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (B) SCK(cudaMemcpyAsync(B, Bd, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+    SCK(cudaMemcpyAsync(&hstat, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SCK(cudaStreamSynchronize(s));
+    if (hstat) {
+        rc = QLP_ERR_TIMEOUT;
+        goto done;
+    }
+    for (int i = 0; i < n; i++) {   // t = (1 - q) s
+        const double rho = rpq[3 * (size_t)i], phi = rpq[3 * (size_t)i + 1];
+        double q = rpq[3 * (size_t)i + 2];
+        if (q >= 1.0) q = 0.999999;
+        t_net[2 * (size_t)i] = (1.0 - q) * ht[2 * (size_t)i];
+        t_net[2 * (size_t)i + 1] = (1.0 - q) * ht[2 * (size_t)i + 1];
+        if (bound_out) {
+            const int c = sur_cell(rho, phi, q);
+            bound_out[i] = (c < 0) ? INFINITY : (double)hb[c];
+        }
+    }
+done:
+    void* bufs[] = {X, T, P, G, Bd, dstatus};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (s) cudaStreamDestroy(s);
+    return rc;
+}
+
+// ray shooting through the surrogate (ctx.cpp selects it)
+int launch_raytrace_sur(const StaticData& sd, Work& w, double thresh, int defer_lens, cudaStream_t st)
+{
+    if (sd.n_sub == 0) return QLP_OK;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!surrogate_ready(dev)) {
+        set_error("%s (%d)", "no trained NFW surrogate on this device", dev);
+        return QLP_ERR_ARG;
+    }
+    SurState& S = g_sur[dev];
+    cudaMemsetAsync(w.fb_count, 0, sizeof(int), st);
+    k_raytrace_sur<<<(sd.n_sub + 127) / 128, 128, SUR_SMEM, st>>>(sd, w.ep, w.spx, w.spy, S.maps, S.small, S.bound,
+                                                                   thresh, defer_lens, w.fb_count, w.fb_ray,
+                                                                   w.fb_xy, w.gs, w.out);
+    int n = 1;
+    if (defer_lens >= 0) {
+        const int blocks = std::min((sd.n_sub + 255) / 256, 152 * 8);
+        k_nfw_fallback<<<blocks, 256, 0, st>>>(w.ep, defer_lens, w.fb_count, w.fb_ray, w.fb_xy, w.spx, w.spy);
+        n++;
+    }
+    count_launches(n);
+    return QLP_OK;
+}
+
+}  // namespace qlpix

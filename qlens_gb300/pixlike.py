@@ -63,6 +63,13 @@ def load_library(build_if_missing=False):
     L.qlp_last_transfer_bytes.argtypes = [C.c_void_p, P(C.c_longlong), P(C.c_longlong)]
     L.qlp_spd_solve_logdet_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p]
+    L.qlp_surrogate_defaults.argtypes = [P(abi.qlp_surrogate_opts)]
+    L.qlp_nfw_surrogate_train.argtypes = [C.c_int, P(abi.qlp_surrogate_opts), P(abi.qlp_surrogate_report)]
+    L.qlp_set_nfw_mode.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.qlp_surrogate_grad_check.argtypes = [C.c_int, P(C.c_float), P(C.c_float), P(C.c_float), C.c_int,
+                                           P(C.c_double), P(C.c_float)]
+    L.qlp_surrogate_eval.argtypes = [C.c_int, P(C.c_double), C.c_int, P(C.c_double), P(C.c_double),
+                                     P(C.c_double), P(C.c_double)]
     L.qlp_last_error.restype = C.c_char_p
     L.qlp_destroy.argtypes = [C.c_void_p]
     _lib = L
@@ -166,6 +173,11 @@ class PixelLikelihood:
         """Replay captured CUDA graphs in eval_batch (default) or launch kernel by kernel."""
         self._check(self.lib.qlp_set_graphs(self.ctx, 1 if on else 0))
 
+    def set_nfw_mode(self, mode, threshold_arcsec=0.0):
+        """abi.QLP_NFW_QUADRATURE or abi.QLP_NFW_SURROGATE (after train_nfw_surrogate);
+        threshold_arcsec <= 0 keeps the default gate (2e-5 arcsec)."""
+        self._check(self.lib.qlp_set_nfw_mode(self.ctx, int(mode), float(threshold_arcsec)))
+
     def last_transfer_bytes(self):
         """(host->device, device->host) bytes moved by the last call."""
         h, d = C.c_longlong(), C.c_longlong()
@@ -264,3 +276,62 @@ class PixelLikelihood:
             self.close()
         except Exception:
             pass
+
+
+# ---- learned NFW deflection -------------------------------------------------
+SURROGATE_NP = 50306        # 3 -> 4 x 128 tanh -> 2
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def train_nfw_surrogate(device=0, **kw):
+    """Train the NFW deflection surrogate on `device` (qlp_nfw_surrogate_train);
+    keyword arguments override qlp_surrogate_opts fields.  Returns the report."""
+    L = load_library()
+    o = abi.qlp_surrogate_opts()
+    L.qlp_surrogate_defaults(C.byref(o))
+    for k, v in kw.items():
+        if k not in dict(abi.qlp_surrogate_opts._fields_):
+            raise TypeError("unknown surrogate option %r" % k)
+        setattr(o, k, v)
+    rep = abi.qlp_surrogate_report()
+    code = L.qlp_nfw_surrogate_train(int(device), C.byref(o), C.byref(rep))
+    if code != abi.QLP_OK:
+        raise QLPixError(code, L.qlp_last_error().decode())
+    return rep.as_dict()
+
+
+def surrogate_grad_check(params, x, t, device=0):
+    """One forward + backward pass of the training kernels (unweighted mean
+    squared error): returns (loss, grad) for params [50306], x [n][3], t [n][2]."""
+    L = load_library()
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    assert params.shape == (SURROGATE_NP,) and x.shape[1] == 3 and t.shape == (x.shape[0], 2)
+    grad = np.empty(SURROGATE_NP, dtype=np.float32)
+    loss = C.c_double(0)
+    code = L.qlp_surrogate_grad_check(int(device), _fp(params), _fp(x), _fp(t), x.shape[0], C.byref(loss),
+                                      _fp(grad))
+    if code != abi.QLP_OK:
+        raise QLPixError(code, L.qlp_last_error().decode())
+    return loss.value, grad
+
+
+def surrogate_eval(rho_phi_q, device=0):
+    """The trained network through the tensor-core inference path at points
+    (log R, phi, q): returns (t [n][2] = log(G/B), quadrature G [n][2],
+    baseline B [n], cell bound [n])."""
+    L = load_library()
+    p = np.ascontiguousarray(rho_phi_q, dtype=np.float64)
+    n = p.shape[0]
+    t = np.empty((n, 2))
+    G = np.empty((n, 2))
+    B = np.empty(n)
+    bound = np.empty(n)
+    code = L.qlp_surrogate_eval(int(device), _dp(p), n, _dp(t), _dp(G), _dp(B), _dp(bound))
+    if code != abi.QLP_OK:
+        raise QLPixError(code, L.qlp_last_error().decode())
+    return t, G, B, bound
