@@ -232,7 +232,10 @@ def main():
             pl.set_nfw_mode(abi.QLP_NFW_SURROGATE)
             nfw = {"mode": "surrogate", "threshold_arcsec": 2e-5, "train_ms": rep["train_ms"],
                    "val_mean_rel": rep["val_mean_rel"], "n_params": rep["n_params"]}
-    B = args.batch or (32 if precision == "mixed" else 4)
+    uneven = wl.draw_instances is not None      # per-instance masks, source grids and lambdas
+    if uneven:
+        pl.set_instance_masks(wl.instance_masks)
+    B = args.batch or (4096 if uneven else 32 if precision == "mixed" else 4)
     pl.set_batch_slots(args.slots or min(B, 32))
     pl.set_graphs(not args.no_graphs)
     stream = torch.cuda.current_stream()
@@ -241,9 +244,14 @@ def main():
     rng = np.random.default_rng(1234 + rank)
     batches = [wl.draw(rng, B) for _ in range(args.warmup + args.steps)]
     pinned = [torch.from_numpy(b).pin_memory() for b in batches]
+    insts = [wl.draw_instances(rng, B) if uneven else (None, None, None) for _ in batches]
+
+    def run_step(k):
+        ids, sizes, lam = insts[k]
+        return pl.eval_batch(pinned[k].numpy(), regparams=lam, mask_ids=ids, src_sizes=sizes)
 
     for k in range(args.warmup):
-        pl.eval_batch(pinned[k].numpy())
+        run_step(k)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -260,7 +268,7 @@ def main():
     t0 = time.perf_counter()
     e0.record(stream)
     for k in range(args.steps):
-        res = pl.eval_batch(pinned[args.warmup + k].numpy())
+        res = run_step(args.warmup + k)
         dev_ms += pl.last_device_ms()
         launches += pl.last_launch_count()
         hb, db = pl.last_transfer_bytes()
@@ -330,6 +338,8 @@ def main():
             "data": "synthetic (seeded mock image; parameters drawn from the prior box)",
             "config": {**wl.describe(), "batch_per_step": B, "precision": precision,
                        "slots": args.slots or min(B, 32),
+                       "uneven": ("per vector: one of %d masks (r 1.5-3.0\"), source side 20-64, "
+                                  "log10 lambda 0-2" % len(wl.instance_masks)) if uneven else None,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set (dense L' %.0f MB) exceeds the 129 MB L2" % (
                            8e-6 * max(r["n_active_pixels"] for r in results) * max(r["n_active_src"] for r in results))},

@@ -130,6 +130,7 @@ class Workload:
         self.instance_masks = instance_masks
         self.instance_src = instance_src
         self.zfac, self.beta = zfac, beta
+        self.draw_instances = None     # (rng, n) -> (mask ids, source sizes, lambdas) for uneven batches
 
     @property
     def n_mask(self):
@@ -214,9 +215,20 @@ def cfg3(seed=3, n_instances=64):
         p[:, 9], p[:, 10] = x0, y0
         return p
 
-    return Workload("cfg3: 100x100 @0.05\", per-instance r in [1.5,3]\", 2x2 split, 11x11 PSF, source side 20-64",
-                    xv, yv, data, mask, psf, 0.02, 2, (64, 64), lenses, 10.0, draw,
-                    instance_masks=masks, instance_src=np.stack([sides, sides], 1))
+    wl = Workload("cfg3: 100x100 @0.05\", per-instance r in [1.5,3]\", 2x2 split, 11x11 PSF, source side 20-64",
+                  xv, yv, data, mask, psf, 0.02, 2, (64, 64), lenses, 10.0, draw,
+                  instance_masks=masks, instance_src=np.stack([sides, sides], 1))
+
+    def draw_instances(rng, n):
+        """Per vector: one of the instance masks, its own source-grid side
+        (uniform 20-64) and regularisation parameter (log10 lambda uniform 0-2)."""
+        ids = rng.integers(0, n_instances, n)
+        side = rng.integers(20, 65, n)
+        lam = 10.0 ** rng.uniform(0.0, 2.0, n)
+        return ids, np.stack([side, side], 1), lam
+
+    wl.draw_instances = draw_instances
+    return wl
 
 
 def cfg4(seed=4):
