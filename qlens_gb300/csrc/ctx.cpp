@@ -253,16 +253,19 @@ static bool model_has_nfw(const qlp_ctx* c)
 }
 
 // The launch sequence of one evaluation on stream st with the workspace of
-// `slot`; sd / so select the mask and source grid.  Everything that changes
-// between evaluations (lens model, regularisation parameter) is read from the
-// slot's EvalParams in device memory, so the sequence can be captured once
-// and replayed.  ev (QLP_N_STAGES+1 events, or null) brackets the stages.
+// `slot`; sd / so size the launches (the evaluation's own mask and source
+// grid, or the slot's capacity when the sequence is captured for replay).
+// Everything that changes between evaluations (lens model, regularisation
+// parameter, mask and source-grid size) is read from the slot's EvalParams in
+// device memory, so one captured sequence serves every evaluation the slot
+// runs.  ev (QLP_N_STAGES+1 events, or null) brackets the stages.
 static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const SrcOpts& so_in, cudaStream_t st,
                         cudaEvent_t* ev)
 {
     StaticData sd = sd_in;
     SrcOpts so = so_in;
     Work& w = slot.w;
+    sd.shape = &w.ep->shape;
     const int Mc = slot.M_cap;
     const int N_max = sd.n_mask;
     const double* regp = regparam_dev(w);
@@ -323,7 +326,7 @@ static int prepare_slot(qlp_ctx* c, Slot& s)
     return ensure_fp64_mats(s);
 }
 
-// Capture the slot's launch sequence for this (mask, source grid) as a graph.
+// Capture the slot's launch sequence, sized for its capacity, as a graph.
 static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const int key[6])
 {
     drop_graph(s);
@@ -349,16 +352,25 @@ static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpt
 
 // One evaluation on slot s: upload its parameters, run (replay or launch) the
 // sequence, copy its result to *h_dst -- all asynchronous on the slot stream.
-static int issue_eval(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, int mask_id,
-                      const EvalParams* h_ep, EvalOut* h_dst, cudaEvent_t* ev)
+static int issue_eval(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const EvalParams* h_ep,
+                      EvalOut* h_dst, cudaEvent_t* ev)
 {
     CK(cudaMemcpyAsync(s.w.ep, h_ep, sizeof(EvalParams), cudaMemcpyHostToDevice, s.stream), "h2d");
     if (c->use_graphs && ev == nullptr) {
-        const int key[6] = {c->precision, mask_id, so.snx, so.sny, model_has_nfw(c) ? 1 : 0, c->nfw_mode};
+        // one graph per slot for every mask and source grid that fits its
+        // capacity: the launches are sized for the capacity, the kernels read
+        // the actual sizes from the EvalParams just uploaded
+        StaticData sdc = sd;
+        sdc.n_mask = s.N_cap;
+        sdc.n_sub = s.N_cap * sd.nsub;
+        SrcOpts soc = so;
+        soc.snx = s.snx_cap;
+        soc.sny = s.sny_cap;
+        const int key[6] = {c->precision, s.N_cap, s.snx_cap, s.sny_cap, model_has_nfw(c) ? 1 : 0, c->nfw_mode};
         bool ok = s.graph && s.graph_gen == c->graph_gen;
         for (int i = 0; ok && i < 6; i++) ok = (s.graph_key[i] == key[i]);
         if (!ok) {
-            int r = capture_graph(c, s, sd, so, key);
+            int r = capture_graph(c, s, sdc, soc, key);
             if (r != QLP_OK) return r;
         }
         CK(cudaGraphLaunch(s.graph, s.stream), "graph launch");
@@ -423,12 +435,13 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     r = build_lens_model(c, lens_params, ep.lm);
     if (r != QLP_OK) { out->status = r; return r; }
     ep.regparam = (regparam > 0) ? regparam : c->opts.regparam;
+    ep.shape = InstShape{c->sd.mpix, c->sd.n_mask, c->sd.n_sub, c->so.snx, c->so.sny};
     Slot& s = c->slots[0];
     long long l0 = kernel_launch_counter();
     cudaStream_t st = c->stream;
     CK(cudaEventRecord(c->fork, st), "event");
     CK(cudaStreamWaitEvent(s.stream, c->fork, 0), "wait");
-    r = issue_eval(c, s, c->sd, c->so, -1, &ep, &c->h_out[0], c->ev);
+    r = issue_eval(c, s, c->sd, c->so, &ep, &c->h_out[0], c->ev);
     if (r != QLP_OK) { out->status = r; return r; }
     CK(cudaEventRecord(s.done, s.stream), "event");
     CK(cudaStreamWaitEvent(st, s.done, 0), "wait");
@@ -456,7 +469,7 @@ int ctx_set_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)
         c->mask_cnt.push_back((int)v.size());
         all.insert(all.end(), v.begin(), v.end());
     }
-    c->graph_gen++;                       // captured graphs hold the old mask pointers
+    // captured graphs stay valid: the mask pointers travel in EvalParams
     if (c->d_inst_mpix) { cudaFree(c->d_inst_mpix); c->d_inst_mpix = nullptr; }
     CK(dalloc(&c->d_inst_mpix, all.size()), "alloc");
     if (!all.empty())
@@ -520,10 +533,9 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         ep.regparam = (regparams && regparams[i] > 0) ? regparams[i] : c->opts.regparam;
         StaticData sd = c->sd;
         SrcOpts so = c->so;
-        int mask_id = -1;
         if (inst) {
             if (inst[i].mask_id >= 0) {
-                mask_id = inst[i].mask_id;
+                const int mask_id = inst[i].mask_id;
                 sd.mpix = c->d_inst_mpix + c->mask_off[mask_id];
                 sd.n_mask = c->mask_cnt[mask_id];
                 sd.n_sub = sd.n_mask * sd.nsub;
@@ -531,8 +543,9 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
             if (inst[i].src_npixels_x > 0) { so.snx = inst[i].src_npixels_x; so.sny = inst[i].src_npixels_y; }
         }
         if (ri == QLP_OK && (so.snx < 2 || so.sny < 2)) ri = QLP_ERR_GRID_TOO_SMALL;
+        ep.shape = InstShape{sd.mpix, sd.n_mask, sd.n_sub, so.snx, so.sny};
         if (ri == QLP_OK)
-            ri = issue_eval(c, s, sd, so, mask_id, &ep, &c->h_out[i], timed ? &c->ev_pool[(size_t)ne * i] : nullptr);
+            ri = issue_eval(c, s, sd, so, &ep, &c->h_out[i], timed ? &c->ev_pool[(size_t)ne * i] : nullptr);
         pre[i] = ri;
         if (ri != QLP_OK && rc == QLP_OK) rc = ri;
     }

@@ -158,11 +158,12 @@ __device__ __forceinline__ int act_at(const int* ai, int snx, int sny, int i, in
     return ai[j * snx + i];
 }
 
-__global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ ai, int snx, int sny,
+__global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ ai,
                       const double* __restrict__ regp, double* __restrict__ F, double* __restrict__ R, int ldF,
                       int do_reg)
 {
     const double regparam = *regp;
+    const int snx = gs->snx, sny = gs->sny;
     const int M = gs->M, Mp = mpad64(M);
     const int ncell = snx * sny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
@@ -198,8 +199,7 @@ void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* 
     const int ncell = so.snx * so.sny;
     if (so.regularization) cudaMemsetAsync(w.R, 0, sizeof(double) * (size_t)w.ldF * w.ldF, st);
     int total = ncell + 64;
-    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regp, w.F, w.R, w.ldF,
-                                               so.regularization);
+    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, regp, w.F, w.R, w.ldF, so.regularization);
     count_launches(1);
     (void)M_max;
 }
@@ -247,11 +247,13 @@ __global__ void __launch_bounds__(256) k_model(const GridState* __restrict__ gs,
     }
 }
 
-__global__ void __launch_bounds__(1024) k_final(StaticData sd, SrcOpts so, const GridState* __restrict__ gs,
+__global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, const GridState* __restrict__ gs,
                                                 const int* __restrict__ rowidx, const double* __restrict__ model,
                                                 const double* __restrict__ s, const int* __restrict__ ai,
                                                 const double* __restrict__ regp, EvalOut* out)
 {
+    const StaticData sd = eval_shape(sd_);
+    const SrcOpts so = eval_grid(so_, sd_);
     const double regparam = *regp;
     __shared__ double red[2][32];
     const int M = gs->M;

@@ -20,10 +20,12 @@ namespace qlpix {
 // thread 0 lays out the corners sequentially.  The clamp to the sourcegrid
 // limits is order independent: bound = (extreme beyond limit) ? limit : extreme.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_grid(StaticData sd, SrcOpts so, const double* __restrict__ spx,
+__global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, const double* __restrict__ spx,
                                                const double* __restrict__ spy, double* cx, double* cy,
                                                double* ccx, double* ccy, GridState* gs)
 {
+    const StaticData sd = eval_shape(sd_);
+    const SrcOpts so = eval_grid(so_, sd_);
     __shared__ double red[4][32];
     __shared__ int cnt_s[32];
     double xmn = DBL_MAX, xmx = -DBL_MAX, ymn = DBL_MAX, ymx = -DBL_MAX;
@@ -110,7 +112,7 @@ void launch_grid(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t 
 // unique cell with x_i <= px < x_{i+1}, y_j <= py < y_{j+1}, so two binary
 // searches over the accumulated corner arrays give the same cell.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_locate(StaticData sd, SrcOpts so, const double* __restrict__ spx,
+__global__ void __launch_bounds__(256) k_locate(StaticData sd_, SrcOpts so_, const double* __restrict__ spx,
                                                 const double* __restrict__ spy, const double* __restrict__ cx_g,
                                                 const double* __restrict__ cy_g, const double* __restrict__ ccx_g,
                                                 const double* __restrict__ ccy_g, int* __restrict__ cell3,
@@ -118,6 +120,8 @@ __global__ void __launch_bounds__(256) k_locate(StaticData sd, SrcOpts so, const
                                                 int* __restrict__ pixmaps)
 {
     extern __shared__ double sm[];
+    const StaticData sd = eval_shape(sd_);
+    const SrcOpts so = eval_grid(so_, sd_);
     const int snx = so.snx, sny = so.sny;
     double* cx = sm;
     double* cy = cx + snx + 1;
@@ -205,7 +209,7 @@ __device__ int block_exclusive_scan(int v, int* warp_tot)
     return base + x - v;
 }
 
-__global__ void __launch_bounds__(1024) k_compact(StaticData sd, SrcOpts so, const int* __restrict__ mapped,
+__global__ void __launch_bounds__(1024) k_compact(StaticData sd_, SrcOpts so_, const int* __restrict__ mapped,
                                                   int* __restrict__ active_index, const int* __restrict__ cell3,
                                                   const int* __restrict__ pixmaps, int* __restrict__ rowidx,
                                                   int* __restrict__ pixindex, int* __restrict__ rowptr,
@@ -213,6 +217,8 @@ __global__ void __launch_bounds__(1024) k_compact(StaticData sd, SrcOpts so, con
 {
     __shared__ int wt[33];
     __shared__ int tot_s;
+    const StaticData sd = eval_shape(sd_);
+    const SrcOpts so = eval_grid(so_, sd_);
     const int T = blockDim.x;
     // ---- source cells ----
     const int ncell = so.snx * so.sny;
@@ -284,13 +290,14 @@ void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream
 // i.e. exactly the row of convert_Lmatrix_to_dense, pixelgrid.cpp:13734-13739),
 // which the PSF kernel gathers from.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_build_L(StaticData sd, const int* __restrict__ rowidx,
+__global__ void __launch_bounds__(128) k_build_L(StaticData sd_, const int* __restrict__ rowidx,
                                                  const int* __restrict__ rowptr, const int* __restrict__ cell3,
                                                  const double* __restrict__ w3, const int* __restrict__ active_index,
                                                  int* __restrict__ Lidx, double* __restrict__ Lval,
                                                  int* __restrict__ cidx, double* __restrict__ cval,
                                                  int* __restrict__ ccnt)
 {
+    const StaticData sd = eval_shape(sd_);
     const int nsub = sd.nsub;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
         const int r = rowidx[m];

@@ -242,11 +242,12 @@ __device__ __forceinline__ int act_at32(const int* ai, int snx, int sny, int i, 
     return ai[j * snx + i];
 }
 
-__global__ void k_reg32(const GridState* __restrict__ gs, const int* __restrict__ ai, int snx, int sny,
+__global__ void k_reg32(const GridState* __restrict__ gs, const int* __restrict__ ai,
                         const double* __restrict__ regp, float* __restrict__ F, float* __restrict__ R, int ld,
                         int do_reg)
 {
     const double regparam = *regp;
+    const int snx = gs->snx, sny = gs->sny;
     const int M = gs->M, Mp = (M + 127) & ~127;   // identity up to the 128-block padding
     const int ncell = snx * sny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
@@ -304,11 +305,12 @@ __global__ void k_axpy(const GridState* __restrict__ gs, const double* __restric
 
 // r = D - v - lambda R s   (v = L'^T C^-1 L' s; R applied by its stencil)
 __global__ void k_residual(const GridState* __restrict__ gs, const double* __restrict__ D,
-                           const double* __restrict__ vv, const int* __restrict__ ai, int snx, int sny,
+                           const double* __restrict__ vv, const int* __restrict__ ai,
                            const double* __restrict__ regp, int do_reg, const double* __restrict__ s,
                            double* __restrict__ r)
 {
     const double regparam = *regp;
+    const int snx = gs->snx, sny = gs->sny;
     const int M = gs->M;
     const int ncell = snx * sny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
@@ -473,8 +475,8 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
     }
     if (ev) cudaEventRecord(ev[4], st);
     if (so.regularization) cudaMemsetAsync(m->R32, 0, sizeof(float) * (size_t)m->ld32 * m->ld32, st);
-    k_reg32<<<(so.snx * so.sny + 128 + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, so.snx, so.sny, regp,
-                                                                m->F32, m->R32, m->ld32, so.regularization);
+    k_reg32<<<(so.snx * so.sny + 128 + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, regp, m->F32, m->R32,
+                                                                m->ld32, so.regularization);
     n++;
     if (so.regularization) {
         // R's factorisation (log det R only) runs on the slot's second stream,
@@ -508,8 +510,8 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
         op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, st);
         op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, st);
         op_LTw(w, N_cap, m->M_cap, m->t, m->part, m->v, st);
-        k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, so.snx, so.sny,
-                                                                  regp, so.regularization, w.s, m->r);
+        k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, regp,
+                                                                  so.regularization, w.s, m->r);
         n++;
     }
     // model image P L s in FP64 for chi^2

@@ -95,8 +95,9 @@ __global__ void k_psf(StaticData sd, const GridState* __restrict__ gs, const int
 }
 
 // Active row -> image pixel, the inverse of the compaction's pixindex.
-__global__ void k_rowpix(StaticData sd, const int* __restrict__ rowidx, int* __restrict__ rowpix)
+__global__ void k_rowpix(StaticData sd_, const int* __restrict__ rowidx, int* __restrict__ rowpix)
 {
+    const StaticData sd = eval_shape(sd_);
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
         int r = rowidx[m];
         if (r >= 0) rowpix[r] = sd.mpix[m];

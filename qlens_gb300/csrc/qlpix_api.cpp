@@ -179,6 +179,7 @@ int qlp_set_lens_model(qlp_ctx* c, const qlp_lens* lenses, int nlens, const qlp_
     for (int k = 0; k < nlens; k++)
         if (lenses[k].plane < 0 || lenses[k].plane >= c->planes.n_planes || n_params_of(lenses[k].type) == 0)
             return fail(QLP_ERR_ARG, "bad lens type or plane");
+    c->graph_gen++;     // captured graphs select kernels by the lens list (NFW, deferred fallback)
     return QLP_OK;
 }
 
@@ -231,6 +232,7 @@ int qlp_set_nfw_mode(qlp_ctx* c, int mode, double threshold_arcsec)
         return fail(QLP_ERR_ARG, "no trained NFW surrogate on this device (qlp_nfw_surrogate_train)");
     c->nfw_mode = mode;
     c->nfw_threshold = (threshold_arcsec > 0) ? threshold_arcsec : 2e-5;
+    c->graph_gen++;     // the gate is a launch argument of the captured ray shooting
     return QLP_OK;
 }
 

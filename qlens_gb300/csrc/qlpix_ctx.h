@@ -27,8 +27,9 @@ struct Slot {
     // second stream of the slot: R's factorisation runs beside F's
     cudaStream_t side = nullptr;
     cudaEvent_t side_fork = nullptr, side_join = nullptr;
-    // the launch sequence captured as a CUDA graph, valid for one
-    // (precision, mask, source grid, NFW) combination and graph generation
+    // the launch sequence captured as a CUDA graph, sized for the slot's
+    // capacity (any mask and source grid that fit), valid for one
+    // (precision, capacity, NFW, NFW mode) combination and graph generation
     cudaGraphExec_t graph = nullptr;
     int graph_key[6] = {0, 0, 0, 0, 0, 0};
     long long graph_gen = 0;

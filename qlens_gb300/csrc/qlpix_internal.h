@@ -30,13 +30,25 @@ struct LensModel {
     LensRec lens[QLP_MAX_LENSES];
 };
 
+// Mask and source-grid size of one evaluation.  Kept in device memory (in
+// the slot's EvalParams): a batch with uneven masks and grids replays one
+// launch sequence sized for the slot's capacity, and the kernels take the
+// actual sizes from here.
+struct InstShape {
+    const int* mpix;          // n_mask masked pixels, j-outer / i-inner order
+    int n_mask, n_sub;        // masked pixels, sub-pixels
+    int snx, sny;             // source-grid cells
+};
+
 // What changes from one evaluation to the next: the lens model (meta
-// parameters computed on the host) and the regularisation parameter.  Kept in
+// parameters computed on the host), the regularisation parameter and the
+// mask / source-grid size.  Kept in
 // device memory, one copy per slot, so that one captured launch sequence (a
 // CUDA graph) serves every evaluation a slot runs.
 struct EvalParams {
     LensModel lm;
     double regparam;
+    InstShape shape;
 };
 
 // Source-grid state computed on the device each evaluation.
@@ -74,7 +86,22 @@ struct StaticData {            // per-context, uploaded once
     // fixed-point scale of the mixed path's L' accumulation: 2^fix_exp keeps
     // sum|psf| * max sqrt(C^-1) (a bound on every |L' sqrt(C^-1)| entry) below 2^61
     int fix_exp;
+    // device address of this evaluation's InstShape: the kernels take mpix,
+    // n_mask, n_sub and the source-grid size from there (the host-side copy
+    // of those fields only sizes the launches)
+    const InstShape* shape;
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ StaticData eval_shape(StaticData s)
+{
+    const InstShape* p = s.shape;
+    s.mpix = p->mpix;
+    s.n_mask = p->n_mask;
+    s.n_sub = p->n_sub;
+    return s;
+}
+#endif
 
 struct SrcOpts {
     int snx, sny;
@@ -85,6 +112,15 @@ struct SrcOpts {
     int regularization;
     double regparam;
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ SrcOpts eval_grid(SrcOpts o, const StaticData& s)
+{
+    o.snx = s.shape->snx;
+    o.sny = s.shape->sny;
+    return o;
+}
+#endif
 
 // Per-evaluation device workspace (sized for the largest case at creation).
 struct Work {

@@ -14,9 +14,10 @@
 namespace qlpix {
 
 template <bool NFW>
-__global__ void __launch_bounds__(256) k_raytrace(StaticData sd, const EvalParams* __restrict__ ep,
+__global__ void __launch_bounds__(256) k_raytrace(StaticData sd_, const EvalParams* __restrict__ ep,
                                                   double* __restrict__ spx, double* __restrict__ spy)
 {
+    const StaticData sd = eval_shape(sd_);
     // the lens model of this evaluation, staged in shared memory
     __shared__ __align__(16) LensModel lm;
     {

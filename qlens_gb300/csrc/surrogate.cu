@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(128, 1) k_sur_infer(int n, const float* __rest
 // the last plane), later in k_nfw_fallback at full occupancy (its lens-frame
 // position is queued and its contribution left out here).  out->pad counts
 // the fallbacks.
-__global__ void __launch_bounds__(128, 1) k_raytrace_sur(StaticData sd, const EvalParams* __restrict__ ep,
+__global__ void __launch_bounds__(128, 1) k_raytrace_sur(StaticData sd_, const EvalParams* __restrict__ ep,
                                                          double* __restrict__ spx, double* __restrict__ spy,
                                                          const __grid_constant__ SurMaps maps,
                                                          const float* __restrict__ small_g,
@@ -573,6 +573,8 @@ __global__ void __launch_bounds__(128, 1) k_raytrace_sur(StaticData sd, const Ev
                                                          int* __restrict__ fb_ray, double* __restrict__ fb_xy,
                                                          GridState* gs, EvalOut* out)
 {
+    const StaticData sd = eval_shape(sd_);
+    if ((int)blockIdx.x * 128 >= sd.n_sub) return;      // launched for the slot's capacity
     extern __shared__ unsigned char smem_raw[];
     __shared__ uint64_t tma_bar, mma_bar;
     __shared__ uint32_t tmem_slot;

@@ -124,3 +124,29 @@ def test_batch_with_nfw_and_two_planes():
         assert res[i]["status"] == 0
         assert abs(res[i]["m2logev"] - ro["m2logev"]) <= REL * abs(ro["m2logev"])
     pl.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_uneven_graph_replay_matches_direct(precision):
+    """One graph per slot serves every mask and source grid that fits the
+    slot: launched for the capacity, the kernels take the actual sizes from
+    the evaluation's parameters in device memory."""
+    from qlens_gb300 import abi
+    g = Golden("tiny_sie")
+    pl = _ctx(g, abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64)
+    pl.set_batch_slots(3)
+    pl.set_instance_masks(_instance_inputs(g, [0.8, 1.0, 1.2], 0.2))
+    P = _draws(g, 9, 13)
+    ids = [0, 1, 2, 2, 1, 0, -1, 1, 2]
+    sizes = [(8, 8), (6, 7), (10, 9), (5, 5), (9, 6), (7, 7), (0, 0), (8, 5), (6, 6)]
+    lam = [10.0, 3.0, 30.0, 10.0, 50.0, 1.0, 10.0, 7.0, 20.0]
+    pl.set_graphs(True)
+    a = pl.eval_batch(P, regparams=lam, mask_ids=ids, src_sizes=sizes)
+    a2 = pl.eval_batch(P, regparams=lam, mask_ids=ids, src_sizes=sizes)
+    pl.set_graphs(False)
+    b = pl.eval_batch(P, regparams=lam, mask_ids=ids, src_sizes=sizes)
+    for i, (ra, ra2, rb) in enumerate(zip(a, a2, b)):
+        assert ra["status"] == rb["status"] == 0, (i, ra["status"], rb["status"])
+        for k in ("m2logev", "chisq0", "logdet_F", "logdet_R", "n_active_pixels", "n_active_src", "L_nnz"):
+            assert ra[k] == rb[k] == ra2[k], (i, k, ra[k], rb[k])
+    pl.close()
