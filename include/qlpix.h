@@ -180,12 +180,21 @@ int qlp_eval(qlp_ctx* ctx, const double* lens_params, double regparam, qlp_resul
 int qlp_set_batch_slots(qlp_ctx* ctx, int slots);
 
 /* on = 1 (default): qlp_eval_batch captures each slot's launch sequence once
- * as a CUDA graph (per precision, mask and source-grid size) and replays it
- * for every evaluation, so one evaluation costs the host a parameter upload
- * and one graph launch instead of ~800 kernel launches.  on = 0: kernels are
- * launched one by one and qlp_stage_times reports the batch's stages.
- * No counterpart in the reference (it has no device launches). */
+ * as a CUDA graph, sized for the slot's capacity, and replays it for every
+ * evaluation (every mask and source-grid size that fits: the kernels read the
+ * actual sizes from the evaluation's parameters in device memory), so one
+ * evaluation costs the host a parameter upload and one graph launch instead
+ * of ~400 kernel launches.  on = 0: kernels are launched one by one and
+ * qlp_stage_times reports the batch's stages.  No counterpart in the
+ * reference (it has no device launches). */
 int qlp_set_graphs(qlp_ctx* ctx, int on);
+
+/* FP64 refinement sweeps of the mixed path's source amplitudes (0..4,
+ * default 1): r = D - F s in FP64 with the sparse operators, s += F32^-1 r.
+ * -2 log(evidence) is stationary in s at the solution, so its error is second
+ * order in the amplitude error; chisq0 alone is first order.  No counterpart
+ * in the reference (it solves in FP64). */
+int qlp_set_refinement(qlp_ctx* ctx, int sweeps);
 
 /* Number of doubles in one lens-parameter vector for the current model. */
 int qlp_n_params(const qlp_ctx* ctx);

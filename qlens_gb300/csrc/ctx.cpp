@@ -293,7 +293,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     launch_dvec(sd, w, N_max, st);
     const bool mixed = (c->precision == QLP_MIXED);
     if (mixed) {
-        int r = run_inversion_mixed(slot, sd, so, regp, st, ev);
+        int r = run_inversion_mixed(slot, sd, so, regp, c->refine, st, ev);
         if (r != QLP_OK) return r;
     } else {
         int r = ensure_fp64_mats(slot);
@@ -453,7 +453,7 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     for (int i = 0; i < QLP_N_STAGES; i++) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
     cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
     fill_result(c->h_out[0], out);
-    if (c->precision == QLP_MIXED) out->refine_iters = 2;
+    if (c->precision == QLP_MIXED) out->refine_iters = c->refine;
     return out->status;
 }
 
@@ -577,7 +577,7 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
             continue;
         }
         fill_result(c->h_out[i], &out[i]);
-        if (c->precision == QLP_MIXED) out[i].refine_iters = 2;
+        if (c->precision == QLP_MIXED) out[i].refine_iters = c->refine;
     }
     return rc;
 }

@@ -8,9 +8,9 @@
 //   F32   += lambda R, R32 = R                                  k_reg32
 //   L_F L_F^T = F32, L_R L_R^T = R32 (FP32 blocked Cholesky)    chol.cuh
 //   log det F, log det R: 2 sum log diag, accumulated in FP64
-//   D = L^T P^T (C^-1 d)                     (FP64, sparseops.cu)
-//   s = F32^-1 D, then twice: r = D - L^T P^T C^-1 P L s - lambda R s (FP64),
-//                              s += F32^-1 r
+//   D = L^T P^T (C^-1 d)                     (FP64; L^T from L by source cell)
+//   s = F32^-1 D, then `refine` times: r = D - L^T P^T C^-1 P L s - lambda R s (FP64),
+//                                       s += F32^-1 r
 //   model = P L s                             (FP64, for chi^2)
 // The plain FP64 path (linalg.cu) computes the same quantities entirely in
 // FP64; the mixed path's deviation from it is measured by the tests.
@@ -33,6 +33,9 @@ struct MixedWork {
     float* colval = nullptr; // nnz_cap
     float* sqc = nullptr;    // N_cap: sqrt(C^-1) per active row
     int nnz_cap = 0;
+    int* col_u = nullptr;    // nnz_cap: rows of each column in atomic (fill) order
+    int* src_u = nullptr;    // nnz_cap: their positions in the merged CSR rows
+    double* colval64 = nullptr; // nnz_cap: FP64 values, rows ascending within a column
     int chunk = 0;           // image rows per k_psf_x accumulator
     float* X_hi = nullptr;
     float* X_lo = nullptr;
@@ -156,18 +159,61 @@ __global__ void __launch_bounds__(1024) k_csc_scan(const GridState* __restrict__
 }
 
 __global__ void k_csc_fill(const GridState* __restrict__ gs, const int* __restrict__ rowptr,
-                           const int* __restrict__ cidx, const double* __restrict__ cval,
-                           const int* __restrict__ ccnt, int* __restrict__ cursor, int* __restrict__ colrow,
-                           float* __restrict__ colval)
+                           const int* __restrict__ cidx, const int* __restrict__ ccnt, int* __restrict__ cursor,
+                           int* __restrict__ col_u, int* __restrict__ src_u)
 {
     const int N = gs->N;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
         const int b = rowptr[r], n = ccnt[r];
         for (int e = 0; e < n; e++) {
             const int pos = atomicAdd(&cursor[cidx[b + e]], 1);
-            colrow[pos] = r;
-            colval[pos] = (float)cval[b + e];
+            col_u[pos] = r;
+            src_u[pos] = b + e;
         }
+    }
+}
+
+// Each column's entries in increasing row order, so that every sum over a
+// column runs in a fixed order (k_csc_fill places them in atomic order): the
+// rank of an entry is the number of entries of its column with a smaller row
+// (rows are distinct within a column of the merged L).  One CTA per column.
+__global__ void __launch_bounds__(128) k_csc_sort(const GridState* __restrict__ gs, const int* __restrict__ colptr,
+                                                  const int* __restrict__ col_u, const int* __restrict__ src_u,
+                                                  const double* __restrict__ cval, int* __restrict__ colrow,
+                                                  float* __restrict__ colval, double* __restrict__ colval64)
+{
+    const int s = blockIdx.x;
+    if (s >= gs->M) return;
+    const int b = colptr[s], n = colptr[s + 1] - b;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int ri = col_u[b + i];
+        int rank = 0;
+        for (int j = 0; j < n; j++) rank += (col_u[b + j] < ri) ? 1 : 0;
+        const double v = cval[src_u[b + i]];
+        colrow[b + rank] = ri;
+        colval[b + rank] = (float)v;
+        colval64[b + rank] = v;
+    }
+}
+
+// out[s] = sum over column s of L of value * w[row]: one warp per column, lane
+// l takes entries l, l+32, ... in row order, then a fixed shuffle tree; zero
+// from M up to the 64-padding.
+__global__ void __launch_bounds__(256) k_LTw_csc(const GridState* __restrict__ gs, const int* __restrict__ colptr,
+                                                 const int* __restrict__ colrow,
+                                                 const double* __restrict__ colval64, const double* __restrict__ w,
+                                                 double* __restrict__ out)
+{
+    const int M = gs->M, Mp = (M + 63) & ~63;
+    const int lane = threadIdx.x & 31;
+    for (int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < Mp; s += gridDim.x * (blockDim.x >> 5)) {
+        double acc = 0;
+        if (s < M) {
+            const int b = colptr[s], e = colptr[s + 1];
+            for (int k = b + lane; k < e; k += 32) acc += colval64[k] * w[colrow[k]];
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) out[s] = acc;
     }
 }
 
@@ -343,7 +389,7 @@ void mixed_free(Slot& c)
     if (!m) return;
     void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
                     m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
-                    m->sqc};
+                    m->sqc, m->col_u, m->src_u, m->colval64};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
     c.mixed = nullptr;
@@ -375,6 +421,9 @@ int mixed_init(Slot& c)
     A((void**)&m->cursor, sizeof(int) * (size_t)M_cap);
     A((void**)&m->colrow, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->colval, sizeof(float) * (size_t)m->nnz_cap);
+    A((void**)&m->col_u, sizeof(int) * (size_t)m->nnz_cap);
+    A((void**)&m->src_u, sizeof(int) * (size_t)m->nnz_cap);
+    A((void**)&m->colval64, sizeof(double) * (size_t)m->nnz_cap);
     A((void**)&m->sqc, sizeof(float) * (size_t)(c.N_cap + 64));
     A((void**)&m->t, sizeof(double) * (size_t)(c.N_cap + 64));
     A((void**)&m->u, sizeof(double) * (size_t)(c.N_cap + 64));
@@ -382,7 +431,6 @@ int mixed_init(Slot& c)
     A((void**)&m->r, sizeof(double) * M_cap);
     A((void**)&m->z, sizeof(double) * M_cap);
     A((void**)&m->y, sizeof(double) * M_cap);
-    A((void**)&m->part, sizeof(double) * (size_t)M_cap * (ltw_chunks(c.N_cap) + 1));
     m->nb = M_cap / C2;
     A((void**)&m->linvF, sizeof(float) * (size_t)m->nb * 2 * C2 * C2);
     A((void**)&m->linv128, sizeof(float) * 2 * C2 * C2);
@@ -432,8 +480,8 @@ static int cholesky_mixed(float* A, int ld, int M_cap128, GridState* gs, int whi
     return n;
 }
 
-int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, cudaStream_t st,
-                        cudaEvent_t* ev)
+int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, int refine,
+                        cudaStream_t st, cudaEvent_t* ev)
 {
     int rc = mixed_init(slot);
     if (rc != QLP_OK) return rc;
@@ -443,18 +491,25 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
     const int Mc = slot.M_cap;
     int n = 0;
 
-    // D = L^T P^T (C^-1 d), FP64
-    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, st);
-    op_LTw(w, N_cap, m->M_cap, m->t, m->part, w.D, st);
-    // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
+    // L by source cell (CSC, rows ascending within a column)
     cudaMemsetAsync(m->nz, 0, (size_t)(m->M_cap / TC_TILE) * m->nkb_cap, st);
     cudaMemsetAsync(m->colcnt, 0, sizeof(int) * (size_t)(m->M_cap + 1), st);
+    const int ltw_blocks = (m->M_cap + 7) / 8;
     {
         const int rb = std::min((N_cap + 255) / 256, 152 * 8);
         k_csc_count<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, w.cvec, m->colcnt, m->sqc);
         k_csc_scan<<<1, 1024, 0, st>>>(w.gs, m->colcnt, m->cursor);
-        k_csc_fill<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.cval, w.ccnt, m->cursor, m->colrow,
-                                                    m->colval);
+        k_csc_fill<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, m->cursor, m->col_u, m->src_u);
+        k_csc_sort<<<m->M_cap, 128, 0, st>>>(w.gs, m->colcnt, m->col_u, m->src_u, w.cval, m->colrow, m->colval,
+                                            m->colval64);
+        n += 4;
+    }
+    // D = L^T P^T (C^-1 d), FP64
+    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, st);
+    k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, w.D);
+    n++;
+    // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
+    {
         // accumulator rows per CTA: all pixels if they fit beside the PSF in 227 KB
         const int nT = sd.pnx * sd.pny;
         const int fit = (int)(((227 * 1024 - sizeof(float) * (size_t)nT) / sizeof(long long)) & ~(size_t)31);
@@ -464,7 +519,7 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
         k_psf_x<<<dim3(m->M_cap, nchunk), 256, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
                                                             w.pixindex, m->sqc, chunk, m->X_hi, m->X_lo,
                                                             m->K_cap, m->nz, m->nkb_cap);
-        n += 4;
+        n++;
     }
     if (ev) cudaEventRecord(ev[3], st);
     {
@@ -494,10 +549,9 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
     k_logdet_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, w.out, 0);
     n++;
     if (so.regularization) cudaStreamWaitEvent(st, slot.side_join, 0);
-    // s = F^-1 D with two FP64 refinement sweeps
+    // s = F^-1 D with `refine` FP64 refinement sweeps
     k_copy_init<<<(Mc + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->r, w.s);
     n++;
-    const int refine = 2;
     for (int it = 0; it <= refine; it++) {
         cudaMemsetAsync(m->flags, 0, sizeof(int) * (size_t)2 * m->nb, st);
         k_trsv128_fwd<<<m->nb, 256, 0, st>>>(m->F32, m->ld32, m->linvF, w.gs, m->r, m->yf, m->flags);
@@ -509,7 +563,8 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
         op_Ls(w, N_cap, w.s, m->t, st);
         op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, st);
         op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, st);
-        op_LTw(w, N_cap, m->M_cap, m->t, m->part, m->v, st);
+        k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, m->v);
+        n++;
         k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, regp,
                                                                   so.regularization, w.s, m->r);
         n++;

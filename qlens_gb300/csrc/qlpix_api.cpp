@@ -197,6 +197,14 @@ int qlp_set_graphs(qlp_ctx* c, int on)
     return QLP_OK;
 }
 
+int qlp_set_refinement(qlp_ctx* c, int sweeps)
+{
+    if (!c || sweeps < 0 || sweeps > 4) return fail(QLP_ERR_ARG, "refinement sweeps must be 0..4");
+    c->refine = sweeps;
+    c->graph_gen++;     // the sweeps are part of the captured sequence
+    return QLP_OK;
+}
+
 int qlp_last_transfer_bytes(const qlp_ctx* c, long long* h2d, long long* d2h)
 {
     if (!c || !h2d || !d2h) return fail(QLP_ERR_ARG, "bad arguments");

@@ -78,6 +78,7 @@ struct qlp_ctx {
     qlpix::EvalParams* h_ep = nullptr;    // pinned, one per batch instance
     int h_ep_cap = 0;
     int use_graphs = 1;                   // batched evaluation replays captured graphs
+    int refine = 1;                       // FP64 refinement sweeps of the mixed path's amplitudes
     int nfw_mode = QLP_NFW_QUADRATURE;    // NFW deflection: quadrature or trained surrogate
     double nfw_threshold = 2e-5;          // surrogate error bound (arcsec) above which a ray falls back
     long long graph_gen = 1;              // bumped whenever captured graphs go stale
@@ -103,7 +104,8 @@ void set_error(const char* fmt, const char* a, int code);
 // mixed.cu
 int mixed_init(Slot& slot);
 void mixed_free(Slot& slot);
-int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, cudaStream_t st,
+int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, int refine,
+                        cudaStream_t st,
                         cudaEvent_t* ev);
 // surrogate.cu
 int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_report* rep);

@@ -60,6 +60,7 @@ def load_library(build_if_missing=False):
     L.qlp_last_launch_count.restype = C.c_longlong
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
     L.qlp_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_set_refinement.argtypes = [C.c_void_p, C.c_int]
     L.qlp_last_transfer_bytes.argtypes = [C.c_void_p, P(C.c_longlong), P(C.c_longlong)]
     L.qlp_spd_solve_logdet_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p]
@@ -177,6 +178,10 @@ class PixelLikelihood:
         """abi.QLP_NFW_QUADRATURE or abi.QLP_NFW_SURROGATE (after train_nfw_surrogate);
         threshold_arcsec <= 0 keeps the default gate (2e-5 arcsec)."""
         self._check(self.lib.qlp_set_nfw_mode(self.ctx, int(mode), float(threshold_arcsec)))
+
+    def set_refinement(self, sweeps):
+        """FP64 refinement sweeps of the mixed path (0..4, default 1)."""
+        self._check(self.lib.qlp_set_refinement(self.ctx, int(sweeps)))
 
     def last_transfer_bytes(self):
         """(host->device, device->host) bytes moved by the last call."""

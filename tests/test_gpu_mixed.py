@@ -61,3 +61,25 @@ def test_mixed_vs_fp64_random_draws():
         assert abs(ra["m2logev"] - rb["m2logev"]) < M2_TOL, (ra["m2logev"], rb["m2logev"])
     p64.close()
     pmx.close()
+
+
+@pytest.mark.parametrize("name", ["cfg1", "powerlaw"])
+def test_refinement_sweeps(name):
+    """-2 log(evidence) is stationary in the amplitudes at the solution, so it
+    settles after the first FP64 refinement sweep (the default); chisq0 alone
+    is first order in the amplitude error."""
+    from qlens_gb300 import QLP_MIXED
+    g = Golden(name)
+    pl = _ctx(g, QLP_MIXED)
+    res = {}
+    for k in (0, 1, 2):
+        pl.set_refinement(k)
+        res[k] = pl.invert_image_surface_brightness_map()
+        assert res[k]["status"] == 0 and res[k]["refine_iters"] == k
+    m2 = {k: res[k]["m2logev"] for k in res}
+    c2 = {k: res[k]["chisq0"] for k in res}
+    print("%s: -2logev %s chisq0 %s" % (name, m2, c2))
+    assert abs(m2[1] - m2[2]) <= 1e-8 * abs(m2[2])
+    assert abs(c2[1] - c2[2]) <= 1e-8 * abs(c2[2])
+    assert abs(m2[0] - m2[2]) <= 1e-2
+    pl.close()
