@@ -188,6 +188,8 @@ def main():
     ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch schedule instead of tuning it on a sample batch first")
     ap.add_argument("--nfw", default="surrogate", choices=["surrogate", "quadrature"],
                     help="NFW deflection: trained MLP surrogate (quadrature fallback) or quadrature only")
     args = ap.parse_args()
@@ -249,6 +251,19 @@ def main():
     def run_step(k):
         ids, sizes, lam = insts[k]
         return pl.eval_batch(pinned[k].numpy(), regparams=lam, mask_ids=ids, src_sizes=sizes)
+
+    # launch schedule: tuned on a sample of the first warm-up batch, before
+    # the timed region (every schedule gives the same results)
+    tune = None
+    if not args.no_autotune:
+        kk = min(B, 256)
+        ids, sizes, lam = insts[0]
+        t_tune = time.perf_counter()
+        rep = pl.autotune(batches[0][:kk], regparams=None if lam is None else lam[:kk],
+                          mask_ids=None if ids is None else ids[:kk], src_sizes=None if sizes is None else sizes[:kk],
+                          reps=2)
+        tune = {"sample": kk, "trials": rep["n_trials"], "start_ms": rep["start_ms"], "best_ms": rep["best_ms"],
+                "wall_s": time.perf_counter() - t_tune}
 
     for k in range(args.warmup):
         run_step(k)
@@ -337,7 +352,8 @@ def main():
             "dtype": "f32-tensor+f64" if precision == "mixed" else "f64",
             "data": "synthetic (seeded mock image; parameters drawn from the prior box)",
             "config": {**wl.describe(), "batch_per_step": B, "precision": precision,
-                       "slots": args.slots or min(B, 32),
+                       "schedule": pl.schedule(),
+                       "autotune": tune,
                        "uneven": ("per vector: one of %d masks (r 1.5-3.0\"), source side 20-64, "
                                   "log10 lambda 0-2" % len(wl.instance_masks)) if uneven else None,
                        "parallelism": "replicas" if world > 1 else "single",

@@ -189,6 +189,39 @@ int qlp_set_batch_slots(qlp_ctx* ctx, int slots);
  * reference (it has no device launches). */
 int qlp_set_graphs(qlp_ctx* ctx, int on);
 
+/* ---- launch schedule and its autotuner (no counterpart in the reference) ----
+ * The knobs of the batched path's launches.  None of them changes a result:
+ * every kernel sums in a fixed order whatever its CTA size or split, so all
+ * schedules give the same bits; they change only the time. */
+typedef struct {
+    int slots;          /* evaluations in flight in qlp_eval_batch, 1..64 (default 16) */
+    int ray_threads;    /* threads per CTA of the FP64 ray shooting: 64, 128 or 256 (default 256) */
+    int psfx_threads;   /* threads per CTA of the mixed path's PSF-to-X build: 128, 256 or 512 (default 256) */
+    int psfx_split;     /* image-row chunks per source cell in that build: 1, 2 or 4 (default 1) */
+} qlp_schedule;
+
+#define QLP_TUNE_MAX_TRIALS 32
+typedef struct {
+    qlp_schedule best;                          /* the schedule the context now uses */
+    double best_ms;                             /* device ms of the sample batch with it */
+    double start_ms;                            /* ... with the schedule the context had before */
+    int n_trials;
+    qlp_schedule trial[QLP_TUNE_MAX_TRIALS];    /* every schedule timed, in order */
+    double trial_ms[QLP_TUNE_MAX_TRIALS];
+} qlp_tune_report;
+
+int qlp_get_schedule(const qlp_ctx* ctx, qlp_schedule* out);
+int qlp_set_schedule(qlp_ctx* ctx, const qlp_schedule* sched);
+
+/* Time the sample batch (arguments as qlp_eval_batch; inst and lambdas may
+ * be NULL) under candidate schedules -- coordinate descent over the knobs
+ * above, each trial one warm-up batch (which also captures the graphs) and
+ * `reps` timed batches, the best device time kept -- and keep the fastest
+ * schedule in the context.  Fails with QLP_ERR_ARG if two schedules give
+ * different results for the sample (they must not).  rep may be NULL. */
+int qlp_autotune(qlp_ctx* ctx, const double* params, const double* lambdas, const qlp_instance* inst, int n,
+                 int reps, qlp_tune_report* rep);
+
 /* FP64 refinement sweeps of the mixed path's source amplitudes (0..4,
  * default 1): r = D - F s in FP64 with the sparse operators, s += F32^-1 r.
  * -2 log(evidence) is stationary in s at the solution, so its error is second

@@ -72,6 +72,26 @@ class qlp_result(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class qlp_schedule(C.Structure):
+    _fields_ = [("slots", C.c_int), ("ray_threads", C.c_int), ("psfx_threads", C.c_int), ("psfx_split", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+QLP_TUNE_MAX_TRIALS = 32
+
+
+class qlp_tune_report(C.Structure):
+    _fields_ = [("best", qlp_schedule), ("best_ms", C.c_double), ("start_ms", C.c_double), ("n_trials", C.c_int),
+                ("trial", qlp_schedule * QLP_TUNE_MAX_TRIALS), ("trial_ms", C.c_double * QLP_TUNE_MAX_TRIALS)]
+
+    def as_dict(self):
+        n = self.n_trials
+        return {"best": self.best.as_dict(), "best_ms": self.best_ms, "start_ms": self.start_ms, "n_trials": n,
+                "trials": [dict(self.trial[i].as_dict(), ms=self.trial_ms[i]) for i in range(n)]}
+
+
 class qlp_surrogate_opts(C.Structure):
     _fields_ = [("n_train", C.c_int), ("batch", C.c_int), ("steps", C.c_int), ("lr", C.c_double),
                 ("seed", C.c_ulonglong)]

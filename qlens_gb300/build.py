@@ -32,6 +32,7 @@ UNITS = [
     ("mixed.cu", []),
     ("surrogate.cu", ["--fmad=false"]),
     ("ctx.cpp", []),
+    ("autotune.cpp", []),
     ("qlpix_api.cpp", []),
 ]
 HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_common.cuh", "tc_syrk.cuh"]

@@ -281,7 +281,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
         int r = launch_raytrace_sur(sd, w, c->nfw_threshold, defer, st);
         if (r != QLP_OK) return r;
     } else {
-        launch_raytrace(sd, model_has_nfw(c), w, st);
+        launch_raytrace(sd, model_has_nfw(c), w, c->ray_threads, st);
     }
     if (ev) cudaEventRecord(ev[1], st);
     launch_grid(sd, so, w, st);
@@ -293,7 +293,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     launch_dvec(sd, w, N_max, st);
     const bool mixed = (c->precision == QLP_MIXED);
     if (mixed) {
-        int r = run_inversion_mixed(slot, sd, so, regp, c->refine, st, ev);
+        int r = run_inversion_mixed(c, slot, sd, so, regp, st, ev);
         if (r != QLP_OK) return r;
     } else {
         int r = ensure_fp64_mats(slot);
@@ -455,6 +455,14 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     fill_result(c->h_out[0], out);
     if (c->precision == QLP_MIXED) out->refine_iters = c->refine;
     return out->status;
+}
+
+// Free the workspaces of slots keep, keep+1, ... (slot 0 always stays).
+void ctx_trim_slots(qlp_ctx* c, int keep)
+{
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (int k = std::max(keep, 1); k < (int)c->slots.size(); k++) free_slot(c->slots[k]);
 }
 
 int ctx_set_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)

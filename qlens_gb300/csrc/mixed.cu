@@ -36,7 +36,6 @@ struct MixedWork {
     int* col_u = nullptr;    // nnz_cap: rows of each column in atomic (fill) order
     int* src_u = nullptr;    // nnz_cap: their positions in the merged CSR rows
     double* colval64 = nullptr; // nnz_cap: FP64 values, rows ascending within a column
-    int chunk = 0;           // image rows per k_psf_x accumulator
     float* X_hi = nullptr;
     float* X_lo = nullptr;
     int K_cap = 0;           // columns of X (image pixels), multiple of 32
@@ -218,7 +217,7 @@ __global__ void __launch_bounds__(256) k_LTw_csc(const GridState* __restrict__ g
 }
 
 // grid (M_cap cells, image-row chunks); chunk rows of 64-bit accumulators
-__global__ void __launch_bounds__(256) k_psf_x(StaticData sd, const GridState* __restrict__ gs,
+__global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
                                                const int* __restrict__ pixindex, const float* __restrict__ sqc,
@@ -416,7 +415,6 @@ int mixed_init(Slot& c)
     A((void**)&m->F32, sizeof(float) * (size_t)M_cap * M_cap);
     A((void**)&m->R32, sizeof(float) * (size_t)M_cap * M_cap);
     m->nnz_cap = 3 * c.N_cap * c.nsub_cap;
-    m->chunk = std::min(K_cap, 24576);
     A((void**)&m->colcnt, sizeof(int) * (size_t)(M_cap + 1));
     A((void**)&m->cursor, sizeof(int) * (size_t)M_cap);
     A((void**)&m->colrow, sizeof(int) * (size_t)m->nnz_cap);
@@ -480,9 +478,10 @@ static int cholesky_mixed(float* A, int ld, int M_cap128, GridState* gs, int whi
     return n;
 }
 
-int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, int refine,
+int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp,
                         cudaStream_t st, cudaEvent_t* ev)
 {
+    const int refine = c->refine;
     int rc = mixed_init(slot);
     if (rc != QLP_OK) return rc;
     MixedWork* m = mw_of(slot);
@@ -510,13 +509,17 @@ int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, con
     n++;
     // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
     {
-        // accumulator rows per CTA: all pixels if they fit beside the PSF in 227 KB
+        // accumulator rows per CTA: the pixels split into psfx_split chunks (or
+        // more, if a chunk does not fit beside the PSF in 227 KB)
         const int nT = sd.pnx * sd.pny;
         const int fit = (int)(((227 * 1024 - sizeof(float) * (size_t)nT) / sizeof(long long)) & ~(size_t)31);
-        const int chunk = std::max(32, std::min(m->chunk, fit));
+        const int split = std::max(1, std::min(c->psfx_split, 4));
+        const int want = ((m->K_cap + split - 1) / split + 31) & ~31;
+        const int chunk = std::max(32, std::min(want, fit));
         const int nchunk = (m->K_cap + chunk - 1) / chunk;
         const size_t smem = sizeof(long long) * (size_t)chunk + sizeof(float) * (size_t)nT;
-        k_psf_x<<<dim3(m->M_cap, nchunk), 256, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
+        const int pt = (c->psfx_threads == 128 || c->psfx_threads == 512) ? c->psfx_threads : 256;
+        k_psf_x<<<dim3(m->M_cap, nchunk), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
                                                             w.pixindex, m->sqc, chunk, m->X_hi, m->X_lo,
                                                             m->K_cap, m->nz, m->nkb_cap);
         n++;

@@ -197,6 +197,26 @@ int qlp_set_graphs(qlp_ctx* c, int on)
     return QLP_OK;
 }
 
+int qlp_get_schedule(const qlp_ctx* c, qlp_schedule* out)
+{
+    if (!c || !out) return fail(QLP_ERR_ARG, "null argument");
+    return ctx_get_schedule(c, out);
+}
+
+int qlp_set_schedule(qlp_ctx* c, const qlp_schedule* s)
+{
+    if (!c || !s) return fail(QLP_ERR_ARG, "null argument");
+    if (ctx_set_schedule(c, s) != QLP_OK) return fail(QLP_ERR_ARG, "schedule value outside its candidate set");
+    return QLP_OK;
+}
+
+int qlp_autotune(qlp_ctx* c, const double* params, const double* lambdas, const qlp_instance* inst, int n, int reps,
+                 qlp_tune_report* rep)
+{
+    if (!c || !params) return fail(QLP_ERR_ARG, "null argument");
+    return ctx_autotune(c, params, lambdas, inst, n, reps, rep);
+}
+
 int qlp_set_refinement(qlp_ctx* c, int sweeps)
 {
     if (!c || sweeps < 0 || sweeps > 4) return fail(QLP_ERR_ARG, "refinement sweeps must be 0..4");

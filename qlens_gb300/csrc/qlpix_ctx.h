@@ -43,7 +43,10 @@ struct qlp_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int precision = QLP_FP64;
-    int max_slots = 16;
+    int max_slots = 16;                   // schedule: evaluations in flight
+    int ray_threads = 256;                // schedule: ray-shooting CTA size
+    int psfx_threads = 256;               // schedule: k_psf_x CTA size
+    int psfx_split = 1;                   // schedule: image-row chunks per source cell in k_psf_x
 
     // lens model
     std::vector<qlp_lens> lenses;
@@ -104,9 +107,15 @@ void set_error(const char* fmt, const char* a, int code);
 // mixed.cu
 int mixed_init(Slot& slot);
 void mixed_free(Slot& slot);
-int run_inversion_mixed(Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp, int refine,
+int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp,
                         cudaStream_t st,
                         cudaEvent_t* ev);
+// autotune.cpp
+int ctx_get_schedule(const qlp_ctx* c, qlp_schedule* out);
+int ctx_set_schedule(qlp_ctx* c, const qlp_schedule* s);
+int ctx_autotune(qlp_ctx* c, const double* params, const double* lambdas, const qlp_instance* inst, int n, int reps,
+                 qlp_tune_report* rep);
+void ctx_trim_slots(qlp_ctx* c, int keep);
 // surrogate.cu
 int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_report* rep);
 bool surrogate_ready(int device);

@@ -162,7 +162,7 @@ inline const double* regparam_dev(const Work& w)
 }
 
 // ---- kernels (launch wrappers implemented in the .cu files) ----
-void launch_raytrace(const StaticData& sd, bool nfw, Work& w, cudaStream_t st);
+void launch_raytrace(const StaticData& sd, bool nfw, Work& w, int threads, cudaStream_t st);
 void launch_grid(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_locate(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);
 void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st);

@@ -43,13 +43,15 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd_, const EvalPara
     }
 }
 
-// nfw: the model has an NFW lens (selects the kernel with the quadrature)
-void launch_raytrace(const StaticData& sd, bool nfw, Work& w, cudaStream_t st)
+// nfw: the model has an NFW lens (selects the kernel with the quadrature);
+// threads: CTA size (64, 128 or 256, from the context's schedule)
+void launch_raytrace(const StaticData& sd, bool nfw, Work& w, int threads, cudaStream_t st)
 {
     if (sd.n_sub == 0) return;
-    int blocks = (sd.n_sub + 255) / 256;
-    if (nfw) k_raytrace<true><<<blocks, 256, 0, st>>>(sd, w.ep, w.spx, w.spy);
-    else k_raytrace<false><<<blocks, 256, 0, st>>>(sd, w.ep, w.spx, w.spy);
+    if (threads != 64 && threads != 128) threads = 256;
+    const int blocks = (sd.n_sub + threads - 1) / threads;
+    if (nfw) k_raytrace<true><<<blocks, threads, 0, st>>>(sd, w.ep, w.spx, w.spy);
+    else k_raytrace<false><<<blocks, threads, 0, st>>>(sd, w.ep, w.spx, w.spy);
     count_launches(1);
 }
 

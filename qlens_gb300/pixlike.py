@@ -61,6 +61,10 @@ def load_library(build_if_missing=False):
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
     L.qlp_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_refinement.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_get_schedule.argtypes = [C.c_void_p, P(abi.qlp_schedule)]
+    L.qlp_set_schedule.argtypes = [C.c_void_p, P(abi.qlp_schedule)]
+    L.qlp_autotune.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(abi.qlp_instance), C.c_int, C.c_int,
+                               P(abi.qlp_tune_report)]
     L.qlp_last_transfer_bytes.argtypes = [C.c_void_p, P(C.c_longlong), P(C.c_longlong)]
     L.qlp_spd_solve_logdet_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p]
@@ -179,6 +183,44 @@ class PixelLikelihood:
         threshold_arcsec <= 0 keeps the default gate (2e-5 arcsec)."""
         self._check(self.lib.qlp_set_nfw_mode(self.ctx, int(mode), float(threshold_arcsec)))
 
+    def schedule(self):
+        s = abi.qlp_schedule()
+        self._check(self.lib.qlp_get_schedule(self.ctx, C.byref(s)))
+        return s.as_dict()
+
+    def set_schedule(self, **kw):
+        s = abi.qlp_schedule()
+        self._check(self.lib.qlp_get_schedule(self.ctx, C.byref(s)))
+        for k, v in kw.items():
+            setattr(s, k, int(v))
+        self._check(self.lib.qlp_set_schedule(self.ctx, C.byref(s)))
+
+    def autotune(self, params, regparams=None, mask_ids=None, src_sizes=None, reps=2):
+        """Time the sample batch under candidate launch schedules and keep the
+        fastest (qlp_autotune); returns the report as a dict."""
+        params = np.ascontiguousarray(params, dtype=np.float64)
+        n = params.shape[0]
+        rp = None
+        if regparams is not None:
+            rpa = np.ascontiguousarray(regparams, dtype=np.float64)
+            rp = _dp(rpa)
+        inst = self._instances(n, mask_ids, src_sizes)
+        rep = abi.qlp_tune_report()
+        self._check(self.lib.qlp_autotune(self.ctx, _dp(params), rp, inst, n, int(reps), C.byref(rep)))
+        return rep.as_dict()
+
+    def _instances(self, n, mask_ids, src_sizes):
+        if mask_ids is None and src_sizes is None:
+            return None
+        inst = (abi.qlp_instance * n)()
+        for i in range(n):
+            inst[i].mask_id = -1 if mask_ids is None else int(mask_ids[i])
+            if src_sizes is None:
+                inst[i].src_npixels_x = inst[i].src_npixels_y = 0
+            else:
+                inst[i].src_npixels_x, inst[i].src_npixels_y = map(int, src_sizes[i])
+        return inst
+
     def set_refinement(self, sweeps):
         """FP64 refinement sweeps of the mixed path (0..4, default 1)."""
         self._check(self.lib.qlp_set_refinement(self.ctx, int(sweeps)))
@@ -223,15 +265,7 @@ class PixelLikelihood:
         if regparams is not None:
             self._rp = np.ascontiguousarray(regparams, dtype=np.float64)
             rp = _dp(self._rp)
-        inst = None
-        if mask_ids is not None or src_sizes is not None:
-            inst = (abi.qlp_instance * n)()
-            for i in range(n):
-                inst[i].mask_id = -1 if mask_ids is None else int(mask_ids[i])
-                if src_sizes is None:
-                    inst[i].src_npixels_x = inst[i].src_npixels_y = 0
-                else:
-                    inst[i].src_npixels_x, inst[i].src_npixels_y = map(int, src_sizes[i])
+        inst = self._instances(n, mask_ids, src_sizes)
         code = self.lib.qlp_eval_batch(self.ctx, _dp(params), rp, inst, n, out)
         if code not in (abi.QLP_OK, abi.QLP_ERR_NOT_SPD, abi.QLP_ERR_NO_SOURCE_PIXELS, abi.QLP_ERR_GRID_TOO_SMALL):
             self._check(code)
