@@ -33,6 +33,7 @@ struct MixedWork {
     float* colval = nullptr; // nnz_cap
     float* sqc = nullptr;    // N_cap: sqrt(C^-1) per active row
     int nnz_cap = 0;
+    int2* pixT = nullptr;    // image pixels, x fastest: (active row or -1, sqrt(C^-1))
     int* col_u = nullptr;    // nnz_cap: rows of each column in atomic (fill) order
     int* src_u = nullptr;    // nnz_cap: their positions in the merged CSR rows
     double* colval64 = nullptr; // nnz_cap: FP64 values, rows ascending within a column
@@ -116,16 +117,23 @@ __device__ __forceinline__ float to_tf32(float f)
     return __uint_as_float(u);
 }
 
-// column counts of the merged pre-PSF L and sqrt(C^-1) per active row
-__global__ void k_csc_count(const GridState* __restrict__ gs, const int* __restrict__ rowptr,
+// column counts of the merged pre-PSF L, sqrt(C^-1) per active row, and the
+// image pixel -> (active row, sqrt(C^-1)) table in x-fastest order that
+// k_psf_x reads (pixT[j * nx + i]; rows of inactive pixels stay -1)
+__global__ void k_csc_count(StaticData sd, const GridState* __restrict__ gs, const int* __restrict__ rowptr,
                             const int* __restrict__ cidx, const int* __restrict__ ccnt,
-                            const double* __restrict__ cvec, int* __restrict__ colcnt, float* __restrict__ sqc)
+                            const double* __restrict__ cvec, const int* __restrict__ rowpix,
+                            int* __restrict__ colcnt, float* __restrict__ sqc, int2* __restrict__ pixT)
 {
     const int N = gs->N;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
         const int b = rowptr[r], n = ccnt[r];
         for (int e = 0; e < n; e++) atomicAdd(&colcnt[cidx[b + e]], 1);
-        sqc[r] = sqrtf((float)cvec[r]);
+        const float sq = sqrtf((float)cvec[r]);
+        sqc[r] = sq;
+        const int pix = rowpix[r];
+        const int i = pix / sd.ny, j = pix - i * sd.ny;
+        pixT[(size_t)j * sd.nx + i] = make_int2(r, __float_as_int(sq));
     }
 }
 
@@ -220,9 +228,9 @@ __global__ void __launch_bounds__(256) k_LTw_csc(const GridState* __restrict__ g
 __global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
-                                               const int* __restrict__ pixindex, const float* __restrict__ sqc,
-                                               int chunk, float* __restrict__ Xh, float* __restrict__ Xl,
-                                               int K_cap, unsigned char* __restrict__ nz, int nkb_cap)
+                                               const int2* __restrict__ pixT, int chunk, float* __restrict__ Xh,
+                                               float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
+                                               int nkb_cap)
 {
     extern __shared__ __align__(16) unsigned char psfx_smem[];
     long long* acc = reinterpret_cast<long long*>(psfx_smem);
@@ -235,27 +243,41 @@ __global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* _
     if (s >= Mp || r0 >= Np) return;
     const int nT = sd.pnx * sd.pny;
     const float scale = ldexpf(1.0f, sd.fix_exp), inv = ldexpf(1.0f, -sd.fix_exp);
+    const int pnx = sd.pnx, pny = sd.pny;
     for (int i = threadIdx.x; i < r1 - r0; i += blockDim.x) acc[i] = 0;
-    for (int t = threadIdx.x; t < nT; t += blockDim.x) tpsf[t] = (float)sd.psf[t];
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl]
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        const int pl = t / pnx, pk = t - pl * pnx;
+        tpsf[t] = (float)sd.psf[pk * pny + pl];
+    }
     __syncthreads();
     if (s < M) {
         const int b = colptr[s], n = colptr[s + 1] - b;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        const int nxh = sd.pnx / 2, nyh = sd.pny / 2;
+        const int nxh = pnx / 2, nyh = pny / 2;
+        const int l0 = lane / pnx, k0 = lane - l0 * pnx;     // this lane's first tap
+        const int dl = 32 / pnx, dk = 32 - dl * pnx;         // and the step to its next
         for (int e = warp; e < n; e += nw) {
             const int q = colrow[b + e];
             const float v = colval[b + e];
             const int pix = rowpix[q];
             const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
+            // lanes run along x: their targets are consecutive active rows, so
+            // the 64-bit shared atomics of one instruction do not collide
+            int pk = k0, pl = l0;
             for (int t = lane; t < nT; t += 32) {
-                const int pk = t / sd.pny, pl = t - pk * sd.pny;
                 const int ii = iq - nxh + pk, jj = jq - nyh + pl;
-                if (ii < 0 || ii >= sd.nx || jj < 0 || jj >= sd.ny) continue;
-                const int r = pixindex[ii * sd.ny + jj];
-                if (r < r0 || r >= r1) continue;            // inactive (-1) or another chunk
-                const float x = tpsf[t] * v * sqc[r];
-                atomicAdd(reinterpret_cast<unsigned long long*>(&acc[r - r0]),
-                          (unsigned long long)__float2ll_rn(x * scale));
+                if (ii >= 0 && ii < sd.nx && jj >= 0 && jj < sd.ny) {
+                    const int2 P = pixT[(size_t)jj * sd.nx + ii];
+                    if (P.x >= r0 && P.x < r1) {                    // inactive (-1) or another chunk
+                        const float x = tpsf[t] * v * __int_as_float(P.y);
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&acc[P.x - r0]),
+                                  (unsigned long long)__float2ll_rn(x * scale));
+                    }
+                }
+                pk += dk;
+                pl += dl;
+                if (pk >= pnx) { pk -= pnx; pl++; }
             }
         }
     }
@@ -388,7 +410,7 @@ void mixed_free(Slot& c)
     if (!m) return;
     void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
                     m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
-                    m->sqc, m->col_u, m->src_u, m->colval64};
+                    m->sqc, m->col_u, m->src_u, m->colval64, m->pixT};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
     c.mixed = nullptr;
@@ -420,6 +442,7 @@ int mixed_init(Slot& c)
     A((void**)&m->colrow, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->colval, sizeof(float) * (size_t)m->nnz_cap);
     A((void**)&m->col_u, sizeof(int) * (size_t)m->nnz_cap);
+    A((void**)&m->pixT, sizeof(int2) * (size_t)c.npix_img);
     A((void**)&m->src_u, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->colval64, sizeof(double) * (size_t)m->nnz_cap);
     A((void**)&m->sqc, sizeof(float) * (size_t)(c.N_cap + 64));
@@ -496,7 +519,9 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     const int ltw_blocks = (m->M_cap + 7) / 8;
     {
         const int rb = std::min((N_cap + 255) / 256, 152 * 8);
-        k_csc_count<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, w.cvec, m->colcnt, m->sqc);
+        cudaMemsetAsync(m->pixT, 0xff, sizeof(int2) * (size_t)slot.npix_img, st);
+        k_csc_count<<<std::max(rb, 1), 256, 0, st>>>(sd, w.gs, w.rowptr, w.cidx, w.ccnt, w.cvec, w.rowpix, m->colcnt,
+                                                     m->sqc, m->pixT);
         k_csc_scan<<<1, 1024, 0, st>>>(w.gs, m->colcnt, m->cursor);
         k_csc_fill<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, m->cursor, m->col_u, m->src_u);
         k_csc_sort<<<m->M_cap, 128, 0, st>>>(w.gs, m->colcnt, m->col_u, m->src_u, w.cval, m->colrow, m->colval,
@@ -520,8 +545,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         const size_t smem = sizeof(long long) * (size_t)chunk + sizeof(float) * (size_t)nT;
         const int pt = (c->psfx_threads == 128 || c->psfx_threads == 512) ? c->psfx_threads : 256;
         k_psf_x<<<dim3(m->M_cap, nchunk), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
-                                                            w.pixindex, m->sqc, chunk, m->X_hi, m->X_lo,
-                                                            m->K_cap, m->nz, m->nkb_cap);
+                                                            m->pixT, chunk, m->X_hi, m->X_lo, m->K_cap, m->nz,
+                                                            m->nkb_cap);
         n++;
     }
     if (ev) cudaEventRecord(ev[3], st);
