@@ -100,7 +100,7 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     CK(dalloc(&w.fb_ray, n_sub), "alloc"); CK(dalloc(&w.fb_xy, 2 * n_sub), "alloc"); CK(dalloc(&w.fb_count, 1), "alloc");
     s.M_cap = Mc;
     s.N_cap = n_mask;
-    s.npix_img = c->nx * c->ny;
+    s.npix_pad = (c->nx + 2 * (c->sd.pnx / 2)) * (c->ny + 2 * (c->sd.pny / 2));
     s.nsub_cap = nsub;
     s.snx_cap = snx_max;
     s.sny_cap = sny_max;

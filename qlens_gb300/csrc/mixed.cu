@@ -118,8 +118,10 @@ __device__ __forceinline__ float to_tf32(float f)
 }
 
 // column counts of the merged pre-PSF L, sqrt(C^-1) per active row, and the
-// image pixel -> (active row, sqrt(C^-1)) table in x-fastest order that
-// k_psf_x reads (pixT[j * nx + i]; rows of inactive pixels stay -1)
+// image pixel -> (active row, sqrt(C^-1)) table that k_psf_x reads: x fastest,
+// with a border of half a PSF on every side so that no tap needs a bounds
+// check (pixT[(j + pny/2) * (nx + 2 (pnx/2)) + i + pnx/2]; the rows of
+// inactive and border pixels stay -1)
 __global__ void k_csc_count(StaticData sd, const GridState* __restrict__ gs, const int* __restrict__ rowptr,
                             const int* __restrict__ cidx, const int* __restrict__ ccnt,
                             const double* __restrict__ cvec, const int* __restrict__ rowpix,
@@ -133,7 +135,8 @@ __global__ void k_csc_count(StaticData sd, const GridState* __restrict__ gs, con
         sqc[r] = sq;
         const int pix = rowpix[r];
         const int i = pix / sd.ny, j = pix - i * sd.ny;
-        pixT[(size_t)j * sd.nx + i] = make_int2(r, __float_as_int(sq));
+        const int nxp = sd.nx + 2 * (sd.pnx / 2);
+        pixT[(size_t)(j + sd.pny / 2) * nxp + i + sd.pnx / 2] = make_int2(r, __float_as_int(sq));
     }
 }
 
@@ -244,40 +247,53 @@ __global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* _
     const int nT = sd.pnx * sd.pny;
     const float scale = ldexpf(1.0f, sd.fix_exp), inv = ldexpf(1.0f, -sd.fix_exp);
     const int pnx = sd.pnx, pny = sd.pny;
+    const int nxp = sd.nx + 2 * (pnx / 2);                    // padded width of pixT
+    int* toff = reinterpret_cast<int*>(tpsf + nT);
     for (int i = threadIdx.x; i < r1 - r0; i += blockDim.x) acc[i] = 0;
-    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl]
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] scaled to the
+    // fixed-point grid (a power of two: exact, so x * scale keeps its bits), and
+    // the tap's offset in pixT from the footprint's corner
     for (int t = threadIdx.x; t < nT; t += blockDim.x) {
         const int pl = t / pnx, pk = t - pl * pnx;
-        tpsf[t] = (float)sd.psf[pk * pny + pl];
+        tpsf[t] = (float)sd.psf[pk * pny + pl] * scale;
+        toff[t] = pl * nxp + pk;
     }
     __syncthreads();
     if (s < M) {
         const int b = colptr[s], n = colptr[s + 1] - b;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        const int nxh = pnx / 2, nyh = pny / 2;
-        const int l0 = lane / pnx, k0 = lane - l0 * pnx;     // this lane's first tap
-        const int dl = 32 / pnx, dk = 32 - dl * pnx;         // and the step to its next
         for (int e = warp; e < n; e += nw) {
             const int q = colrow[b + e];
             const float v = colval[b + e];
             const int pix = rowpix[q];
             const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
-            // lanes run along x: their targets are consecutive active rows, so
-            // the 64-bit shared atomics of one instruction do not collide
-            int pk = k0, pl = l0;
-            for (int t = lane; t < nT; t += 32) {
-                const int ii = iq - nxh + pk, jj = jq - nyh + pl;
-                if (ii >= 0 && ii < sd.nx && jj >= 0 && jj < sd.ny) {
-                    const int2 P = pixT[(size_t)jj * sd.nx + ii];
-                    if (P.x >= r0 && P.x < r1) {                    // inactive (-1) or another chunk
-                        const float x = tpsf[t] * v * __int_as_float(P.y);
-                        atomicAdd(reinterpret_cast<unsigned long long*>(&acc[P.x - r0]),
-                                  (unsigned long long)__float2ll_rn(x * scale));
+            // the footprint's corner (iq - pnx/2, jq - pny/2) sits at (iq, jq) of
+            // the padded table; lanes run along x, so the targets of one
+            // instruction are consecutive active rows and its 64-bit shared
+            // atomics do not collide
+            const int2* corner = pixT + (size_t)jq * nxp + iq;
+            // four taps per lane in flight: their table loads are independent
+            for (int t0 = lane; t0 < nT; t0 += 128) {
+                int2 P[4];
+                float w[4];
+                #pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int t = t0 + 32 * u;
+                    P[u] = make_int2(-1, 0);
+                    w[u] = 0.0f;
+                    if (t < nT) {
+                        P[u] = corner[toff[t]];
+                        w[u] = tpsf[t];
                     }
                 }
-                pk += dk;
-                pl += dl;
-                if (pk >= pnx) { pk -= pnx; pl++; }
+                #pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (P[u].x >= r0 && P[u].x < r1) {              // inactive (-1) or another chunk
+                        const float x = w[u] * v * __int_as_float(P[u].y);
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&acc[P[u].x - r0]),
+                                  (unsigned long long)__float2ll_rn(x));
+                    }
+                }
             }
         }
     }
@@ -442,7 +458,7 @@ int mixed_init(Slot& c)
     A((void**)&m->colrow, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->colval, sizeof(float) * (size_t)m->nnz_cap);
     A((void**)&m->col_u, sizeof(int) * (size_t)m->nnz_cap);
-    A((void**)&m->pixT, sizeof(int2) * (size_t)c.npix_img);
+    A((void**)&m->pixT, sizeof(int2) * (size_t)c.npix_pad);
     A((void**)&m->src_u, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->colval64, sizeof(double) * (size_t)m->nnz_cap);
     A((void**)&m->sqc, sizeof(float) * (size_t)(c.N_cap + 64));
@@ -519,7 +535,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     const int ltw_blocks = (m->M_cap + 7) / 8;
     {
         const int rb = std::min((N_cap + 255) / 256, 152 * 8);
-        cudaMemsetAsync(m->pixT, 0xff, sizeof(int2) * (size_t)slot.npix_img, st);
+        cudaMemsetAsync(m->pixT, 0xff, sizeof(int2) * (size_t)slot.npix_pad, st);
         k_csc_count<<<std::max(rb, 1), 256, 0, st>>>(sd, w.gs, w.rowptr, w.cidx, w.ccnt, w.cvec, w.rowpix, m->colcnt,
                                                      m->sqc, m->pixT);
         k_csc_scan<<<1, 1024, 0, st>>>(w.gs, m->colcnt, m->cursor);
@@ -537,12 +553,13 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         // accumulator rows per CTA: the pixels split into psfx_split chunks (or
         // more, if a chunk does not fit beside the PSF in 227 KB)
         const int nT = sd.pnx * sd.pny;
-        const int fit = (int)(((227 * 1024 - sizeof(float) * (size_t)nT) / sizeof(long long)) & ~(size_t)31);
+        const int fit = (int)(((227 * 1024 - (sizeof(float) + sizeof(int)) * (size_t)nT) / sizeof(long long)) &
+                              ~(size_t)31);
         const int split = std::max(1, std::min(c->psfx_split, 4));
         const int want = ((m->K_cap + split - 1) / split + 31) & ~31;
         const int chunk = std::max(32, std::min(want, fit));
         const int nchunk = (m->K_cap + chunk - 1) / chunk;
-        const size_t smem = sizeof(long long) * (size_t)chunk + sizeof(float) * (size_t)nT;
+        const size_t smem = sizeof(long long) * (size_t)chunk + (sizeof(float) + sizeof(int)) * (size_t)nT;
         const int pt = (c->psfx_threads == 128 || c->psfx_threads == 512) ? c->psfx_threads : 256;
         k_psf_x<<<dim3(m->M_cap, nchunk), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
                                                             m->pixT, chunk, m->X_hi, m->X_lo, m->K_cap, m->nz,

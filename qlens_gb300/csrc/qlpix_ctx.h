@@ -22,7 +22,7 @@ struct Slot {
     int N_cap = 0;                  // capacity in masked pixels
     int nsub_cap = 0;
     int snx_cap = 0, sny_cap = 0;
-    int npix_img = 0;               // image pixels (nx * ny)
+    int npix_pad = 0;               // image pixels with a PSF-half-width border: (nx + 2 (pnx/2)) (ny + 2 (pny/2))
     bool fp64_mats = false;         // F and R in FP64 allocated
     cudaEvent_t done = nullptr;
     // second stream of the slot: R's factorisation runs beside F's
