@@ -119,6 +119,9 @@ typedef struct {
     int status;
     int refine_iters;     /* FP64 refinement sweeps used (mixed precision) */
     int nfw_fallbacks;    /* rays that took the NFW quadrature instead of the surrogate */
+    double regparam;      /* the regularisation parameter used (the optimised one with
+                             qlp_set_regparam_optimization on) */
+    int regopt_evals;     /* -2 log(evidence) evaluations of the lambda optimisation (0 = off) */
 } qlp_result;
 
 /* Training of the NFW deflection surrogate (qlp_nfw_surrogate_train). */
@@ -221,6 +224,27 @@ int qlp_set_schedule(qlp_ctx* ctx, const qlp_schedule* sched);
  * different results for the sample (they must not).  rep may be NULL. */
 int qlp_autotune(qlp_ctx* ctx, const double* params, const double* lambdas, const qlp_instance* inst, int n,
                  int reps, qlp_tune_report* rep);
+
+/* ---- regularisation-parameter optimisation ----
+ * QLens's 'optimize_regparam on' (QLens::optimize_regularization_parameter,
+ * pixelgrid.cpp:15865-15890): qlp_eval and qlp_eval_batch choose lambda per
+ * evaluation by Brent's method over log10(lambda) in [minlog, maxlog]
+ * (tolerance tol on log10(lambda), at most max_iter iterations; QLens's
+ * defaults -3, 5, 0.01, 20), minimising chi^2 over the active pixels + the
+ * regularisation terms + log det F (QLens::chisq_regparam_dense,
+ * pixelgrid.cpp:16526-16700), and return the evaluation at the best lambda
+ * (qlp_result.regparam, .regopt_evals).  L, L^T C^-1 L and R are built once
+ * per evaluation; each trial factors F = L^T C^-1 L + lambda R.  Batched
+ * evaluations advance their minimisations in lockstep, one trial per slot per
+ * round.  on = 0 restores the fixed lambda.  Ignored without regularisation. */
+int qlp_set_regparam_optimization(qlp_ctx* ctx, int on, double minlog, double maxlog, double tol, int max_iter);
+
+/* Brent's minimiser that the optimisation uses (the steps of
+ * QLens::brents_min_method, pixelgrid.cpp:16849-16932) on a host function:
+ * *xmin = the point with the least value, *evals = evaluations.  Exposed to
+ * test it against the reference's algorithm. */
+int qlp_brent_min(double (*f)(double x, void* user), void* user, double ax, double bx, double tol, int max_iter,
+                  double* xmin, int* evals);
 
 /* FP64 refinement sweeps of the mixed path's source amplitudes (0..4,
  * default 1): r = D - F s in FP64 with the sparse operators, s += F32^-1 r.

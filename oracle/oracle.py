@@ -36,6 +36,7 @@ def build(force=False):
 
 
 _lib = None
+BRENT_FN = C.CFUNCTYPE(C.c_double, C.c_double, C.c_void_p)
 
 
 def lib():
@@ -50,6 +51,10 @@ def lib():
         _lib.oracle_get.restype = C.c_long
         _lib.oracle_get.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
         _lib.oracle_threads.restype = C.c_int
+        _lib.oracle_set_regopt.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
+        _lib.oracle_brent_min.restype = C.c_double
+        _lib.oracle_brent_min.argtypes = [BRENT_FN, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int,
+                                          C.POINTER(C.c_int)]
         _lib.oracle_mlp_n_params.restype = C.c_int
         _lib.oracle_mlp_loss_grad.restype = C.c_double
         _lib.oracle_mlp_loss_grad.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double),
@@ -74,9 +79,14 @@ def get(name):
     return out
 
 
-def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.0, planes=None):
-    """Run the oracle; returns the qlp_result as a dict."""
+def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.0, planes=None, regopt=None):
+    """Run the oracle; returns the qlp_result as a dict.  regopt: None, or
+    (minlog, maxlog, tol, max_iter) for QLens's 'optimize_regparam on'."""
     L = lib()
+    if regopt is None:
+        L.oracle_set_regopt(0, -3.0, 5.0, 0.01, 20)
+    else:
+        L.oracle_set_regopt(1, *map(float, regopt[:3]), int(regopt[3]))
     lenses = abi.make_lenses(lens_spec)
     pl = planes if planes is not None else abi.make_planes()
     res = abi.qlp_result()
@@ -106,3 +116,19 @@ def mlp_loss_grad(params, x, t):
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     loss = L.oracle_mlp_loss_grad(dp(p), x.shape[0], dp(x), dp(t), dp(g), dp(y))
     return loss, g, y
+
+
+def brent_min(f, ax, bx, tol, maxit):
+    """QLens's Brent minimiser (oracle_brent_min) on a Python function of one
+    variable; returns (x_min, evaluations, list of the points evaluated)."""
+    L = lib()
+    pts = []
+
+    def cb(x, _):
+        pts.append(x)
+        return float(f(x))
+
+    fn = BRENT_FN(cb)
+    n = C.c_int(0)
+    x = L.oracle_brent_min(fn, None, ax, bx, tol, maxit, C.byref(n))
+    return x, n.value, pts

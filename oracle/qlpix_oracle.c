@@ -309,6 +309,79 @@ static double cholesky_logdet_packed_lower(const double* a, int n)
 }
 
 /* repack_matrix_lower (pixelgrid.cpp:17300-17321): packed upper (row-major) -> packed lower (row-major) */
+/* ---------------------------------------------------------------------------
+ * Brent's method for a minimum: QLens::brents_min_method (pixelgrid.cpp:
+ * 16849-16932), restated step for step (same start point, tolerances, step
+ * choices and bracket updates).  Returns the point with the least value;
+ * *nevals counts the function evaluations.
+ * ------------------------------------------------------------------------- */
+double oracle_brent_min(double (*f)(double, void*), void* user, double ax, double bx, double tol, int maxit,
+                        int* nevals)
+{
+    const double CGOLD = 0.3819660, ZEPS = 1.0e-10, ROOTPREC = 1.0e-8;
+    double a = ax, b = bx, xstep = 0.0, e = 0.0;
+    double x, w, wprev, fx, fw, fwprev, u, fu, tol1, tol2, xmid;
+    int n = 0;
+    x = w = wprev = bx - CGOLD * (bx - ax);
+    fw = fwprev = fx = f(x, user);
+    n++;
+    for (int iter = 0; iter < maxit; iter++) {
+        xmid = 0.5 * (a + b);
+        tol1 = tol * fabs(x);
+        tol2 = 2.0 * (tol1 + ZEPS);
+        if (fabs(x - xmid) <= (tol2 - 0.5 * (b - a))) break;
+        if ((w != wprev) && (fabs(e) > tol1)) {
+            double r = (x - w) * (fx - fwprev);
+            double q = (x - wprev) * (fx - fw);
+            double p = (x - wprev) * q - (x - w) * r;
+            q = 2.0 * (q - r);
+            if (q > 0.0) p = -p;
+            q = fabs(q);
+            double etemp = e;
+            e = xstep;
+            if ((fabs(p) >= fabs(0.5 * q * etemp)) || (p <= q * (a - x)) || (p >= q * (b - x))) {
+                e = (x >= xmid) ? a - x : b - x;
+                xstep = CGOLD * e;
+            } else {
+                xstep = p / q;
+                u = x + xstep;
+                if ((u - a < tol2) || (b - u < tol2))
+                    xstep = ((xmid - x) >= 0 ? (tol1 >= 0 ? tol1 : -tol1) : (tol1 >= 0 ? -tol1 : tol1));
+            }
+        } else {
+            e = (x >= xmid) ? a - x : b - x;
+            xstep = CGOLD * e;
+        }
+        if (fabs(xstep) >= ROOTPREC) u = x + xstep;
+        else u = x + (xstep >= 0 ? ROOTPREC : -ROOTPREC);
+        fu = f(u, user);
+        n++;
+        if (fu <= fx) {
+            if (u >= x) a = x; else b = x;
+            wprev = w; w = x; x = u;
+            fwprev = fw; fw = fx; fx = fu;
+        } else {
+            if (u < x) a = u; else b = u;
+            if (fu <= fw || w == x) {
+                wprev = w; fwprev = fw;
+                w = u; fw = fu;
+            } else if ((fu <= fwprev) || (wprev == x) || (wprev == w)) {
+                wprev = u; fwprev = fu;
+            }
+        }
+    }
+    if (nevals) *nevals = n;
+    return x;
+}
+
+/* 'optimize_regparam on' settings (lens.cpp:421-425 defaults) */
+static struct { int on; double minlog, maxlog, tol; int maxit; } g_regopt = {0, -3.0, 5.0, 0.01, 20};
+
+void oracle_set_regopt(int on, double minlog, double maxlog, double tol, int maxit)
+{
+    g_regopt.on = on; g_regopt.minlog = minlog; g_regopt.maxlog = maxlog; g_regopt.tol = tol; g_regopt.maxit = maxit;
+}
+
 static void repack_lower(const double* up, double* lo, int n)
 {
     long k = 0;
@@ -320,6 +393,53 @@ static void repack_lower(const double* up, double* lo, int n)
             k++;
         }
     }
+}
+
+/* -2 log(evidence) as a function of log10(lambda) for fixed L and R:
+ * QLens::chisq_regparam_dense (pixelgrid.cpp:16526-16700), the packed branch:
+ * F = F0 + lambda R, Cholesky, solve, log det, the model over the active
+ * pixels, Ed = sum (model - d)^2 C^-1 over them (the reference sums it with an
+ * OpenMP reduction; here in pixel order), and the regularisation prior term. */
+struct regopt_ctx {
+    const double *F0, *Rp, *D, *Lp, *dvec, *cvec;
+    int M, npix;
+    long ntot;
+    double logdetR;
+};
+
+static double regopt_objective(double logreg, void* user)
+{
+    const struct regopt_ctx* c = (const struct regopt_ctx*)user;
+    const int M = c->M;
+    const double lam = pow(10, logreg);
+    double* Fc = (double*)malloc(sizeof(double) * c->ntot);
+    double* Fl = (double*)malloc(sizeof(double) * c->ntot);
+    double* s = (double*)malloc(sizeof(double) * M);
+    for (long e = 0; e < c->ntot; e++) Fc[e] = c->F0[e] + lam * c->Rp[e];
+    repack_lower(Fc, Fl, M);
+    cholesky_packed_lower(Fl, M);
+    cholesky_solve_packed_lower(Fl, c->D, s, M);
+    const double logdet = cholesky_logdet_packed_lower(Fl, M);
+    double Ed = 0;
+    for (int r = 0; r < c->npix; r++) {
+        double m = 0;
+        for (int j = 0; j < M; j++) m += c->Lp[(size_t)r * M + j] * s[j];
+        const double dd = m - c->dvec[r];
+        Ed += dd * dd * c->cvec[r];
+    }
+    double Es = 0;
+    for (int i = 0; i < M; i++) {
+        long rs = (long)i * M - (long)i * (i - 1) / 2;
+        Es += c->Rp[rs] * (s[i] * s[i]);
+        for (int j = i + 1; j < M; j++) {
+            double rv = c->Rp[rs + (j - i)];
+            if (rv != 0) Es += 2 * s[i] * rv * s[j];
+        }
+    }
+    double chisq = Ed + (lam * Es - M * log(lam) - c->logdetR);
+    chisq += logdet;
+    free(Fc); free(Fl); free(s);
+    return chisq;
 }
 
 /* ------------------------------------------------------------------ */
@@ -636,6 +756,18 @@ int oracle_eval(const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts*
             logdetR = cholesky_logdet_packed_lower(Rl, M);
             free(Rl);
         }
+        /* optimize_regparam: lambda = 10^x with x from Brent's method over the
+           objective above (optimize_regularization_parameter, pixelgrid.cpp:
+           15865-15890); the inversion below then runs at that lambda, which
+           reproduces the best trial's amplitudes and log det F */
+        if (g_regopt.on && M > 0 && out->status == 0) {
+            struct regopt_ctx rc = {Fp, Rp, D, Lp, dvec, cvec, M, npix, ntot, logdetR};
+            int nev = 0;
+            const double x = oracle_brent_min(regopt_objective, &rc, g_regopt.minlog, g_regopt.maxlog, g_regopt.tol,
+                                              g_regopt.maxit, &nev);
+            regparam = pow(10, x);
+            out->regopt_evals = nev;
+        }
         /* add_regularization_term_to_dense_Fmatrix (pixelgrid.cpp:15781-15819) */
         for (long e = 0; e < ntot; e++) Fp[e] += regparam * Rp[e];
     }
@@ -701,6 +833,7 @@ int oracle_eval(const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts*
     out->Es_times_two = Es;
     out->regterms = regterms;
     out->m2logev = loglike;
+    out->regparam = regparam;
     g_last.D = D; g_last.s = s; g_last.model = model;
 
     free(mpix); free(cx); free(cy); free(ccx); free(ccy); free(cell3); free(mapped); free(pixmaps);

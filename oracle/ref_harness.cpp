@@ -124,6 +124,14 @@ int main(int argc, char** argv)
 	double m2logev_entry = lens.invert_surface_brightness_map_from_data(chisq0_entry, false, true);
 	const double logdetF_entry = lens.Fmatrix_log_determinant;
 	const double logdetR_entry = lens.Rmatrix_log_determinant;
+	// With 'optimize_regparam on' the entry point has just chosen lambda by
+	// Brent's method (QLens::optimize_regularization_parameter,
+	// pixelgrid.cpp:15865) and left it in the source grid's regparam.  The
+	// step-by-step pass below then runs the plain inversion at that lambda
+	// (create_lensing_matrices_from_Lmatrix_dense adds lambda R only when the
+	// optimisation is off, pixelgrid.cpp:15719).
+	const int regopt = lens.optimize_regparam ? 1 : 0;
+	lens.optimize_regparam = false;
 
 	// ---------- 2. the Cartesian branch, step by step ----------
 	ImagePixelGrid* g = lens.image_pixel_grids[0];
@@ -276,6 +284,7 @@ int main(int argc, char** argv)
 	sc << "logdetR_steps " << logdetR_steps << "\n";
 	sc << "regterms " << regterms << "\n";
 	sc << "regparam " << regparam << "\n";
+	sc << "regopt " << regopt << "\n";
 	sc << "n_active_pixels " << npix << "\n";
 	sc << "n_active_src " << nsrc << "\n";
 	sc << "L_nnz " << nnz << "\n";

@@ -35,7 +35,7 @@ UNITS = [
     ("autotune.cpp", []),
     ("qlpix_api.cpp", []),
 ]
-HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_common.cuh", "tc_syrk.cuh"]
+HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_common.cuh", "tc_syrk.cuh", "brent.h"]
 
 
 def _newer(src, obj, deps):

@@ -7,6 +7,7 @@
 #include <vector>
 #include <algorithm>
 #include "qlpix_ctx.h"
+#include "brent.h"
 
 namespace qlpix {
 
@@ -46,7 +47,7 @@ static void free_work(Work& w)
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
                     w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep,
-                    w.fb_ray, w.fb_xy, w.fb_count};
+                    w.fb_ray, w.fb_xy, w.fb_count, w.F0};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
@@ -56,6 +57,9 @@ static void drop_graph(Slot& s)
     if (s.graph) cudaGraphExecDestroy(s.graph);
     s.graph = nullptr;
     s.graph_gen = 0;
+    if (s.graph_trial) cudaGraphExecDestroy(s.graph_trial);
+    s.graph_trial = nullptr;
+    s.trial_gen = 0;
 }
 
 static void free_slot(Slot& s)
@@ -218,6 +222,7 @@ void ctx_free(qlp_ctx* c)
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);
     if (c->h_ep) cudaFreeHost(c->h_ep);
+    if (c->h_trial) cudaFreeHost(c->h_trial);
     for (int i = 0; i <= QLP_N_STAGES; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
@@ -259,9 +264,11 @@ static bool model_has_nfw(const qlp_ctx* c)
 // Everything that changes between evaluations (lens model, regularisation
 // parameter, mask and source-grid size) is read from the slot's EvalParams in
 // device memory, so one captured sequence serves every evaluation the slot
-// runs.  ev (QLP_N_STAGES+1 events, or null) brackets the stages.
+// runs.  ev (QLP_N_STAGES+1 events, or null) brackets the stages.  part:
+// PIPE_ALL the whole evaluation; PIPE_PRE / PIPE_TRIAL the lambda-independent
+// part and one lambda trial of the regularisation-parameter optimisation.
 static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const SrcOpts& so_in, cudaStream_t st,
-                        cudaEvent_t* ev)
+                        cudaEvent_t* ev, int part)
 {
     StaticData sd = sd_in;
     SrcOpts so = so_in;
@@ -270,6 +277,23 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     const int Mc = slot.M_cap;
     const int N_max = sd.n_mask;
     const double* regp = regparam_dev(w);
+    const bool mixed = (c->precision == QLP_MIXED);
+    if (part == PIPE_TRIAL) {
+        if (mixed) {
+            int r = run_inversion_mixed(c, slot, sd, so, regp, PIPE_TRIAL, st, nullptr);
+            if (r != QLP_OK) return r;
+        } else {
+            const size_t bytes = sizeof(double) * (size_t)w.ldF * Mc;
+            cudaMemsetAsync(&w.gs->not_spd_F, 0, sizeof(int), st);
+            cudaMemcpyAsync(w.F, w.F0, bytes, cudaMemcpyDeviceToDevice, st);
+            launch_regularization(so, w, Mc, regp, REG_F, st);
+            launch_cholesky_fp64(w.F, w.ldF, Mc, w.gs, 0, w.linv, st);
+            launch_logdet(w.F, w.ldF, Mc, w, 0, st);
+            launch_solve_fp64(w, Mc, st);
+        }
+        launch_model_chi2(sd, so, w, N_max, Mc, regp, st, mixed);
+        return QLP_OK;
+    }
     cudaMemsetAsync(w.out, 0, sizeof(EvalOut), st);
     if (ev) cudaEventRecord(ev[0], st);
     if (c->nfw_mode == QLP_NFW_SURROGATE && model_has_nfw(c)) {
@@ -292,10 +316,10 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     launch_rowpix(sd, w, st);
     if (ev) cudaEventRecord(ev[2], st);
     launch_dvec(sd, w, N_max, st);
-    const bool mixed = (c->precision == QLP_MIXED);
     if (mixed) {
-        int r = run_inversion_mixed(c, slot, sd, so, regp, st, ev);
+        int r = run_inversion_mixed(c, slot, sd, so, regp, part, st, ev);
         if (r != QLP_OK) return r;
+        if (part == PIPE_PRE) return QLP_OK;
     } else {
         int r = ensure_fp64_mats(slot);
         if (r != QLP_OK) return r;
@@ -304,11 +328,14 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
         if (ev) cudaEventRecord(ev[3], st);
         launch_syrk_fp64(sd, w, N_max, Mc, st);
         if (ev) cudaEventRecord(ev[4], st);
-        launch_regularization(so, w, Mc, regp, st);
+        if (part == PIPE_PRE)
+            cudaMemcpyAsync(w.F0, w.F, sizeof(double) * (size_t)w.ldF * Mc, cudaMemcpyDeviceToDevice, st);
+        launch_regularization(so, w, Mc, regp, part == PIPE_PRE ? REG_R : (REG_F | REG_R), st);
         if (so.regularization) {
             launch_cholesky_fp64(w.R, w.ldF, Mc, w.gs, 1, w.linv, st);
             launch_logdet(w.R, w.ldF, Mc, w, 1, st);
         }
+        if (part == PIPE_PRE) return QLP_OK;
         launch_cholesky_fp64(w.F, w.ldF, Mc, w.gs, 0, w.linv, st);
         launch_logdet(w.F, w.ldF, Mc, w, 0, st);
         launch_solve_fp64(w, Mc, st);
@@ -323,40 +350,50 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
 // a stream capture.
 static int prepare_slot(qlp_ctx* c, Slot& s)
 {
-    if (c->precision == QLP_MIXED) return mixed_init(s);
-    return ensure_fp64_mats(s);
+    const bool regopt = c->regopt && c->so.regularization;
+    if (c->precision == QLP_MIXED) return regopt ? mixed_ensure_f0(s) : mixed_init(s);
+    int r = ensure_fp64_mats(s);
+    if (r == QLP_OK && regopt && !s.w.F0) CK(dalloc(&s.w.F0, (size_t)s.M_cap * s.M_cap), "alloc F0");
+    return r;
 }
 
 // Capture the slot's launch sequence, sized for its capacity, as a graph.
-static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const int key[6])
+static int capture_graph(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const int key[7], int part)
 {
-    drop_graph(s);
+    const bool trial = (part == PIPE_TRIAL);
+    cudaGraphExec_t& slot_graph = trial ? s.graph_trial : s.graph;
+    if (slot_graph) cudaGraphExecDestroy(slot_graph);
+    slot_graph = nullptr;
     int r = prepare_slot(c, s);
     if (r != QLP_OK) return r;
     const long long l0 = kernel_launch_counter();
     CK(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal), "capture");
-    r = run_pipeline(c, s, sd, so, s.stream, nullptr);
+    r = run_pipeline(c, s, sd, so, s.stream, nullptr, part);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s.stream, &g);
     const long long n = kernel_launch_counter() - l0;
     count_launches((int)-n);            // nothing ran yet: replays count them
     if (r != QLP_OK) { if (g) cudaGraphDestroy(g); return r; }
     if (e != cudaSuccess || !g) return cuda_fail(e, "stream capture");
-    e = cudaGraphInstantiate(&s.graph, g, 0);
+    e = cudaGraphInstantiate(&slot_graph, g, 0);
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) { s.graph = nullptr; return cuda_fail(e, "graph instantiate"); }
-    for (int i = 0; i < 6; i++) s.graph_key[i] = key[i];
-    s.graph_gen = c->graph_gen;
-    s.graph_launches = n;
+    if (e != cudaSuccess) { slot_graph = nullptr; return cuda_fail(e, "graph instantiate"); }
+    for (int i = 0; i < 7; i++) (trial ? s.trial_key : s.graph_key)[i] = key[i];
+    (trial ? s.trial_gen : s.graph_gen) = c->graph_gen;
+    (trial ? s.trial_launches : s.graph_launches) = n;
     return QLP_OK;
 }
 
 // One evaluation on slot s: upload its parameters, run (replay or launch) the
 // sequence, copy its result to *h_dst -- all asynchronous on the slot stream.
 static int issue_eval(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& so, const EvalParams* h_ep,
-                      EvalOut* h_dst, cudaEvent_t* ev)
+                      EvalOut* h_dst, cudaEvent_t* ev, int part = PIPE_ALL)
 {
-    CK(cudaMemcpyAsync(s.w.ep, h_ep, sizeof(EvalParams), cudaMemcpyHostToDevice, s.stream), "h2d");
+    if (part == PIPE_TRIAL)      // a lambda trial changes lambda only
+        CK(cudaMemcpyAsync(&s.w.ep->regparam, &h_ep->regparam, sizeof(double), cudaMemcpyHostToDevice, s.stream),
+           "h2d");
+    else
+        CK(cudaMemcpyAsync(s.w.ep, h_ep, sizeof(EvalParams), cudaMemcpyHostToDevice, s.stream), "h2d");
     if (c->use_graphs && ev == nullptr) {
         // one graph per slot for every mask and source grid that fits its
         // capacity: the launches are sized for the capacity, the kernels read
@@ -367,22 +404,27 @@ static int issue_eval(qlp_ctx* c, Slot& s, const StaticData& sd, const SrcOpts& 
         SrcOpts soc = so;
         soc.snx = s.snx_cap;
         soc.sny = s.sny_cap;
-        const int key[6] = {c->precision, s.N_cap, s.snx_cap, s.sny_cap, model_has_nfw(c) ? 1 : 0, c->nfw_mode};
-        bool ok = s.graph && s.graph_gen == c->graph_gen;
-        for (int i = 0; ok && i < 6; i++) ok = (s.graph_key[i] == key[i]);
+        const int key[7] = {c->precision, s.N_cap, s.snx_cap, s.sny_cap, model_has_nfw(c) ? 1 : 0, c->nfw_mode,
+                            part};
+        const bool trial = (part == PIPE_TRIAL);
+        const cudaGraphExec_t have = trial ? s.graph_trial : s.graph;
+        const int* have_key = trial ? s.trial_key : s.graph_key;
+        bool ok = have && (trial ? s.trial_gen : s.graph_gen) == c->graph_gen;
+        for (int i = 0; ok && i < 7; i++) ok = (have_key[i] == key[i]);
         if (!ok) {
-            int r = capture_graph(c, s, sdc, soc, key);
+            int r = capture_graph(c, s, sdc, soc, key, part);
             if (r != QLP_OK) return r;
         }
-        CK(cudaGraphLaunch(s.graph, s.stream), "graph launch");
-        count_launches((int)s.graph_launches);
+        CK(cudaGraphLaunch(trial ? s.graph_trial : s.graph, s.stream), "graph launch");
+        count_launches((int)(trial ? s.trial_launches : s.graph_launches));
     } else {
         int r = prepare_slot(c, s);
         if (r != QLP_OK) return r;
-        r = run_pipeline(c, s, sd, so, s.stream, ev);
+        r = run_pipeline(c, s, sd, so, s.stream, ev, part);
         if (r != QLP_OK) return r;
     }
-    CK(cudaMemcpyAsync(h_dst, s.w.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, s.stream), "d2h");
+    if (part != PIPE_PRE)
+        CK(cudaMemcpyAsync(h_dst, s.w.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, s.stream), "d2h");
     return QLP_OK;
 }
 
@@ -405,6 +447,8 @@ static void fill_result(const EvalOut& o, qlp_result* out)
 
 static int ensure_results(qlp_ctx* c, int n)
 {
+    if (!c->h_trial) CK(cudaMallocHost((void**)&c->h_trial, sizeof(EvalOut) * QLP_MAX_SLOTS), "pinned");
+    if ((int)c->regopt_lam.size() < n) { c->regopt_lam.resize(n); c->regopt_evals.resize(n); }
     if (c->h_out_cap < n) {
         if (c->h_out) cudaFreeHost(c->h_out);
         c->h_out = nullptr;
@@ -417,6 +461,58 @@ static int ensure_results(qlp_ctx* c, int n)
         CK(cudaMallocHost((void**)&c->h_ep, sizeof(EvalParams) * n), "pinned");
         c->h_ep_cap = n;
     }
+    return QLP_OK;
+}
+
+// The regularisation-parameter optimisation of the batch instances inst[j]
+// (j = 0 .. k-1), instance inst[j] on slot j (QLens's 'optimize_regparam on':
+// QLens::optimize_regularization_parameter, pixelgrid.cpp:15865-15890).  Each
+// slot runs its instance's lambda-independent part once, then Brent's method
+// over log10(lambda) (brent.h) advances all instances in lockstep: one lambda
+// trial per instance per round, launched on every slot before the host waits
+// for them.  The trial with the least objective (QLens::chisq_regparam_dense,
+// pixelgrid.cpp:16526-16700: chi^2 over the active pixels + regularisation
+// terms + log det F) gives the instance's result, as the reference keeps the
+// amplitudes and log det F of its best trial; its lambda goes to regopt_lam.
+static int regopt_wave(qlp_ctx* c, const std::vector<int>& inst, const std::vector<StaticData>& sds,
+                       const std::vector<SrcOpts>& sos)
+{
+    const int k = (int)inst.size();
+    for (int j = 0; j < k; j++) {
+        int r = issue_eval(c, c->slots[j], sds[j], sos[j], &c->h_ep[inst[j]], nullptr, nullptr, PIPE_PRE);
+        if (r != QLP_OK) return r;
+    }
+    std::vector<BrentMin> br(k);
+    std::vector<double> best(k, INFINITY);
+    std::vector<char> act(k);
+    for (int j = 0; j < k; j++) br[j].reset(c->regopt_minlog, c->regopt_maxlog, c->regopt_tol, c->regopt_maxit);
+    while (true) {
+        bool any = false;
+        for (int j = 0; j < k; j++) {
+            double x;
+            act[j] = br[j].want(&x);
+            if (!act[j]) continue;
+            EvalParams& ep = c->h_ep[inst[j]];
+            ep.regparam = pow(10.0, x);
+            int r = issue_eval(c, c->slots[j], sds[j], sos[j], &ep, &c->h_trial[j], nullptr, PIPE_TRIAL);
+            if (r != QLP_OK) return r;
+            any = true;
+        }
+        if (!any) break;
+        for (int j = 0; j < k; j++)
+            if (act[j]) CK(cudaStreamSynchronize(c->slots[j].stream), "lambda trial");
+        for (int j = 0; j < k; j++) {
+            if (!act[j]) continue;
+            const double f = c->h_trial[j].f_regopt;
+            if (f < best[j]) {
+                best[j] = f;
+                c->h_out[inst[j]] = c->h_trial[j];
+                c->regopt_lam[inst[j]] = c->h_ep[inst[j]].regparam;
+            }
+            br[j].give(f);
+        }
+    }
+    for (int j = 0; j < k; j++) c->regopt_evals[inst[j]] = br[j].evals();
     return QLP_OK;
 }
 
@@ -442,6 +538,26 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     cudaStream_t st = c->stream;
     CK(cudaEventRecord(c->fork, st), "event");
     CK(cudaStreamWaitEvent(s.stream, c->fork, 0), "wait");
+    if (c->regopt && c->so.regularization) {
+        // lambda optimisation: the pre part and the trials, timed as a whole
+        CK(cudaEventRecord(c->ev[0], s.stream), "event");
+        r = regopt_wave(c, {0}, {c->sd}, {c->so});
+        if (r != QLP_OK) { out->status = r; return r; }
+        for (int i = 1; i <= QLP_N_STAGES; i++) CK(cudaEventRecord(c->ev[i], s.stream), "event");
+        CK(cudaEventRecord(s.done, s.stream), "event");
+        CK(cudaStreamWaitEvent(st, s.done, 0), "wait");
+        CK(cudaStreamSynchronize(st), "eval");
+        c->last_launches = kernel_launch_counter() - l0;
+        c->last_h2d = sizeof(EvalParams) + sizeof(double) * c->regopt_evals[0];
+        c->last_d2h = sizeof(EvalOut) * c->regopt_evals[0];
+        for (int i = 0; i < QLP_N_STAGES; i++) c->stage_ms[i] = 0;
+        cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
+        fill_result(c->h_out[0], out);
+        if (c->precision == QLP_MIXED) out->refine_iters = c->refine;
+        out->regparam = c->regopt_lam[0];
+        out->regopt_evals = c->regopt_evals[0];
+        return out->status;
+    }
     r = issue_eval(c, s, c->sd, c->so, &ep, &c->h_out[0], c->ev);
     if (r != QLP_OK) { out->status = r; return r; }
     CK(cudaEventRecord(s.done, s.stream), "event");
@@ -455,6 +571,7 @@ int ctx_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result*
     cudaEventElapsedTime(&c->device_ms, c->ev[0], c->ev[QLP_N_STAGES]);
     fill_result(c->h_out[0], out);
     if (c->precision == QLP_MIXED) out->refine_iters = c->refine;
+    out->regparam = ep.regparam;
     return out->status;
 }
 
@@ -522,7 +639,7 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
     }
     int r = ensure_results(c, n);
     if (r != QLP_OK) return r;
-    const bool timed = !c->use_graphs;     // direct launches record the stage events
+    const bool timed = !c->use_graphs && !(c->regopt && c->so.regularization);  // stage events: direct launches
     const int ne = QLP_N_STAGES + 1;
     while (timed && (int)c->ev_pool.size() < ne * n) {
         cudaEvent_t e;
@@ -535,6 +652,11 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
     for (int k = 0; k < S; k++) CK(cudaStreamWaitEvent(c->slots[k].stream, c->fork, 0), "wait");
     std::vector<int> pre(n, QLP_OK);
     int rc = QLP_OK;
+    // lambda optimisation: instances go in waves of S, one per slot
+    const bool regopt = c->regopt && c->so.regularization;
+    std::vector<int> wave;
+    std::vector<StaticData> wave_sd;
+    std::vector<SrcOpts> wave_so;
     for (int i = 0; i < n; i++) {
         Slot& s = c->slots[i % S];
         EvalParams& ep = c->h_ep[i];
@@ -553,8 +675,20 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         }
         if (ri == QLP_OK && (so.snx < 2 || so.sny < 2)) ri = QLP_ERR_GRID_TOO_SMALL;
         ep.shape = InstShape{sd.mpix, sd.n_mask, sd.n_sub, so.snx, so.sny};
-        if (ri == QLP_OK)
+        c->regopt_lam[i] = ep.regparam;
+        c->regopt_evals[i] = 0;
+        if (ri == QLP_OK && regopt) {
+            wave.push_back(i);
+            wave_sd.push_back(sd);
+            wave_so.push_back(so);
+        } else if (ri == QLP_OK) {
             ri = issue_eval(c, s, sd, so, &ep, &c->h_out[i], timed ? &c->ev_pool[(size_t)ne * i] : nullptr);
+        }
+        if (regopt && ((int)wave.size() == S || (i == n - 1 && !wave.empty()))) {
+            const int rw = regopt_wave(c, wave, wave_sd, wave_so);
+            if (rw != QLP_OK) return rw;
+            wave.clear(); wave_sd.clear(); wave_so.clear();
+        }
         pre[i] = ri;
         if (ri != QLP_OK && rc == QLP_OK) rc = ri;
     }
@@ -587,6 +721,8 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         }
         fill_result(c->h_out[i], &out[i]);
         if (c->precision == QLP_MIXED) out[i].refine_iters = c->refine;
+        out[i].regparam = c->regopt_lam[i];
+        out[i].regopt_evals = c->regopt_evals[i];
     }
     return rc;
 }

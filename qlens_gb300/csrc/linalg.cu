@@ -160,8 +160,9 @@ __device__ __forceinline__ int act_at(const int* ai, int snx, int sny, int i, in
 
 __global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ ai,
                       const double* __restrict__ regp, double* __restrict__ F, double* __restrict__ R, int ldF,
-                      int do_reg)
+                      int do_reg, int parts)
 {
+    const bool toF = parts & REG_F, toR = parts & REG_R;
     const double regparam = *regp;
     const int snx = gs->snx, sny = gs->sny;
     const int M = gs->M, Mp = mpad64(M);
@@ -169,8 +170,8 @@ __global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ 
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
         if (c >= ncell) {   // identity padding
             int i = M + (c - ncell);
-            F[(size_t)i * ldF + i] = 1.0;
-            if (do_reg) R[(size_t)i * ldF + i] = 1.0;
+            if (toF) F[(size_t)i * ldF + i] = 1.0;
+            if (do_reg && toR) R[(size_t)i * ldF + i] = 1.0;
             continue;
         }
         if (!do_reg) continue;
@@ -183,23 +184,30 @@ __global__ void k_reg(const GridState* __restrict__ gs, const int* __restrict__ 
                       act_at(ai, snx, sny, ci, cj + 2), act_at(ai, snx, sny, ci, cj - 2)};
         double diag = 8.0;
         for (int k = 0; k < 4; k++) if (nb1[k] >= 0) diag += 1.0;
-        R[(size_t)a * ldF + a] = diag;
-        F[(size_t)a * ldF + a] += regparam * diag;
+        if (toR) R[(size_t)a * ldF + a] = diag;
+        if (toF) F[(size_t)a * ldF + a] += regparam * diag;
         for (int k = 0; k < 4; k++) {
             int b = nb1[k];
-            if (b >= 0 && b < a) { R[(size_t)a * ldF + b] = -4.0; F[(size_t)a * ldF + b] += regparam * -4.0; }
+            if (b >= 0 && b < a) {
+                if (toR) R[(size_t)a * ldF + b] = -4.0;
+                if (toF) F[(size_t)a * ldF + b] += regparam * -4.0;
+            }
             int b2 = nb2[k];
-            if (b2 >= 0 && nb1[k] >= 0 && b2 < a) { R[(size_t)a * ldF + b2] = 1.0; F[(size_t)a * ldF + b2] += regparam * 1.0; }
+            if (b2 >= 0 && nb1[k] >= 0 && b2 < a) {
+                if (toR) R[(size_t)a * ldF + b2] = 1.0;
+                if (toF) F[(size_t)a * ldF + b2] += regparam * 1.0;
+            }
         }
     }
 }
 
-void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* regp, cudaStream_t st)
+void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* regp, int parts, cudaStream_t st)
 {
     const int ncell = so.snx * so.sny;
-    if (so.regularization) cudaMemsetAsync(w.R, 0, sizeof(double) * (size_t)w.ldF * w.ldF, st);
+    if (so.regularization && (parts & REG_R)) cudaMemsetAsync(w.R, 0, sizeof(double) * (size_t)w.ldF * w.ldF, st);
     int total = ncell + 64;
-    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, regp, w.F, w.R, w.ldF, so.regularization);
+    k_reg<<<(total + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, regp, w.F, w.R, w.ldF, so.regularization,
+                                               parts);
     count_launches(1);
     (void)M_max;
 }
@@ -255,15 +263,16 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
     const StaticData sd = eval_shape(sd_);
     const SrcOpts so = eval_grid(so_, sd_);
     const double regparam = *regp;
-    __shared__ double red[2][32];
+    __shared__ double red[3][32];
     const int M = gs->M;
-    double chi = 0, es = 0;
+    double chi = 0, es = 0, chi_act = 0;
     for (int m = threadIdx.x; m < sd.n_mask; m += blockDim.x) {
         const int pix = sd.mpix[m];
         const double c = sd.use_noise_map ? sd.covinv[pix] : sd.cov_inverse;
         const int r = rowidx[m];
         double dd = (r >= 0) ? model[r] - sd.data[pix] : sd.data[pix];
         chi += dd * dd * c;
+        if (r >= 0) chi_act += dd * dd * c;     // the pixels the lambda optimisation's chi^2 runs over
     }
     if (so.regularization && regparam != 0) {
         const int snx = so.snx, sny = so.sny;
@@ -287,12 +296,17 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
     for (int o = 16; o > 0; o >>= 1) {
         chi += __shfl_xor_sync(0xffffffffu, chi, o);
         es += __shfl_xor_sync(0xffffffffu, es, o);
+        chi_act += __shfl_xor_sync(0xffffffffu, chi_act, o);
     }
-    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = chi; red[1][threadIdx.x >> 5] = es; }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = chi;
+        red[1][threadIdx.x >> 5] = es;
+        red[2][threadIdx.x >> 5] = chi_act;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double c2 = 0, e2 = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { c2 += red[0][k]; e2 += red[1][k]; }
+        double c2 = 0, e2 = 0, ca = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { c2 += red[0][k]; e2 += red[1][k]; ca += red[2][k]; }
         double regterms = 0, loglike = 0;
         if (so.regularization && M > 0) {
             if (regparam != 0) {
@@ -304,6 +318,8 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
         loglike += c2;
         int status = gs->status;
         if (status == 0 && (gs->not_spd_F || gs->not_spd_R)) status = QLP_ERR_NOT_SPD;
+        // QLens::chisq_regparam_dense (pixelgrid.cpp:16688-16692): Ed + prior + log det F
+        out->f_regopt = ca + ((so.regularization && M > 0) ? ((regparam != 0 ? regterms : 0.0) + out->logdet_F) : 0.0);
         out->chisq0 = c2;
         out->Es_times_two = e2;
         out->regterms = regterms;

@@ -34,6 +34,7 @@ struct MixedWork {
     float* sqc = nullptr;    // N_cap: sqrt(C^-1) per active row
     int nnz_cap = 0;
     int2* pixT = nullptr;    // image pixels, x fastest: (active row or -1, sqrt(C^-1))
+    float* F0 = nullptr;     // lambda optimisation: X X^T before lambda R (allocated on first use)
     int* col_u = nullptr;    // nnz_cap: rows of each column in atomic (fill) order
     int* src_u = nullptr;    // nnz_cap: their positions in the merged CSR rows
     double* colval64 = nullptr; // nnz_cap: FP64 values, rows ascending within a column
@@ -327,8 +328,9 @@ __device__ __forceinline__ int act_at32(const int* ai, int snx, int sny, int i, 
 
 __global__ void k_reg32(const GridState* __restrict__ gs, const int* __restrict__ ai,
                         const double* __restrict__ regp, float* __restrict__ F, float* __restrict__ R, int ld,
-                        int do_reg)
+                        int do_reg, int parts)
 {
+    const bool toF = parts & REG_F, toR = parts & REG_R;
     const double regparam = *regp;
     const int snx = gs->snx, sny = gs->sny;
     const int M = gs->M, Mp = (M + 127) & ~127;   // identity up to the 128-block padding
@@ -336,8 +338,8 @@ __global__ void k_reg32(const GridState* __restrict__ gs, const int* __restrict_
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell + (Mp - M); c += gridDim.x * blockDim.x) {
         if (c >= ncell) {
             int i = M + (c - ncell);
-            F[(size_t)i * ld + i] = 1.0f;
-            if (do_reg) R[(size_t)i * ld + i] = 1.0f;
+            if (toF) F[(size_t)i * ld + i] = 1.0f;
+            if (do_reg && toR) R[(size_t)i * ld + i] = 1.0f;
             continue;
         }
         if (!do_reg) continue;
@@ -350,18 +352,18 @@ __global__ void k_reg32(const GridState* __restrict__ gs, const int* __restrict_
                       act_at32(ai, snx, sny, ci, cj + 2), act_at32(ai, snx, sny, ci, cj - 2)};
         double diag = 8.0;
         for (int k = 0; k < 4; k++) if (nb1[k] >= 0) diag += 1.0;
-        R[(size_t)a * ld + a] = (float)diag;
-        F[(size_t)a * ld + a] = (float)((double)F[(size_t)a * ld + a] + regparam * diag);
+        if (toR) R[(size_t)a * ld + a] = (float)diag;
+        if (toF) F[(size_t)a * ld + a] = (float)((double)F[(size_t)a * ld + a] + regparam * diag);
         for (int k = 0; k < 4; k++) {
             int b = nb1[k];
             if (b >= 0 && b < a) {
-                R[(size_t)a * ld + b] = -4.0f;
-                F[(size_t)a * ld + b] = (float)((double)F[(size_t)a * ld + b] - 4.0 * regparam);
+                if (toR) R[(size_t)a * ld + b] = -4.0f;
+                if (toF) F[(size_t)a * ld + b] = (float)((double)F[(size_t)a * ld + b] - 4.0 * regparam);
             }
             int b2 = nb2[k];
             if (b2 >= 0 && nb1[k] >= 0 && b2 < a) {
-                R[(size_t)a * ld + b2] = 1.0f;
-                F[(size_t)a * ld + b2] = (float)((double)F[(size_t)a * ld + b2] + regparam);
+                if (toR) R[(size_t)a * ld + b2] = 1.0f;
+                if (toF) F[(size_t)a * ld + b2] = (float)((double)F[(size_t)a * ld + b2] + regparam);
             }
         }
     }
@@ -426,7 +428,7 @@ void mixed_free(Slot& c)
     if (!m) return;
     void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
                     m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
-                    m->sqc, m->col_u, m->src_u, m->colval64, m->pixT};
+                    m->sqc, m->col_u, m->src_u, m->colval64, m->pixT, m->F0};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
     c.mixed = nullptr;
@@ -517,8 +519,28 @@ static int cholesky_mixed(float* A, int ld, int M_cap128, GridState* gs, int whi
     return n;
 }
 
+// The lambda optimisation's F0 = X X^T (before lambda R): allocated outside
+// any stream capture, before the first PIPE_PRE / PIPE_TRIAL sequence.
+int mixed_ensure_f0(Slot& slot)
+{
+    int rc = mixed_init(slot);
+    if (rc != QLP_OK) return rc;
+    MixedWork* m = mw_of(slot);
+    if (m->F0) return QLP_OK;
+    if (cudaMalloc(&m->F0, sizeof(float) * (size_t)m->ld32 * m->M_cap) != cudaSuccess) {
+        m->F0 = nullptr;
+        set_error("%s (%d)", "lambda optimisation workspace allocation failed", m->M_cap);
+        return QLP_ERR_NOMEM;
+    }
+    return QLP_OK;
+}
+
+// part: PIPE_ALL the whole inversion at the slot's lambda; PIPE_PRE everything
+// that does not depend on lambda (D, X, F0 = X X^T kept aside, R and its log
+// det); PIPE_TRIAL one lambda of the optimisation (F = F0 + lambda R, its
+// factor, log det and the refined amplitudes, the model image).
 int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp,
-                        cudaStream_t st, cudaEvent_t* ev)
+                        int part, cudaStream_t st, cudaEvent_t* ev)
 {
     const int refine = c->refine;
     int rc = mixed_init(slot);
@@ -527,12 +549,24 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     Work& w = slot.w;
     const int N_cap = sd.n_mask;
     const int Mc = slot.M_cap;
+    const size_t f_bytes = sizeof(float) * (size_t)m->ld32 * m->M_cap;
+    const int ltw_blocks = (m->M_cap + 7) / 8;
     int n = 0;
+    if (part != PIPE_ALL && !m->F0) {
+        set_error("%s (%d)", "lambda optimisation workspace missing", part);
+        return QLP_ERR_ARG;
+    }
+    if (part == PIPE_TRIAL) {
+        cudaMemsetAsync(&w.gs->not_spd_F, 0, sizeof(int), st);
+        cudaMemcpyAsync(m->F32, m->F0, f_bytes, cudaMemcpyDeviceToDevice, st);
+        k_reg32<<<(so.snx * so.sny + 128 + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, regp, m->F32, m->R32,
+                                                                    m->ld32, so.regularization, REG_F);
+        n++;
+    } else {
 
     // L by source cell (CSC, rows ascending within a column)
     cudaMemsetAsync(m->nz, 0, (size_t)(m->M_cap / TC_TILE) * m->nkb_cap, st);
     cudaMemsetAsync(m->colcnt, 0, sizeof(int) * (size_t)(m->M_cap + 1), st);
-    const int ltw_blocks = (m->M_cap + 7) / 8;
     {
         const int rb = std::min((N_cap + 255) / 256, 152 * 8);
         cudaMemsetAsync(m->pixT, 0xff, sizeof(int2) * (size_t)slot.npix_pad, st);
@@ -574,9 +608,11 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         n++;
     }
     if (ev) cudaEventRecord(ev[4], st);
+    if (part == PIPE_PRE) cudaMemcpyAsync(m->F0, m->F32, f_bytes, cudaMemcpyDeviceToDevice, st);
     if (so.regularization) cudaMemsetAsync(m->R32, 0, sizeof(float) * (size_t)m->ld32 * m->ld32, st);
     k_reg32<<<(so.snx * so.sny + 128 + 255) / 256, 256, 0, st>>>(w.gs, w.active_index, regp, m->F32, m->R32,
-                                                                m->ld32, so.regularization);
+                                                                m->ld32, so.regularization,
+                                                                part == PIPE_PRE ? REG_R : (REG_F | REG_R));
     n++;
     if (so.regularization) {
         // R's factorisation (log det R only) runs on the slot's second stream,
@@ -590,10 +626,16 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         n++;
         cudaEventRecord(slot.side_join, slot.side);
     }
+    if (part == PIPE_PRE) {
+        if (so.regularization) cudaStreamWaitEvent(st, slot.side_join, 0);
+        count_launches(n);
+        return QLP_OK;
+    }
+    }   // part != PIPE_TRIAL
     n += cholesky_mixed(m->F32, m->ld32, m->M_cap, w.gs, 0, 1 << 20, m->linvF, (size_t)2 * C2 * C2, st);
     k_logdet_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, w.out, 0);
     n++;
-    if (so.regularization) cudaStreamWaitEvent(st, slot.side_join, 0);
+    if (so.regularization && part == PIPE_ALL) cudaStreamWaitEvent(st, slot.side_join, 0);
     // s = F^-1 D with `refine` FP64 refinement sweeps
     k_copy_init<<<(Mc + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->r, w.s);
     n++;

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include "qlpix_internal.h"
 #include "qlpix_ctx.h"
+#include "brent.h"
 
 namespace qlpix {
 
@@ -194,6 +195,33 @@ int qlp_set_graphs(qlp_ctx* c, int on)
 {
     if (!c) return fail(QLP_ERR_ARG, "null context");
     c->use_graphs = on ? 1 : 0;
+    return QLP_OK;
+}
+
+int qlp_set_regparam_optimization(qlp_ctx* c, int on, double minlog, double maxlog, double tol, int max_iter)
+{
+    if (!c) return fail(QLP_ERR_ARG, "null context");
+    if (on && !(minlog < maxlog && tol > 0 && max_iter >= 1)) return fail(QLP_ERR_ARG, "bad lambda optimisation range");
+    c->regopt = on ? 1 : 0;
+    if (on) {
+        c->regopt_minlog = minlog;
+        c->regopt_maxlog = maxlog;
+        c->regopt_tol = tol;
+        c->regopt_maxit = max_iter;
+    }
+    c->graph_gen++;     // the captured sequences split into a lambda-independent part and trials
+    return QLP_OK;
+}
+
+int qlp_brent_min(double (*f)(double, void*), void* user, double ax, double bx, double tol, int max_iter,
+                  double* xmin, int* evals)
+{
+    if (!f || !xmin || !(ax < bx) || max_iter < 0) return fail(QLP_ERR_ARG, "bad Brent arguments");
+    qlpix::BrentMin b(ax, bx, tol, max_iter);
+    double x;
+    while (b.want(&x)) b.give(f(x, user));
+    *xmin = b.xmin();
+    if (evals) *evals = b.evals();
     return QLP_OK;
 }
 

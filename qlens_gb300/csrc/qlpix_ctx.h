@@ -30,11 +30,17 @@ struct Slot {
     cudaEvent_t side_fork = nullptr, side_join = nullptr;
     // the launch sequence captured as a CUDA graph, sized for the slot's
     // capacity (any mask and source grid that fit), valid for one
-    // (precision, capacity, NFW, NFW mode) combination and graph generation
+    // (precision, capacity, NFW, NFW mode, lambda optimisation) combination and
+    // graph generation; with the lambda optimisation on, `graph` holds the
+    // lambda-independent part and `graph_trial` one lambda trial
     cudaGraphExec_t graph = nullptr;
-    int graph_key[6] = {0, 0, 0, 0, 0, 0};
+    int graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
     long long graph_gen = 0;
     long long graph_launches = 0;   // kernels per replay
+    cudaGraphExec_t graph_trial = nullptr;
+    int trial_key[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long trial_gen = 0;
+    long long trial_launches = 0;
 };
 
 }  // namespace qlpix
@@ -76,6 +82,9 @@ struct qlp_ctx {
 
     qlpix::EvalOut* h_out = nullptr;      // pinned, one per batch instance
     int h_out_cap = 0;
+    qlpix::EvalOut* h_trial = nullptr;    // pinned, one per slot: results of lambda trials
+    std::vector<double> regopt_lam;       // per batch instance: the lambda of its result
+    std::vector<int> regopt_evals;        // per batch instance: lambda trials run
     cudaEvent_t ev[QLP_N_STAGES + 1] = {};
     cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<cudaEvent_t> ev_pool;     // (QLP_N_STAGES+1) per batched instance
@@ -83,6 +92,11 @@ struct qlp_ctx {
     int h_ep_cap = 0;
     int use_graphs = 1;                   // batched evaluation replays captured graphs
     int refine = 1;                       // FP64 refinement sweeps of the mixed path's amplitudes
+    // regularisation-parameter optimisation (QLens 'optimize_regparam on'):
+    // Brent's method over log10(lambda), QLens's defaults
+    int regopt = 0;
+    double regopt_minlog = -3.0, regopt_maxlog = 5.0, regopt_tol = 0.01;
+    int regopt_maxit = 20;
     int nfw_mode = QLP_NFW_QUADRATURE;    // NFW deflection: quadrature or trained surrogate
     double nfw_threshold = 2e-5;          // surrogate error bound (arcsec) above which a ray falls back
     long long graph_gen = 1;              // bumped whenever captured graphs go stale
@@ -108,8 +122,15 @@ void set_error(const char* fmt, const char* a, int code);
 // mixed.cu
 int mixed_init(Slot& slot);
 void mixed_free(Slot& slot);
+// launch sequences of one evaluation: the whole of it, or, for the
+// regularisation-parameter optimisation, its lambda-independent part and one
+// lambda trial
+#define PIPE_ALL 0
+#define PIPE_PRE 1
+#define PIPE_TRIAL 2
+int mixed_ensure_f0(Slot& slot);
 int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, const SrcOpts& so, const double* regp,
-                        cudaStream_t st,
+                        int part, cudaStream_t st,
                         cudaEvent_t* ev);
 // autotune.cpp
 int ctx_get_schedule(const qlp_ctx* c, qlp_schedule* out);

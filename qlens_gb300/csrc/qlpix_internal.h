@@ -65,6 +65,8 @@ struct GridState {
 // Scalars of one evaluation, written by the final assembly kernel.
 struct EvalOut {
     double chisq0, logdet_F, logdet_R, Es_times_two, regterms, m2logev;
+    double f_regopt;                   // the lambda optimisation's objective: chi^2 over the active
+                                       // pixels + regularisation terms + log det F
     int n_active_pixels, n_active_src, L_nnz, status, refine_iters;
     int pad;                           // rays that took the NFW quadrature instead of the surrogate
 };
@@ -153,6 +155,7 @@ struct Work {
     EvalParams* ep;                    // this slot's per-evaluation parameters
     // rays whose NFW deflection the surrogate hands to the quadrature (n_sub capacity)
     int* fb_ray;  double* fb_xy;  int* fb_count;
+    double* F0;                        // plain path, lambda optimisation: L'^T C^-1 L' before lambda R
 };
 
 // Device address of the regularisation parameter of a slot's EvalParams.
@@ -177,7 +180,10 @@ int ltw_chunks(int N_cap);
 void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st);
 void launch_D(Work& w, int N_max, int M_max, cudaStream_t st);
 void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st);
-void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* regp, cudaStream_t st);
+// parts: REG_F adds lambda R to F, REG_R writes R (both: the plain evaluation)
+#define REG_F 1
+#define REG_R 2
+void launch_regularization(const SrcOpts& so, Work& w, int M_max, const double* regp, int parts, cudaStream_t st);
 int  launch_cholesky_fp64(double* A, int ld, int M_max, const GridState* gs, int which, double* linv,
                           cudaStream_t st);
 void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaStream_t st);

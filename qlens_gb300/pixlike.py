@@ -17,6 +17,7 @@ import numpy as np
 from . import abi
 
 _lib = None
+BRENT_FN = C.CFUNCTYPE(C.c_double, C.c_double, C.c_void_p)
 
 
 class LibraryUnavailable(RuntimeError):
@@ -61,6 +62,9 @@ def load_library(build_if_missing=False):
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
     L.qlp_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_refinement.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_set_regparam_optimization.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
+    L.qlp_brent_min.argtypes = [BRENT_FN, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double),
+                                P(C.c_int)]
     L.qlp_get_schedule.argtypes = [C.c_void_p, P(abi.qlp_schedule)]
     L.qlp_set_schedule.argtypes = [C.c_void_p, P(abi.qlp_schedule)]
     L.qlp_autotune.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), P(abi.qlp_instance), C.c_int, C.c_int,
@@ -221,6 +225,12 @@ class PixelLikelihood:
                 inst[i].src_npixels_x, inst[i].src_npixels_y = map(int, src_sizes[i])
         return inst
 
+    def set_regparam_optimization(self, on=True, minlog=-3.0, maxlog=5.0, tol=0.01, max_iter=20):
+        """QLens's 'optimize_regparam on': choose lambda per evaluation by
+        Brent's method over log10(lambda) (defaults: QLens's)."""
+        self._check(self.lib.qlp_set_regparam_optimization(self.ctx, 1 if on else 0, float(minlog), float(maxlog),
+                                                           float(tol), int(max_iter)))
+
     def set_refinement(self, sweeps):
         """FP64 refinement sweeps of the mixed path (0..4, default 1)."""
         self._check(self.lib.qlp_set_refinement(self.ctx, int(sweeps)))
@@ -374,3 +384,22 @@ def surrogate_eval(rho_phi_q, device=0):
     if code != abi.QLP_OK:
         raise QLPixError(code, L.qlp_last_error().decode())
     return t, G, B, bound
+
+
+def brent_min(f, ax, bx, tol, max_iter):
+    """The library's Brent minimiser (qlp_brent_min) on a Python function:
+    returns (x_min, evaluations, list of the points evaluated)."""
+    L = load_library()
+    pts = []
+
+    def cb(x, _):
+        pts.append(x)
+        return float(f(x))
+
+    fn = BRENT_FN(cb)
+    x = C.c_double(0)
+    n = C.c_int(0)
+    code = L.qlp_brent_min(fn, None, float(ax), float(bx), float(tol), int(max_iter), C.byref(x), C.byref(n))
+    if code != abi.QLP_OK:
+        raise QLPixError(code, L.qlp_last_error().decode())
+    return x.value, n.value, pts

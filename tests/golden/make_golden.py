@@ -233,6 +233,15 @@ inversion_method dense
     ),
 }
 
+# 'optimize_regparam on': the entry point chooses lambda by Brent's method over
+# log10(lambda) in [-3, 5] (QLens::optimize_regularization_parameter,
+# pixelgrid.cpp:15865); the scalars then hold the chosen lambda ('regparam')
+# and the intermediates are those of the plain inversion at that lambda.
+for _base in ("tiny_sie", "powerlaw"):
+    CASES["regopt_" + _base] = dict(CASES[_base], script=CASES[_base]["script"].replace(
+        "inversion_method dense\n", "inversion_method dense\noptimize_regparam on\n"))
+assert all("optimize_regparam on" in CASES[k]["script"] for k in ("regopt_tiny_sie", "regopt_powerlaw"))
+
 ARRAYS_F64 = ["zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
               "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
               "F_diag", "F_packed_upper", "s", "model"]

@@ -8,6 +8,7 @@ from qlens_gb300 import abi
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["tiny_sie", "fixed_grid", "powerlaw", "nfw", "twoplane", "cfg1"]
+REGOPT_CASES = ["regopt_tiny_sie", "regopt_powerlaw"]
 
 
 class Golden:
@@ -38,6 +39,12 @@ class Golden:
                 o.auto_sourcegrid = 0
                 o.xmin, o.xmax, o.ymin, o.ymax = map(float, w[1:])
         self.opts = o
+
+    @property
+    def regopt(self):
+        """(minlog, maxlog, tol, max_iter) of QLens's 'optimize_regparam on'
+        (its defaults, lens.cpp:421-425) when the case was run with it, else None."""
+        return (-3.0, 5.0, 0.01, 20) if int(self.sc.get("regopt", 0)) else None
 
     def params(self):
         return abi.flat_params(self.lenses)

@@ -1,0 +1,78 @@
+"""Regularisation-parameter optimisation on the GPU (QLens's 'optimize_regparam
+on'): each evaluation builds L, L^T C^-1 L and R once, then Brent's method over
+log10(lambda) runs trials F = L^T C^-1 L + lambda R.  Against the goldens the
+compiled reference produced with the option on: the plain FP64 path within
+1e-6 relative in -2 log(evidence) and lambda; the mixed path within the
+stated |delta log L| < 0.1.  Batched minimisations advance in lockstep and
+give the same bits as single evaluations."""
+import numpy as np
+import pytest
+
+from goldens import REGOPT_CASES, Golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(g, precision):
+    from qlens_gb300 import PixelLikelihood
+    pl = PixelLikelihood.from_opts(g.image, g.psf, g.opts, precision=precision)
+    pl.set_lens_model(g.lenses, *g.zbeta())
+    pl.set_regparam_optimization(True, *g.regopt)
+    return pl
+
+
+@pytest.mark.parametrize("name", REGOPT_CASES)
+def test_regopt_fp64_vs_reference(name):
+    from qlens_gb300 import abi
+    g = Golden(name)
+    pl = _ctx(g, abi.QLP_FP64)
+    r = pl.invert_image_surface_brightness_map()
+    print("%s: lambda %.12g (ref %.12g), -2logev %.10f (ref %.10f), %d trials" % (
+        name, r["regparam"], g.sc["regparam"], r["m2logev"], g.sc["m2logev"], r["regopt_evals"]))
+    assert r["status"] == 0
+    assert abs(r["regparam"] - g.sc["regparam"]) <= 1e-6 * g.sc["regparam"]
+    assert abs(r["m2logev"] - g.sc["m2logev"]) <= 1e-6 * abs(g.sc["m2logev"])
+    assert abs(r["logdet_F"] - g.sc["logdetF"]) <= 1e-6 * abs(g.sc["logdetF"])
+    assert r["regopt_evals"] >= 5
+    # switching it off returns to the script's fixed lambda
+    pl.set_regparam_optimization(False)
+    r0 = pl.invert_image_surface_brightness_map()
+    assert r0["regparam"] == g.opts.regparam and r0["regopt_evals"] == 0
+    assert r0["m2logev"] > r["m2logev"]
+    pl.close()
+
+
+@pytest.mark.parametrize("name", REGOPT_CASES)
+def test_regopt_mixed_vs_reference(name):
+    from qlens_gb300 import abi
+    g = Golden(name)
+    pl = _ctx(g, abi.QLP_MIXED)
+    r = pl.invert_image_surface_brightness_map()
+    print("%s mixed: lambda %.8g (ref %.8g), -2logev diff %.2e" % (
+        name, r["regparam"], g.sc["regparam"], r["m2logev"] - g.sc["m2logev"]))
+    assert r["status"] == 0
+    assert abs(r["m2logev"] - g.sc["m2logev"]) < 0.2
+    assert abs(np.log10(r["regparam"]) - np.log10(g.sc["regparam"])) < 0.05
+    pl.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_regopt_batch_matches_single(precision):
+    from qlens_gb300 import abi
+    g = Golden("regopt_powerlaw")
+    pl = _ctx(g, abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64)
+    pl.set_batch_slots(3)
+    rng = np.random.default_rng(12)
+    P = np.tile(np.array(g.params()), (5, 1))
+    P[:, 0] *= rng.uniform(0.97, 1.03, 5)
+    P[:, 3] = rng.uniform(0.65, 0.85, 5)
+    singles = [pl.invert_image_surface_brightness_map(p) for p in P]
+    pl.set_graphs(True)
+    a = pl.eval_batch(P)
+    pl.set_graphs(False)
+    b = pl.eval_batch(P)
+    for i, (rs, ra, rb) in enumerate(zip(singles, a, b)):
+        assert rs["status"] == ra["status"] == rb["status"] == 0
+        for k in ("m2logev", "regparam", "regopt_evals", "logdet_F", "chisq0"):
+            assert rs[k] == ra[k] == rb[k], (i, k, rs[k], ra[k], rb[k])
+    pl.close()
