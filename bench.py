@@ -188,6 +188,8 @@ def main():
     ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--regopt", action="store_true",
+                    help="choose lambda per evaluation by Brent's method (QLens 'optimize_regparam on')")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch schedule instead of tuning it on a sample batch first")
     ap.add_argument("--nfw", default="surrogate", choices=["surrogate", "quadrature"],
@@ -234,6 +236,8 @@ def main():
             pl.set_nfw_mode(abi.QLP_NFW_SURROGATE)
             nfw = {"mode": "surrogate", "threshold_arcsec": 2e-5, "train_ms": rep["train_ms"],
                    "val_mean_rel": rep["val_mean_rel"], "n_params": rep["n_params"]}
+    if args.regopt:
+        pl.set_regparam_optimization(True)
     uneven = wl.draw_instances is not None      # per-instance masks, source grids and lambdas
     if uneven:
         pl.set_instance_masks(wl.instance_masks)
@@ -368,6 +372,8 @@ def main():
             "stage_ms_single_eval": [float(x) for x in stage],
             "graphs": not args.no_graphs,
             "failed_evals": len(bad),
+            "regopt": ({"lambda_trials_per_eval": float(np.mean([r["regopt_evals"] for r in results])),
+                        "range_log10": [-3, 5], "tol": 0.01} if args.regopt else None),
             "nfw": (dict(nfw, fallback_rays_per_eval=float(np.mean([r["nfw_fallbacks"] for r in results])))
                     if nfw else None),
             "stream_span_ms": span_ms,

@@ -34,10 +34,16 @@ def test_regopt_fp64_vs_reference(name):
     assert abs(r["m2logev"] - g.sc["m2logev"]) <= 1e-6 * abs(g.sc["m2logev"])
     assert abs(r["logdet_F"] - g.sc["logdetF"]) <= 1e-6 * abs(g.sc["logdetF"])
     assert r["regopt_evals"] >= 5
-    # switching it off returns to the script's fixed lambda
+    # switched off: the golden's lambda (the optimised one) reproduces the
+    # optimised evidence, the script's own lambda gives a worse one
     pl.set_regparam_optimization(False)
-    r0 = pl.invert_image_surface_brightness_map()
-    assert r0["regparam"] == g.opts.regparam and r0["regopt_evals"] == 0
+    r1 = pl.invert_image_surface_brightness_map()
+    assert r1["regopt_evals"] == 0 and r1["regparam"] == g.sc["regparam"]
+    assert abs(r1["m2logev"] - g.sc["m2logev"]) <= 1e-6 * abs(g.sc["m2logev"])
+    base = Golden(name.replace("regopt_", ""))
+    r0 = pl.invert_image_surface_brightness_map(None, base.opts.regparam)
+    assert r0["regparam"] == base.opts.regparam
+    assert abs(r0["m2logev"] - base.sc["m2logev"]) <= 1e-6 * abs(base.sc["m2logev"])
     assert r0["m2logev"] > r["m2logev"]
     pl.close()
 
