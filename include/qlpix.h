@@ -200,7 +200,9 @@ typedef struct {
     int slots;          /* evaluations in flight in qlp_eval_batch, 1..64 (default 16) */
     int ray_threads;    /* threads per CTA of the FP64 ray shooting: 64, 128 or 256 (default 256) */
     int psfx_threads;   /* threads per CTA of the mixed path's PSF-to-X build: 128, 256 or 512 (default 256) */
-    int psfx_split;     /* image-row chunks per source cell in that build: 1, 2 or 4 (default 1) */
+    int psfx_split;     /* row chunks (mode 0) or image-row bands (mode 1) per source cell: 1, 2 or 4 (default 1) */
+    int psfx_mode;      /* PSF-to-X build: 0 scatters into active-row accumulators through a pixel table,
+                           1 into a dense window of image rows (default: 1 for PSFs of 500 taps or more) */
 } qlp_schedule;
 
 #define QLP_TUNE_MAX_TRIALS 32

@@ -74,7 +74,8 @@ class qlp_result(C.Structure):
 
 
 class qlp_schedule(C.Structure):
-    _fields_ = [("slots", C.c_int), ("ray_threads", C.c_int), ("psfx_threads", C.c_int), ("psfx_split", C.c_int)]
+    _fields_ = [("slots", C.c_int), ("ray_threads", C.c_int), ("psfx_threads", C.c_int), ("psfx_split", C.c_int),
+                ("psfx_mode", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

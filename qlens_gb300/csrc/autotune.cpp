@@ -32,13 +32,14 @@ void apply(qlp_ctx* c, const qlp_schedule& s)
     c->ray_threads = s.ray_threads;
     c->psfx_threads = s.psfx_threads;
     c->psfx_split = s.psfx_split;
+    c->psfx_mode = s.psfx_mode;
     c->graph_gen++;          // captured graphs hold the old launch shapes
 }
 
 bool same(const qlp_schedule& a, const qlp_schedule& b)
 {
     return a.slots == b.slots && a.ray_threads == b.ray_threads && a.psfx_threads == b.psfx_threads &&
-           a.psfx_split == b.psfx_split;
+           a.psfx_split == b.psfx_split && a.psfx_mode == b.psfx_mode;
 }
 
 }  // namespace
@@ -51,6 +52,7 @@ int ctx_get_schedule(const qlp_ctx* c, qlp_schedule* out)
     out->ray_threads = c->ray_threads;
     out->psfx_threads = c->psfx_threads;
     out->psfx_split = c->psfx_split;
+    out->psfx_mode = c->psfx_mode;
     return QLP_OK;
 }
 
@@ -60,6 +62,7 @@ int ctx_set_schedule(qlp_ctx* c, const qlp_schedule* s)
     if (s->ray_threads != 64 && s->ray_threads != 128 && s->ray_threads != 256) return QLP_ERR_ARG;
     if (s->psfx_threads != 128 && s->psfx_threads != 256 && s->psfx_threads != 512) return QLP_ERR_ARG;
     if (s->psfx_split != 1 && s->psfx_split != 2 && s->psfx_split != 4) return QLP_ERR_ARG;
+    if (s->psfx_mode != 0 && s->psfx_mode != 1) return QLP_ERR_ARG;
     apply(c, *s);
     return QLP_OK;
 }
@@ -124,6 +127,7 @@ int ctx_autotune(qlp_ctx* c, const double* params, const double* lambdas, const 
     r.start_ms = best_ms;
     const std::vector<Knob> knobs = {
         {&qlp_schedule::slots, {8, 16, 32, 64}},
+        {&qlp_schedule::psfx_mode, {0, 1}},
         {&qlp_schedule::psfx_threads, {128, 256, 512}},
         {&qlp_schedule::psfx_split, {1, 2, 4}},
         {&qlp_schedule::ray_threads, {64, 128, 256}},

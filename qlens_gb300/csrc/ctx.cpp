@@ -178,16 +178,18 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     sd.nsub = opts->nsplit * opts->nsplit;
     sd.n_sub = sd.n_mask * sd.nsub;
     sd.pnx = psf->nx; sd.pny = psf->ny;
+    // default PSF-to-X schedule: the dense window of image rows pays off once
+    // the footprint work dominates (measured: 31x31 PSFs gain, 21x21 lose on
+    // an annular mask); the autotuner can override it
+    if (c->psfx_mode < 0) c->psfx_mode = (psf->nx * psf->ny >= 500) ? 1 : 0;
     sd.use_noise_map = noise_map ? 1 : 0;
     sd.cov_inverse = cov_inverse;
     sd.xvals = c->d_xvals; sd.yvals = c->d_yvals; sd.data = c->d_data; sd.covinv = c->d_covinv;
     sd.mpix = c->d_mpix; sd.psf = c->d_psf;
     {
-        double psum = 0, cmax = 0;
+        double psum = 0;
         for (int t = 0; t < psf->nx * psf->ny; t++) psum += fabs(psf->matrix[t]);
-        for (int t = 0; t < npx; t++) cmax = std::max(cmax, covinv[t]);
-        const double bound = std::max(psum, 1e-30) * std::max(sqrt(cmax), 1e-30);
-        sd.fix_exp = std::max(0, std::min(100, 61 - (int)ceil(log2(bound))));
+        sd.fix_exp_x = std::max(0, std::min(100, 61 - (int)ceil(log2(4.0 * std::max(psum, 1e-30)))));
     }
 
     SrcOpts& so = c->so;

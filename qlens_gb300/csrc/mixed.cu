@@ -15,6 +15,7 @@
 // The plain FP64 path (linalg.cu) computes the same quantities entirely in
 // FP64; the mixed path's deviation from it is measured by the tests.
 #include <cuda.h>
+#include <climits>
 #include <cstring>
 #include <algorithm>
 #include "qlpix_ctx.h"
@@ -104,12 +105,12 @@ static int make_map(CUtensorMap* map, float* base, int rows, int cols)
 // Row s of X is the PSF-convolved image of source cell s: every pixel q that
 // sees s (column s of the pre-PSF L) spreads L[q][s] over its PSF neighbours
 // p with weight psf[k][l] (the transpose of QLens's gather,
-// pixelgrid.cpp:14126-14168), scaled by sqrt(C^-1) of p.  The sums are
-// accumulated as 64-bit fixed point in shared memory, so they are exact and
-// independent of the order the atomics land in (the result is the same bits
-// every run); each product is formed in FP32 and rounded once to the
-// fixed-point grid 2^-fix_exp, far below FP32 resolution.  X's rows are
-// written contiguously, no dense L' is stored, and L is read once per cell.
+// pixelgrid.cpp:14126-14168); the sum at p is then scaled by sqrt(C^-1) of p.
+// The sums are accumulated as 64-bit fixed point in shared memory, so they
+// are exact and independent of the order the atomics land in (the result is
+// the same bits every run); each product is formed in FP32 and rounded once
+// to the fixed-point grid 2^-fix_exp_x, far below FP32 resolution.  No dense
+// L' is stored; each CTA covers one cell and one band of image rows.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float to_tf32(float f)
 {
@@ -228,11 +229,154 @@ __global__ void __launch_bounds__(256) k_LTw_csc(const GridState* __restrict__ g
     }
 }
 
-// grid (M_cap cells, image-row chunks); chunk rows of 64-bit accumulators
-__global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* __restrict__ gs,
+// Schedule "bands": grid (M_cap cells, image-row bands).  Each CTA accumulates, for source cell
+// s, the PSF-convolved image of column s of L on the image rows [j0, j1) of
+// its band, in 64-bit fixed point on a dense shared-memory window that spans
+// the bounding box of the footprints reaching the band (at most H rows x
+// (nx + pnx - 1) columns), then writes X[s][r] = sqrt(C^-1)_r times that sum
+// for every active pixel r of the band (zero outside the box).  The column's
+// entries are sorted by active row, i.e. by image row j (j-outer order), so
+// the entries that reach the band are one contiguous range, and so are the
+// band's active rows; for each entry only the PSF rows that land in the band
+// are visited, lanes along x (consecutive accumulators: the 64-bit shared
+// atomics of one instruction do not collide).
+__device__ __forceinline__ int lower_bound_row(const int* __restrict__ rowpix, const int* __restrict__ idx, int n,
+                                               int ny, int jmin)
+{
+    // first position p in [0, n) whose pixel (rowpix[idx ? idx[p] : p]) has y index >= jmin
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int pix = rowpix[idx ? idx[mid] : mid];
+        if (pix - (pix / ny) * ny < jmin) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
-                                               const int2* __restrict__ pixT, int chunk, float* __restrict__ Xh,
+                                               const float* __restrict__ sqc, int H, float* __restrict__ Xh,
+                                               float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
+                                               int nkb_cap)
+{
+    extern __shared__ __align__(16) unsigned char psfx_smem[];
+    const int pnx = sd.pnx, pny = sd.pny, nxh = pnx / 2, nyh = pny / 2;
+    const int nT = pnx * pny;
+    const int Wmax = sd.nx + pnx - 1;
+    long long* acc = reinterpret_cast<long long*>(psfx_smem);
+    float* tpsf = reinterpret_cast<float*>(acc + (size_t)H * Wmax);
+    int* toff = reinterpret_cast<int*>(tpsf + nT);
+    int* sh = toff + nT;          // [0..1] entry range, [2..3] band's active rows, [4..7] box
+    const int N = gs->N, M = gs->M;
+    const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
+    const int s = blockIdx.x;
+    const int j0 = blockIdx.y * H, j1 = min(j0 + H, sd.ny);
+    if (s >= Mp || j0 >= sd.ny) return;
+    const float scale = ldexpf(1.0f, sd.fix_exp_x), inv = ldexpf(1.0f, -sd.fix_exp_x);
+    const int b = (s < M) ? colptr[s] : 0, n = (s < M) ? colptr[s + 1] - b : 0;
+    if (threadIdx.x == 0) {
+        // entries whose footprint (rows jq - nyh .. jq - nyh + pny - 1) can
+        // reach rows [j0, j1): jq in [j0 - nyh, j1 + nyh)
+        sh[0] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
+        sh[1] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
+        // the band's active rows
+        sh[2] = lower_bound_row(rowpix, nullptr, N, sd.ny, j0);
+        sh[3] = lower_bound_row(rowpix, nullptr, N, sd.ny, j1);
+        sh[4] = INT_MAX; sh[5] = INT_MIN; sh[6] = INT_MAX; sh[7] = INT_MIN;
+    }
+    __syncthreads();
+    const int e0 = sh[0], e1 = sh[1];
+    // bounding box of the entries (x and y image indices)
+    {
+        int imn = INT_MAX, imx = INT_MIN, jmn = INT_MAX, jmx = INT_MIN;
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            const int pix = rowpix[colrow[b + e]];
+            const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
+            imn = min(imn, iq); imx = max(imx, iq); jmn = min(jmn, jq); jmx = max(jmx, jq);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            imn = min(imn, __shfl_xor_sync(0xffffffffu, imn, o));
+            imx = max(imx, __shfl_xor_sync(0xffffffffu, imx, o));
+            jmn = min(jmn, __shfl_xor_sync(0xffffffffu, jmn, o));
+            jmx = max(jmx, __shfl_xor_sync(0xffffffffu, jmx, o));
+        }
+        if ((threadIdx.x & 31) == 0 && e1 > e0) {
+            atomicMin(&sh[4], imn); atomicMax(&sh[5], imx); atomicMin(&sh[6], jmn); atomicMax(&sh[7], jmx);
+        }
+    }
+    __syncthreads();
+    const bool any = e1 > e0;
+    const int imin = any ? sh[4] : 0;
+    // window: rows [wr0, wr1) of the image, columns imin - nxh .. imin - nxh + Wb - 1
+    const int wr0 = any ? max(j0, sh[6] - nyh) : j0;
+    const int wr1 = any ? min(j1, sh[7] - nyh + pny) : j0;
+    const int Wb = any ? sh[5] - imin + pnx : 0;
+    for (int i = threadIdx.x; i < (wr1 - wr0) * Wb; i += blockDim.x) acc[i] = 0;
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] scaled to the
+    // fixed-point grid, and the tap's offset in the window from the
+    // footprint's corner
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        const int pl = t / pnx, pk = t - pl * pnx;
+        tpsf[t] = (float)sd.psf[pk * pny + pl] * scale;
+        toff[t] = pl * Wb + pk;
+    }
+    __syncthreads();
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int e = e0 + warp; e < e1; e += nw) {
+            const int q = colrow[b + e];
+            const float v = colval[b + e];
+            const int pix = rowpix[q];
+            const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
+            // PSF rows pl land on image row jq - nyh + pl; keep those in [wr0, wr1)
+            const int pl0 = max(0, wr0 - (jq - nyh)), pl1 = min(pny, wr1 - (jq - nyh));
+            // the footprint's corner (iq - nxh, jq - nyh) in window coordinates
+            unsigned long long* corner = reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb + (iq - imin);
+            const int t1 = pl1 * pnx;
+            for (int t = pl0 * pnx + lane; t < t1; t += 32)
+                atomicAdd(corner + toff[t], (unsigned long long)__float2ll_rn(tpsf[t] * v));
+        }
+    }
+    __syncthreads();
+    // X[s][r] for the band's active rows r: v = sqrt(C^-1)_r * sum (0 outside
+    // the window), hi = v rounded to TF32, lo = the TF32 rounding of v - hi;
+    // the first band also clears X[s][N .. N rounded up to 32) (the SYRK reads
+    // whole blocks)
+    for (int r = sh[2] + threadIdx.x; r < sh[3]; r += blockDim.x) {
+        const int pix = rowpix[r];
+        const int i = pix / sd.ny, j = pix - i * sd.ny;
+        const int wc = i - imin + nxh;
+        float h = 0.0f, l = 0.0f;
+        if (j >= wr0 && j < wr1 && wc >= 0 && wc < Wb) {
+            const float v = ((float)acc[(j - wr0) * Wb + wc] * inv) * sqc[r];
+            h = to_tf32(v);
+            l = to_tf32(v - h);
+        }
+        Xh[(size_t)s * K_cap + r] = h;
+        Xl[(size_t)s * K_cap + r] = l;
+        if (h != 0.0f || l != 0.0f) nz[(size_t)(s / TC_TILE) * nkb_cap + r / TC_KB] = 1;
+    }
+    if (blockIdx.y == 0) {
+        const int Np = (N + TC_KB - 1) / TC_KB * TC_KB;
+        for (int r = N + threadIdx.x; r < Np; r += blockDim.x) {
+            Xh[(size_t)s * K_cap + r] = 0.0f;
+            Xl[(size_t)s * K_cap + r] = 0.0f;
+        }
+    }
+}
+
+// Schedule "rows": grid (M_cap cells, chunks of active rows); one CTA holds
+// the 64-bit accumulators of a chunk of active rows and scatters each entry
+// of column s over its PSF footprint through the active-row table of the
+// padded image (pixT).  Each product psf x v is rounded once to the grid
+// 2^-fix_exp_x and sqrt(C^-1) applied to the sum, exactly as the "bands"
+// schedule does, so both give the same bits.
+__global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridState* __restrict__ gs,
+                                               const int* __restrict__ colptr, const int* __restrict__ colrow,
+                                               const float* __restrict__ colval, const int* __restrict__ rowpix,
+                                               const int2* __restrict__ pixT, const float* __restrict__ sqc,
+                                               int chunk, float* __restrict__ Xh,
                                                float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
                                                int nkb_cap)
 {
@@ -246,7 +390,7 @@ __global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* _
     const int r0 = blockIdx.y * chunk, r1 = min(r0 + chunk, Np);
     if (s >= Mp || r0 >= Np) return;
     const int nT = sd.pnx * sd.pny;
-    const float scale = ldexpf(1.0f, sd.fix_exp), inv = ldexpf(1.0f, -sd.fix_exp);
+    const float scale = ldexpf(1.0f, sd.fix_exp_x), inv = ldexpf(1.0f, -sd.fix_exp_x);
     const int pnx = sd.pnx, pny = sd.pny;
     const int nxp = sd.nx + 2 * (pnx / 2);                    // padded width of pixT
     int* toff = reinterpret_cast<int*>(tpsf + nT);
@@ -289,27 +433,27 @@ __global__ void __launch_bounds__(512) k_psf_x(StaticData sd, const GridState* _
                 }
                 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    if (P[u].x >= r0 && P[u].x < r1) {              // inactive (-1) or another chunk
-                        const float x = w[u] * v * __int_as_float(P[u].y);
+                    if (P[u].x >= r0 && P[u].x < r1)                // inactive (-1) or another chunk
                         atomicAdd(reinterpret_cast<unsigned long long*>(&acc[P[u].x - r0]),
-                                  (unsigned long long)__float2ll_rn(x));
-                    }
+                                  (unsigned long long)__float2ll_rn(w[u] * v));
                 }
             }
         }
     }
     __syncthreads();
-    // write row s of X for pixels [r0, r1): hi = x rounded to TF32, lo = the
-    // TF32 rounding of the exact remainder; one warp covers one 32-pixel block
+    // write row s of X for pixels [r0, r1): v = sqrt(C^-1)_r * sum, hi = v
+    // rounded to TF32, lo = the TF32 rounding of v - hi (zero beyond the N
+    // active rows); one warp covers one 32-pixel block
     const int span = r1 - r0;
     for (int i0 = 0; i0 < span; i0 += blockDim.x) {
         const int i = i0 + threadIdx.x;
         float h = 0.0f, l = 0.0f;
         if (i < span) {
-            const long long a = acc[i];
-            h = to_tf32((float)a * inv);
-            const long long rem = a - __float2ll_rn(h * scale);
-            l = to_tf32((float)rem * inv);
+            if (r0 + i < N) {
+                const float v = ((float)acc[i] * inv) * sqc[r0 + i];
+                h = to_tf32(v);
+                l = to_tf32(v - h);
+            }
             Xh[(size_t)s * K_cap + r0 + i] = h;
             Xl[(size_t)s * K_cap + r0 + i] = l;
         }
@@ -486,7 +630,8 @@ int mixed_init(Slot& c)
         set_error("%s (%d)", "cuTensorMapEncodeTiled unavailable or failed", 0);
         return QLP_ERR_CUDA;
     }
-    cudaFuncSetAttribute(k_psf_x, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_psf_x_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_psf_x_band, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
     cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
     cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
@@ -584,20 +729,35 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     n++;
     // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
     {
-        // accumulator rows per CTA: the pixels split into psfx_split chunks (or
-        // more, if a chunk does not fit beside the PSF in 227 KB)
         const int nT = sd.pnx * sd.pny;
-        const int fit = (int)(((227 * 1024 - (sizeof(float) + sizeof(int)) * (size_t)nT) / sizeof(long long)) &
-                              ~(size_t)31);
         const int split = std::max(1, std::min(c->psfx_split, 4));
-        const int want = ((m->K_cap + split - 1) / split + 31) & ~31;
-        const int chunk = std::max(32, std::min(want, fit));
-        const int nchunk = (m->K_cap + chunk - 1) / chunk;
-        const size_t smem = sizeof(long long) * (size_t)chunk + (sizeof(float) + sizeof(int)) * (size_t)nT;
         const int pt = (c->psfx_threads == 128 || c->psfx_threads == 512) ? c->psfx_threads : 256;
-        k_psf_x<<<dim3(m->M_cap, nchunk), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix,
-                                                            m->pixT, chunk, m->X_hi, m->X_lo, m->K_cap, m->nz,
-                                                            m->nkb_cap);
+        if (c->psfx_mode == 1) {
+            // image rows per CTA: as many as fit beside the PSF tables in about
+            // half an SM's shared memory (two CTAs per SM), divided by psfx_split
+            const int W = sd.nx + sd.pnx - 1;
+            const size_t tap_bytes = (sizeof(float) + sizeof(int)) * (size_t)nT + 8 * sizeof(int);
+            const size_t avail = (110 * 1024 > tap_bytes) ? 110 * 1024 - tap_bytes : 0;
+            const int fit = std::max(1, (int)(avail / (sizeof(long long) * W)));
+            const int H = std::max(1, std::min(sd.ny, fit) / split);
+            const int nband = (sd.ny + H - 1) / H;
+            const size_t smem = sizeof(long long) * (size_t)H * W + tap_bytes;
+            k_psf_x_band<<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
+                                                                   w.rowpix, m->sqc, H, m->X_hi, m->X_lo, m->K_cap,
+                                                                   m->nz, m->nkb_cap);
+        } else {
+            // accumulator rows per CTA: the active rows split into psfx_split
+            // chunks (or more, if a chunk does not fit beside the PSF in 227 KB)
+            const int fit = (int)(((227 * 1024 - (sizeof(float) + sizeof(int)) * (size_t)nT) / sizeof(long long)) &
+                                  ~(size_t)31);
+            const int want = ((m->K_cap + split - 1) / split + 31) & ~31;
+            const int chunk = std::max(32, std::min(want, fit));
+            const int nchunk = (m->K_cap + chunk - 1) / chunk;
+            const size_t smem = sizeof(long long) * (size_t)chunk + (sizeof(float) + sizeof(int)) * (size_t)nT;
+            k_psf_x_rows<<<dim3(m->M_cap, nchunk), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
+                                                                    w.rowpix, m->pixT, m->sqc, chunk, m->X_hi,
+                                                                    m->X_lo, m->K_cap, m->nz, m->nkb_cap);
+        }
         n++;
     }
     if (ev) cudaEventRecord(ev[3], st);

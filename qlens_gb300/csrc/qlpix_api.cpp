@@ -330,7 +330,9 @@ int qlp_set_stream(qlp_ctx* c, void* stream)
 int qlp_eval(qlp_ctx* c, const double* lens_params, double regparam, qlp_result* out)
 {
     if (!c || !out) return fail(QLP_ERR_ARG, "null argument");
-    return ctx_eval(c, lens_params, regparam, out);
+    const int r = ctx_eval(c, lens_params, regparam, out);
+    if (r != QLP_OK && out->status == QLP_OK) out->status = r;   // a failure before any result
+    return r;
 }
 
 int qlp_set_instance_masks(qlp_ctx* c, const unsigned char* masks, int n_masks)
@@ -343,7 +345,15 @@ int qlp_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
                    qlp_result* out)
 {
     if (!c || !out || n < 0 || (n > 0 && !params)) return fail(QLP_ERR_ARG, "bad batch arguments");
-    return ctx_eval_batch(c, params, regparams, inst, n, out);
+    const int r = ctx_eval_batch(c, params, regparams, inst, n, out);
+    // a failure of the batch itself (not of one instance's likelihood) leaves
+    // no valid result: every instance reports it
+    if (r != QLP_OK && r != QLP_ERR_NOT_SPD && r != QLP_ERR_NO_SOURCE_PIXELS && r != QLP_ERR_GRID_TOO_SMALL)
+        for (int i = 0; i < n; i++) {
+            memset(&out[i], 0, sizeof(out[i]));
+            out[i].status = r;
+        }
+    return r;
 }
 
 int qlp_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value, int* active_index,

@@ -53,7 +53,9 @@ struct qlp_ctx {
     int max_slots = 16;                   // schedule: evaluations in flight
     int ray_threads = 256;                // schedule: ray-shooting CTA size
     int psfx_threads = 256;               // schedule: k_psf_x CTA size
-    int psfx_split = 1;                   // schedule: image-row chunks per source cell in k_psf_x
+    int psfx_split = 1;                   // schedule: row chunks / bands per source cell in the PSF-to-X build
+    int psfx_mode = -1;                   // schedule: PSF-to-X kernel, 0 active-row chunks, 1 image-row
+                                          // bands (-1: chosen from the PSF size at creation)
 
     // lens model
     std::vector<qlp_lens> lenses;

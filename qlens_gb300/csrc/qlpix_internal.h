@@ -85,9 +85,10 @@ struct StaticData {            // per-context, uploaded once
     const double* covinv;      // nx*ny (filled with cov_inverse when uniform)
     const int* mpix;           // n_mask: i*ny+j, j-outer / i-inner order
     const double* psf;         // pnx*pny
-    // fixed-point scale of the mixed path's L' accumulation: 2^fix_exp keeps
-    // sum|psf| * max sqrt(C^-1) (a bound on every |L' sqrt(C^-1)| entry) below 2^61
-    int fix_exp;
+    // fixed-point scale of the mixed path's PSF-to-X sums of psf x L
+    // (sqrt(C^-1) is applied to the sum): 2^fix_exp_x keeps 4 sum|psf| below
+    // 2^61 (|L entries| <= 4)
+    int fix_exp_x;
     // device address of this evaluation's InstShape: the kernels take mpix,
     // n_mask, n_sub and the source-grid size from there (the host-side copy
     // of those fields only sizes the launches)

@@ -11,7 +11,7 @@ from goldens import Golden
 pytestmark = pytest.mark.gpu
 
 CANDIDATES = {"slots": {1, 2, 3, 4, 8, 16, 32, 64}, "ray_threads": {64, 128, 256},
-              "psfx_threads": {128, 256, 512}, "psfx_split": {1, 2, 4}}
+              "psfx_threads": {128, 256, 512}, "psfx_split": {1, 2, 4}, "psfx_mode": {0, 1}}
 
 
 def _ctx(g, precision):
@@ -39,9 +39,10 @@ def test_schedules_give_identical_results(precision):
     pl = _ctx(g, abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64)
     P = _draws(g, 6, 3)
     ref = None
-    for sched in ({"slots": 2, "ray_threads": 256, "psfx_threads": 256, "psfx_split": 1},
-                  {"slots": 4, "ray_threads": 64, "psfx_threads": 512, "psfx_split": 4},
-                  {"slots": 3, "ray_threads": 128, "psfx_threads": 128, "psfx_split": 2}):
+    for sched in ({"slots": 2, "ray_threads": 256, "psfx_threads": 256, "psfx_split": 1, "psfx_mode": 0},
+                  {"slots": 4, "ray_threads": 64, "psfx_threads": 512, "psfx_split": 4, "psfx_mode": 1},
+                  {"slots": 3, "ray_threads": 128, "psfx_threads": 128, "psfx_split": 2, "psfx_mode": 0},
+                  {"slots": 2, "ray_threads": 256, "psfx_threads": 256, "psfx_split": 1, "psfx_mode": 1}):
         pl.set_schedule(**sched)
         assert pl.schedule() == sched
         res = pl.eval_batch(P)
@@ -52,6 +53,8 @@ def test_schedules_give_identical_results(precision):
                 assert a[k] == b[k], (sched, k, a[k], b[k])
     with pytest.raises(Exception):
         pl.set_schedule(psfx_split=3)
+    with pytest.raises(Exception):
+        pl.set_schedule(psfx_mode=2)
     pl.close()
 
 
