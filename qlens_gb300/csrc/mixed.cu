@@ -275,16 +275,14 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     if (s >= Mp || j0 >= sd.ny) return;
     const float scale = ldexpf(1.0f, sd.fix_exp_x), inv = ldexpf(1.0f, -sd.fix_exp_x);
     const int b = (s < M) ? colptr[s] : 0, n = (s < M) ? colptr[s + 1] - b : 0;
-    if (threadIdx.x == 0) {
-        // entries whose footprint (rows jq - nyh .. jq - nyh + pny - 1) can
-        // reach rows [j0, j1): jq in [j0 - nyh, j1 + nyh)
-        sh[0] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
-        sh[1] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
-        // the band's active rows
-        sh[2] = lower_bound_row(rowpix, nullptr, N, sd.ny, j0);
-        sh[3] = lower_bound_row(rowpix, nullptr, N, sd.ny, j1);
-        sh[4] = INT_MAX; sh[5] = INT_MIN; sh[6] = INT_MAX; sh[7] = INT_MIN;
-    }
+    // four binary searches, one thread each: the entries whose footprint
+    // (rows jq - nyh .. jq - nyh + pny - 1) can reach rows [j0, j1), i.e. jq in
+    // [j0 - nyh, j1 + nyh), and the band's active rows
+    if (threadIdx.x == 0) sh[0] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
+    if (threadIdx.x == 32) sh[1] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
+    if (threadIdx.x == 64) sh[2] = lower_bound_row(rowpix, nullptr, N, sd.ny, j0);
+    if (threadIdx.x == 96) sh[3] = lower_bound_row(rowpix, nullptr, N, sd.ny, j1);
+    if (threadIdx.x == 1) { sh[4] = INT_MAX; sh[5] = INT_MIN; sh[6] = INT_MAX; sh[7] = INT_MIN; }
     __syncthreads();
     const int e0 = sh[0], e1 = sh[1];
     // bounding box of the entries (x and y image indices)
