@@ -187,8 +187,11 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     sd.xvals = c->d_xvals; sd.yvals = c->d_yvals; sd.data = c->d_data; sd.covinv = c->d_covinv;
     sd.mpix = c->d_mpix; sd.psf = c->d_psf;
     {
-        double psum = 0;
+        double psum = 0, cmax = 0;
         for (int t = 0; t < psf->nx * psf->ny; t++) psum += fabs(psf->matrix[t]);
+        for (int t = 0; t < npx; t++) cmax = std::max(cmax, covinv[t]);
+        const double xmax = 4.0 * std::max(psum, 1e-30) * std::max(sqrt(cmax), 1e-30);
+        sd.x_exp = std::max(-60, std::min(60, (int)floor(log2(16384.0 / xmax))));
         sd.fix_exp_x = std::max(0, std::min(100, 61 - (int)ceil(log2(4.0 * std::max(psum, 1e-30)))));
     }
 

@@ -15,6 +15,7 @@
 // The plain FP64 path (linalg.cu) computes the same quantities entirely in
 // FP64; the mixed path's deviation from it is measured by the tests.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <climits>
 #include <cstring>
 #include <algorithm>
@@ -39,8 +40,9 @@ struct MixedWork {
     int* col_u = nullptr;    // nnz_cap: rows of each column in atomic (fill) order
     int* src_u = nullptr;    // nnz_cap: their positions in the merged CSR rows
     double* colval64 = nullptr; // nnz_cap: FP64 values, rows ascending within a column
-    float* X_hi = nullptr;
-    float* X_lo = nullptr;
+    void* X_hi = nullptr;    // F16 (or TF32 in FP32 storage) parts of X
+    void* X_lo = nullptr;
+    bool half = true;        // X in F16 for the kind::f16 SYRK
     int K_cap = 0;           // columns of X (image pixels), multiple of 32
     int M_cap = 0;           // rows of X, multiple of 128
     unsigned char* nz = nullptr;
@@ -84,15 +86,18 @@ static EncodeTiledFn get_encode()
     return fn;
 }
 
-static int make_map(CUtensorMap* map, float* base, int rows, int cols)
+// 128-row boxes of 128 bytes (32 FP32 or 64 F16 values), 128-byte swizzle
+static int make_map(CUtensorMap* map, void* base, int rows, int cols, bool half)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc) return QLP_ERR_CUDA;
+    const size_t esz = half ? 2 : 4;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
-    cuuint32_t box[2] = {TC_KB, TC_TILE};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * esz};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esz), TC_TILE};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+    CUresult r = enc(map, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims,
+                     strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? QLP_OK : QLP_ERR_CUDA;
@@ -117,6 +122,26 @@ __device__ __forceinline__ float to_tf32(float f)
     uint32_t u;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(f));
     return __uint_as_float(u);
+}
+
+// One entry of X split into hi + lo: TF32 parts in FP32 storage, or F16 parts
+// of v scaled by xs (a power of two that puts X's largest entry near 2^14,
+// undone exactly by the SYRK).  Returns whether either part is nonzero.
+__device__ __forceinline__ bool store_x(void* Xh, void* Xl, size_t idx, float v, float xs, bool half)
+{
+    if (half) {
+        const float vs = v * xs;
+        const __half h = __float2half_rn(vs);
+        const __half l = __float2half_rn(vs - __half2float(h));
+        reinterpret_cast<__half*>(Xh)[idx] = h;
+        reinterpret_cast<__half*>(Xl)[idx] = l;
+        return __half2float(h) != 0.0f || __half2float(l) != 0.0f;
+    }
+    const float h = to_tf32(v);
+    const float l = to_tf32(v - h);
+    reinterpret_cast<float*>(Xh)[idx] = h;
+    reinterpret_cast<float*>(Xl)[idx] = l;
+    return h != 0.0f || l != 0.0f;
 }
 
 // column counts of the merged pre-PSF L, sqrt(C^-1) per active row, and the
@@ -256,8 +281,9 @@ __device__ __forceinline__ int lower_bound_row(const int* __restrict__ rowpix, c
 __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
-                                               const float* __restrict__ sqc, int H, float* __restrict__ Xh,
-                                               float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
+                                               const float* __restrict__ sqc, int H, void* __restrict__ Xh,
+                                               void* __restrict__ Xl, float xs, int half, int K_cap,
+                                               unsigned char* __restrict__ nz,
                                                int nkb_cap)
 {
     extern __shared__ __align__(16) unsigned char psfx_smem[];
@@ -338,29 +364,20 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     }
     __syncthreads();
     // X[s][r] for the band's active rows r: v = sqrt(C^-1)_r * sum (0 outside
-    // the window), hi = v rounded to TF32, lo = the TF32 rounding of v - hi;
-    // the first band also clears X[s][N .. N rounded up to 32) (the SYRK reads
-    // whole blocks)
+    // the window) split into hi + lo; the first band also clears X[s][N .. N
+    // rounded up to 64) (the SYRK reads whole stages)
     for (int r = sh[2] + threadIdx.x; r < sh[3]; r += blockDim.x) {
         const int pix = rowpix[r];
         const int i = pix / sd.ny, j = pix - i * sd.ny;
         const int wc = i - imin + nxh;
-        float h = 0.0f, l = 0.0f;
-        if (j >= wr0 && j < wr1 && wc >= 0 && wc < Wb) {
-            const float v = ((float)acc[(j - wr0) * Wb + wc] * inv) * sqc[r];
-            h = to_tf32(v);
-            l = to_tf32(v - h);
-        }
-        Xh[(size_t)s * K_cap + r] = h;
-        Xl[(size_t)s * K_cap + r] = l;
-        if (h != 0.0f || l != 0.0f) nz[(size_t)(s / TC_TILE) * nkb_cap + r / TC_KB] = 1;
+        float v = 0.0f;
+        if (j >= wr0 && j < wr1 && wc >= 0 && wc < Wb) v = ((float)acc[(j - wr0) * Wb + wc] * inv) * sqc[r];
+        if (store_x(Xh, Xl, (size_t)s * K_cap + r, v, xs, half))
+            nz[(size_t)(s / TC_TILE) * nkb_cap + r / TC_KB] = 1;
     }
     if (blockIdx.y == 0) {
-        const int Np = (N + TC_KB - 1) / TC_KB * TC_KB;
-        for (int r = N + threadIdx.x; r < Np; r += blockDim.x) {
-            Xh[(size_t)s * K_cap + r] = 0.0f;
-            Xl[(size_t)s * K_cap + r] = 0.0f;
-        }
+        const int Np = (N + 63) & ~63;
+        for (int r = N + threadIdx.x; r < Np; r += blockDim.x) store_x(Xh, Xl, (size_t)s * K_cap + r, 0.0f, xs, half);
     }
 }
 
@@ -374,8 +391,8 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
                                                const int2* __restrict__ pixT, const float* __restrict__ sqc,
-                                               int chunk, float* __restrict__ Xh,
-                                               float* __restrict__ Xl, int K_cap, unsigned char* __restrict__ nz,
+                                               int chunk, void* __restrict__ Xh, void* __restrict__ Xl, float xs,
+                                               int half, int K_cap, unsigned char* __restrict__ nz,
                                                int nkb_cap)
 {
     extern __shared__ __align__(16) unsigned char psfx_smem[];
@@ -383,7 +400,7 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
     float* tpsf = reinterpret_cast<float*>(acc + chunk);
     const int N = gs->N, M = gs->M;
     const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
-    const int Np = (N + TC_KB - 1) / TC_KB * TC_KB;
+    const int Np = (N + 63) & ~63;                           // whole 64-pixel stages for the F16 SYRK
     const int s = blockIdx.x;
     const int r0 = blockIdx.y * chunk, r1 = min(r0 + chunk, Np);
     if (s >= Mp || r0 >= Np) return;
@@ -439,23 +456,17 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
         }
     }
     __syncthreads();
-    // write row s of X for pixels [r0, r1): v = sqrt(C^-1)_r * sum, hi = v
-    // rounded to TF32, lo = the TF32 rounding of v - hi (zero beyond the N
-    // active rows); one warp covers one 32-pixel block
+    // write row s of X for pixels [r0, r1): v = sqrt(C^-1)_r * sum split into
+    // hi + lo (zero beyond the N active rows); one warp covers one 32-pixel block
     const int span = r1 - r0;
     for (int i0 = 0; i0 < span; i0 += blockDim.x) {
         const int i = i0 + threadIdx.x;
-        float h = 0.0f, l = 0.0f;
+        bool nonzero = false;
         if (i < span) {
-            if (r0 + i < N) {
-                const float v = ((float)acc[i] * inv) * sqc[r0 + i];
-                h = to_tf32(v);
-                l = to_tf32(v - h);
-            }
-            Xh[(size_t)s * K_cap + r0 + i] = h;
-            Xl[(size_t)s * K_cap + r0 + i] = l;
+            const float v = (r0 + i < N) ? ((float)acc[i] * inv) * sqc[r0 + i] : 0.0f;
+            nonzero = store_x(Xh, Xl, (size_t)s * K_cap + r0 + i, v, xs, half);
         }
-        const unsigned any = __ballot_sync(0xffffffffu, (h != 0.0f) || (l != 0.0f));
+        const unsigned any = __ballot_sync(0xffffffffu, nonzero);
         if ((threadIdx.x & 31) == 0 && any && i < span)
             nz[(size_t)(s / TC_TILE) * nkb_cap + (r0 + i) / TC_KB] = 1;
     }
@@ -591,8 +602,9 @@ int mixed_init(Slot& c)
     m->ld32 = M_cap;
     cudaError_t e = cudaSuccess;
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, bytes > 0 ? bytes : 16); };
-    A((void**)&m->X_hi, sizeof(float) * (size_t)M_cap * K_cap);
-    A((void**)&m->X_lo, sizeof(float) * (size_t)M_cap * K_cap);
+    const size_t xbytes = (m->half ? 2 : 4) * (size_t)M_cap * K_cap;
+    A((void**)&m->X_hi, xbytes);
+    A((void**)&m->X_lo, xbytes);
     A((void**)&m->nz, (size_t)(M_cap / TC_TILE) * m->nkb_cap);
     A((void**)&m->F32, sizeof(float) * (size_t)M_cap * M_cap);
     A((void**)&m->R32, sizeof(float) * (size_t)M_cap * M_cap);
@@ -622,9 +634,10 @@ int mixed_init(Slot& c)
         set_error("%s (%d)", "mixed-precision workspace allocation failed", (int)e);
         return QLP_ERR_NOMEM;
     }
-    cudaMemset(m->X_hi, 0, sizeof(float) * (size_t)M_cap * K_cap);
-    cudaMemset(m->X_lo, 0, sizeof(float) * (size_t)M_cap * K_cap);
-    if (make_map(&m->map_hi, m->X_hi, M_cap, K_cap) != QLP_OK || make_map(&m->map_lo, m->X_lo, M_cap, K_cap) != QLP_OK) {
+    cudaMemset(m->X_hi, 0, xbytes);
+    cudaMemset(m->X_lo, 0, xbytes);
+    if (make_map(&m->map_hi, m->X_hi, M_cap, K_cap, m->half) != QLP_OK ||
+        make_map(&m->map_lo, m->X_lo, M_cap, K_cap, m->half) != QLP_OK) {
         set_error("%s (%d)", "cuTensorMapEncodeTiled unavailable or failed", 0);
         return QLP_ERR_CUDA;
     }
@@ -632,7 +645,8 @@ int mixed_init(Slot& c)
     cudaFuncSetAttribute(k_psf_x_band, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
     cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
-    cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    cudaFuncSetAttribute(k_syrk_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    cudaFuncSetAttribute(k_syrk_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     m->ready = true;
     return QLP_OK;
 }
@@ -726,6 +740,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, w.D);
     n++;
     // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
+    const float xs = m->half ? ldexpf(1.0f, sd.x_exp) : 1.0f;     // F16 scale of X
     {
         const int nT = sd.pnx * sd.pny;
         const int split = std::max(1, std::min(c->psfx_split, 4));
@@ -741,8 +756,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
             const int nband = (sd.ny + H - 1) / H;
             const size_t smem = sizeof(long long) * (size_t)H * W + tap_bytes;
             k_psf_x_band<<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
-                                                                   w.rowpix, m->sqc, H, m->X_hi, m->X_lo, m->K_cap,
-                                                                   m->nz, m->nkb_cap);
+                                                                   w.rowpix, m->sqc, H, m->X_hi, m->X_lo, xs,
+                                                                   m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
         } else {
             // accumulator rows per CTA: the active rows split into psfx_split
             // chunks (or more, if a chunk does not fit beside the PSF in 227 KB)
@@ -754,15 +769,20 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
             const size_t smem = sizeof(long long) * (size_t)chunk + (sizeof(float) + sizeof(int)) * (size_t)nT;
             k_psf_x_rows<<<dim3(m->M_cap, nchunk), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
                                                                     w.rowpix, m->pixT, m->sqc, chunk, m->X_hi,
-                                                                    m->X_lo, m->K_cap, m->nz, m->nkb_cap);
+                                                                    m->X_lo, xs, m->half ? 1 : 0, m->K_cap, m->nz,
+                                                                    m->nkb_cap);
         }
         n++;
     }
     if (ev) cudaEventRecord(ev[3], st);
     {
         const int nt = m->M_cap / TC_TILE;
-        k_syrk_tc<<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(m->map_hi, m->map_lo, w.gs, m->nz, m->nkb_cap, m->F32,
-                                                            m->ld32);
+        if (m->half)
+            k_syrk_tc<true><<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(m->map_hi, m->map_lo, w.gs, m->nz, m->nkb_cap,
+                                                                      m->F32, m->ld32, ldexpf(1.0f, -2 * sd.x_exp));
+        else
+            k_syrk_tc<false><<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(m->map_hi, m->map_lo, w.gs, m->nz,
+                                                                       m->nkb_cap, m->F32, m->ld32, 1.0f);
         n++;
     }
     if (ev) cudaEventRecord(ev[4], st);

@@ -89,6 +89,9 @@ struct StaticData {            // per-context, uploaded once
     // (sqrt(C^-1) is applied to the sum): 2^fix_exp_x keeps 4 sum|psf| below
     // 2^61 (|L entries| <= 4)
     int fix_exp_x;
+    // F16 operands of the mixed path's SYRK: X scaled by 2^x_exp puts its
+    // largest possible entry (4 sum|psf| max sqrt(C^-1)) at or below 2^14
+    int x_exp;
     // device address of this evaluation's InstShape: the kernels take mpix,
     // n_mask, n_sub and the source-grid size from there (the host-side copy
     // of those fields only sizes the launches)

@@ -1,20 +1,24 @@
-// tc_syrk.cuh -- F = X X^T on the 5th-generation tensor cores (tcgen05, TF32).
+// tc_syrk.cuh -- F = X X^T on the 5th-generation tensor cores (tcgen05).
 //
 // X is L'^T scaled by sqrt(C^-1): M_cap rows (source cells) x K_cap columns
-// (image pixels), FP32, K contiguous, split into a TF32-rounded high part and
-// a TF32-rounded remainder so that hi*hi + hi*lo + lo*hi carries ~22 bits
-// (the "3xTF32" scheme).  One CTA computes one 128x128 tile of the lower
+// (image pixels), K contiguous, split into a rounded high part and a rounded
+// remainder so that hi*hi + hi*lo + lo*hi carries ~22 bits.  Two operand
+// types, one kernel: TF32 (FP32 storage, kind::tf32, K = 8 per MMA, 32 pixels
+// per 128-byte stage row) or F16 (kind::f16 at twice the tensor rate, K = 16
+// per MMA, 64 pixels per stage row; X scaled by a power of two so that its
+// largest entry is near 2^14, undone exactly in the epilogue).  Both have 11
+// significant bits per part.  One CTA computes one 128x128 tile of the lower
 // triangle of F:
-//   warp 0 / lane 0  TMA producer: 128x32 FP32 boxes (128 B rows, 128 B
-//                    swizzle) of X_hi, X_lo for the tile's row block and
-//                    column block into a 3-stage shared-memory ring;
+//   warp 0 / lane 0  TMA producer: 128-row boxes of 128 B (128 B swizzle) of
+//                    X_hi, X_lo for the tile's row block and column block
+//                    into a 3-stage shared-memory ring;
 //   warp 1 / lane 0  MMA issuer: 3 products x 4 k-steps of
-//                    tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=128, K=8)
-//                    per stage into a 128x128 FP32 accumulator in TMEM;
+//                    tcgen05.mma.cta_group::1 (M=128, N=128) per stage into a
+//                    128x128 FP32 accumulator in TMEM;
 //   all 4 warps      epilogue: tcgen05.ld 32x32b.x32, FP32 stores to F.
-// Block sparsity: a K block (32 pixels) is processed only if both the row
-// block and the column block of X have a nonzero there (flags from the
-// conversion kernel), so the work follows the overlap of the two source-cell
+// Block sparsity: a stage is processed only if both the row block and the
+// column block of X have a nonzero among its pixels (flags per 32 pixels from
+// the PSF-to-X build), so the work follows the overlap of the two source-cell
 // blocks' footprints in the image instead of the full pixel count.
 // Every mbarrier wait is bounded by ~1 s of %globaltimer; on expiry the
 // kernel raises QLP_ERR_TIMEOUT in the GridState, stops issuing work, frees
@@ -26,12 +30,16 @@ namespace qlpix {
 
 // grid: one CTA per lower-triangle 128x128 tile of the M_cap x M_cap output.
 // nzflags[rb * nkb_cap + kb] != 0 when rows [128 rb, 128 rb + 128) of X have a
-// nonzero in columns [32 kb, 32 kb + 32).
+// nonzero in columns [32 kb, 32 kb + 32).  HALF: F16 operands (64 pixels per
+// stage: flags 2 kb and 2 kb + 1); fscale multiplies the result (2^-2s for X
+// scaled by 2^s).
+template <bool HALF>
 __global__ void __launch_bounds__(128, 1) k_syrk_tc(const __grid_constant__ CUtensorMap map_hi,
                                                     const __grid_constant__ CUtensorMap map_lo,
                                                     GridState* gs, const unsigned char* __restrict__ nzflags,
-                                                    int nkb_cap, float* __restrict__ F, int ldF)
+                                                    int nkb_cap, float* __restrict__ F, int ldF, float fscale)
 {
+    constexpr int KPS = HALF ? 2 * TC_KB : TC_KB;      // pixels per stage (128 bytes of a row)
     extern __shared__ unsigned char smem_raw[];
     __shared__ uint64_t full_bar[TC_STAGES];
     __shared__ uint64_t empty_bar[TC_STAGES];
@@ -53,7 +61,7 @@ __global__ void __launch_bounds__(128, 1) k_syrk_tc(const __grid_constant__ CUte
     const int M = gs->M, N = gs->N;
     const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
     if (bi * TC_TILE >= Mp) return;
-    const int nkb = (N + TC_KB - 1) / TC_KB;
+    const int nkb = (N + KPS - 1) / KPS;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -83,31 +91,36 @@ __global__ void __launch_bounds__(128, 1) k_syrk_tc(const __grid_constant__ CUte
 
     const unsigned char* fi = nzflags + (size_t)bi * nkb_cap;
     const unsigned char* fj = nzflags + (size_t)bj * nkb_cap;
+    // stage kb has work when both blocks have a nonzero among its pixels
+    auto live = [&](int kb) -> bool {
+        if (HALF) return (fi[2 * kb] | fi[2 * kb + 1]) && (fj[2 * kb] | fj[2 * kb + 1]);
+        return fi[kb] && fj[kb];
+    };
 
     if (warp == 0 && lane == 0) {
         // ---- TMA producer ----
         int it = 0;
         for (int kb = 0; kb < nkb; kb++) {
-            if (!(fi[kb] && fj[kb])) continue;
+            if (!live(kb)) continue;
             const int s = it % TC_STAGES;
             if (it >= TC_STAGES) {
                 if (!mbar_wait_bounded(&empty_bar[s], ((it / TC_STAGES) & 1) ^ 1, &abort_flag)) break;
             }
             unsigned char* st = smem + s * TC_STAGE_BYTES;
             mbar_expect_tx(&full_bar[s], TC_STAGE_BYTES);
-            tma_load_2d(&map_hi, &full_bar[s], st, kb * TC_KB, bi * TC_TILE);
-            tma_load_2d(&map_lo, &full_bar[s], st + TC_TILE_BYTES, kb * TC_KB, bi * TC_TILE);
-            tma_load_2d(&map_hi, &full_bar[s], st + 2 * TC_TILE_BYTES, kb * TC_KB, bj * TC_TILE);
-            tma_load_2d(&map_lo, &full_bar[s], st + 3 * TC_TILE_BYTES, kb * TC_KB, bj * TC_TILE);
+            tma_load_2d(&map_hi, &full_bar[s], st, kb * KPS, bi * TC_TILE);
+            tma_load_2d(&map_lo, &full_bar[s], st + TC_TILE_BYTES, kb * KPS, bi * TC_TILE);
+            tma_load_2d(&map_hi, &full_bar[s], st + 2 * TC_TILE_BYTES, kb * KPS, bj * TC_TILE);
+            tma_load_2d(&map_lo, &full_bar[s], st + 3 * TC_TILE_BYTES, kb * KPS, bj * TC_TILE);
             it++;
         }
         n_issued = it;
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----
-        const uint32_t idesc = idesc_tf32_128x128();
+        const uint32_t idesc = HALF ? idesc_f16_128x128() : idesc_tf32_128x128();
         int it = 0;
         for (int kb = 0; kb < nkb; kb++) {
-            if (!(fi[kb] && fj[kb])) continue;
+            if (!live(kb)) continue;
             const int s = it % TC_STAGES;
             if (!mbar_wait_bounded(&full_bar[s], (it / TC_STAGES) & 1, &abort_flag)) break;
             tc_fence_after();
@@ -117,11 +130,18 @@ __global__ void __launch_bounds__(128, 1) k_syrk_tc(const __grid_constant__ CUte
             const uint64_t b_hi = sdesc_sw128(smem_u32(st + 2 * TC_TILE_BYTES));
             const uint64_t b_lo = sdesc_sw128(smem_u32(st + 3 * TC_TILE_BYTES));
             #pragma unroll
-            for (int kk = 0; kk < TC_KB / 8; kk++) {
-                const uint64_t off = (uint64_t)((kk * 32) >> 4);   // 8 TF32 = 32 bytes along K
-                mma_tf32(tmem, a_hi + off, b_hi + off, idesc, (it > 0 || kk > 0) ? 1u : 0u);
-                mma_tf32(tmem, a_hi + off, b_lo + off, idesc, 1u);
-                mma_tf32(tmem, a_lo + off, b_hi + off, idesc, 1u);
+            for (int kk = 0; kk < 4; kk++) {
+                // one MMA takes 32 bytes along K: 8 TF32 or 16 F16 values
+                const uint64_t off = (uint64_t)((kk * 32) >> 4);
+                if (HALF) {
+                    mma_f16(tmem, a_hi + off, b_hi + off, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                    mma_f16(tmem, a_hi + off, b_lo + off, idesc, 1u);
+                    mma_f16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+                } else {
+                    mma_tf32(tmem, a_hi + off, b_hi + off, idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                    mma_tf32(tmem, a_hi + off, b_lo + off, idesc, 1u);
+                    mma_tf32(tmem, a_lo + off, b_hi + off, idesc, 1u);
+                }
             }
             mma_commit(&empty_bar[s]);
             it++;
@@ -149,7 +169,8 @@ __global__ void __launch_bounds__(128, 1) k_syrk_tc(const __grid_constant__ CUte
             tmem_ld_32cols(taddr, v);
             #pragma unroll
             for (int i = 0; i < 32; i += 4)
-                *reinterpret_cast<float4*>(out + c + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                *reinterpret_cast<float4*>(out + c + i) =
+                    make_float4(v[i] * fscale, v[i + 1] * fscale, v[i + 2] * fscale, v[i + 3] * fscale);
         }
     } else {
         for (int c = 0; c < TC_TILE; c += 4) *reinterpret_cast<float4*>(out + c) = make_float4(0.f, 0.f, 0.f, 0.f);
