@@ -37,7 +37,7 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import numpy as np  # noqa: E402
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_syrk_tc launch on cfg2 (ncu, GB300)
-SYRK_TC_DRAM_BYTES_CFG2 = 268.482e6 + 11.716e6
+SYRK_TC_DRAM_BYTES_CFG2 = 115.223e6 + 9.662e6
 
 METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 at |ΔlogL|<0.1"
 UNIT = "evals/s"
