@@ -5,13 +5,38 @@
 
 namespace qlpix {
 
-// SPLE_Lens::deflection_angular_factor (models.cpp:336-351): the Tessore et
-// al. (2015) series for the core-free elliptical power law, complex products
-// written out as (ac - bd, ad + bc); |z|^2 through hypot like std::norm.
-__device__ __forceinline__ void sple_angular_factor(const LensRec& L, double phi, double& fr, double& fi)
+// Coefficients rho_i = f (beta i - 1) / (beta i + 1) of the Tessore series
+// for i = 1 .. SPLE_RHO_TAB, the same expression as in the series loop, so a
+// table filled once per CTA holds the bits the loop would compute.
+#define SPLE_RHO_TAB 48
+__device__ __forceinline__ double sple_rho(const LensRec& L, int i)
 {
     double beta = 2.0 / (2 - L.alpha);
     double ff = (1 - L.q) / (1 + L.q);
+    return ff * (beta * i - 1) / (beta * i + 1);
+}
+
+// The series' stopping test |o|^2 > 1e-16 |f|^2, |z|^2 as hypot(re, im)^2
+// (std::norm).  The plain sums of squares differ from those by a few ulp, so
+// they decide whenever they are clear of the threshold by a relative 1e-12;
+// only a near tie evaluates the hypot form -- the decision is the same.
+__device__ __forceinline__ bool sple_series_continues(double orr, double oi, double fr, double fi)
+{
+    const double A = orr * orr + oi * oi;
+    const double t = 1e-16 * (fr * fr + fi * fi);
+    if (A > t * (1.0 + 1e-12)) return true;
+    if (A < t * (1.0 - 1e-12)) return false;
+    const double a = hypot(orr, oi), c = hypot(fr, fi);
+    return a * a > 1e-16 * (c * c);
+}
+
+// SPLE_Lens::deflection_angular_factor (models.cpp:336-351): the Tessore et
+// al. (2015) series for the core-free elliptical power law, complex products
+// written out as (ac - bd, ad + bc).  rho_tab: rho_1 .. rho_SPLE_RHO_TAB for
+// this lens (sple_rho), or null.
+__device__ __forceinline__ void sple_angular_factor(const LensRec& L, double phi, double& fr, double& fi,
+                                                    const double* rho_tab)
+{
     double s1, c1;
     sincos(phi, &s1, &c1);
     fr = 1.0 * c1; fi = 1.0 * s1;
@@ -19,21 +44,19 @@ __device__ __forceinline__ void sple_angular_factor(const LensRec& L, double phi
     double s2, c2;
     sincos(2 * phi, &s2, &c2);
     int i = 1;
-    double nw, nf;
     do {
-        double rho = ff * (beta * i - 1) / (beta * i + 1);
+        const double rho = (rho_tab && i <= SPLE_RHO_TAB) ? rho_tab[i - 1] : sple_rho(L, i);
         double pr = -(rho * c2), pi = -(rho * s2);
         double nr = pr * orr - pi * oi;
         double ni = pr * oi + pi * orr;
         orr = nr; oi = ni;
         fr += orr; fi += oi;
         i++;
-        double a = hypot(orr, oi); nw = a * a;
-        double c = hypot(fr, fi);  nf = c * c;
-    } while (nw > 1e-16 * nf && i < 1000);
+    } while (sple_series_continues(orr, oi, fr, fi) && i < 1000);
 }
 
-__device__ __forceinline__ void sple_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+__device__ __forceinline__ void sple_deflection(const LensRec& L, double x, double y, double& dx, double& dy,
+                                                const double* rho_tab = nullptr)
 {
     if (L.kind == 1) {
         // SPLE_Lens::deflection_elliptical_iso (models.cpp:208-216)
@@ -53,7 +76,7 @@ __device__ __forceinline__ void sple_deflection(const LensRec& L, double x, doub
             phi = -phi;
         }
         double fr, fi;
-        sple_angular_factor(L, phi, fr, fi);
+        sple_angular_factor(L, phi, fr, fi, rho_tab);
         double scal = 2 * L.bprime * L.q / (1 + L.q) * pow(L.bprime / R, L.alpha - 1);
         dx = scal * fr;
         dy = scal * fi;
@@ -74,7 +97,8 @@ namespace qlpix {
 // LensProfile::deflection (profile.cpp:1782-1805); Shear::deflection (models.cpp:2266-2272).
 // NFW = false compiles the kernel without the quadrature (no NFW lens in the model).
 template <bool NFW>
-__device__ __forceinline__ void lens_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+__device__ __forceinline__ void lens_deflection(const LensRec& L, double x, double y, double& dx, double& dy,
+                                                const double* rho_tab = nullptr)
 {
     if (L.type == QLP_LENS_SHEAR) {
         x -= L.xc; y -= L.yc;
@@ -91,7 +115,7 @@ __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, doub
         x = xp;
     }
     double ax, ay;
-    if (!NFW || L.type == QLP_LENS_SPLE) sple_deflection(L, x, y, ax, ay);
+    if (!NFW || L.type == QLP_LENS_SPLE) sple_deflection(L, x, y, ax, ay, rho_tab);
     else nfw_deflection(L, x, y, ax, ay);
     if (rot) {
         double xp = ax * L.costheta - ay * L.sintheta;
@@ -101,9 +125,12 @@ __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, doub
     dx = ax; dy = ay;
 }
 
-// QLens::deflection + QLens::find_sourcept (lenscalc.cpp:81-113, 325-330)
+// QLens::deflection + QLens::find_sourcept (lenscalc.cpp:81-113, 325-330).
+// rho_tab: SPLE_RHO_TAB series coefficients per lens (lens k at k *
+// SPLE_RHO_TAB), or null.
 template <bool NFW>
-__device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, double y, double& bx, double& by)
+__device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, double y, double& bx, double& by,
+                                              const double* rho_tab = nullptr)
 {
     double defx = 0, defy = 0;
     double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
@@ -121,7 +148,7 @@ __device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, dou
             for (int k = 0; k < lm.nlens; k++) {
                 if (lm.lens[k].plane != i) continue;
                 double ax, ay;
-                lens_deflection<NFW>(lm.lens[k], xi, yi, ax, ay);
+                lens_deflection<NFW>(lm.lens[k], xi, yi, ax, ay, rho_tab ? rho_tab + k * SPLE_RHO_TAB : nullptr);
                 dsx[i] += ax; dsy[i] += ay;
             }
             dsx[i] *= lm.zfac[i];

@@ -18,12 +18,20 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd_, const EvalPara
                                                   double* __restrict__ spx, double* __restrict__ spy)
 {
     const StaticData sd = eval_shape(sd_);
-    // the lens model of this evaluation, staged in shared memory
+    // the lens model of this evaluation, staged in shared memory, and the
+    // power-law series coefficients of each lens (the same bits the series
+    // loop would compute; used only by core-free power laws)
     __shared__ __align__(16) LensModel lm;
+    __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
     {
         const double* src = reinterpret_cast<const double*>(&ep->lm);
         double* dst = reinterpret_cast<double*>(&lm);
         for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < lm.nlens * SPLE_RHO_TAB; e += blockDim.x) {
+        const LensRec& L = lm.lens[e / SPLE_RHO_TAB];
+        rho_tab[e] = (L.type == QLP_LENS_SPLE && L.kind == 2) ? sple_rho(L, e % SPLE_RHO_TAB + 1) : 0.0;
     }
     __syncthreads();
     const int ns = sd.nsplit, nsub = sd.nsub;
@@ -37,7 +45,7 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd_, const EvalPara
         double px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
         double py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
         double bx, by;
-        find_sourcept<NFW>(lm, px, py, bx, by);
+        find_sourcept<NFW>(lm, px, py, bx, by, rho_tab);
         spx[t] = bx;
         spy[t] = by;
     }
