@@ -334,8 +334,10 @@ void launch_build_L(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream
 {
     (void)so;
     if (sd.n_mask == 0) return;
-    int blocks = (sd.n_mask + 127) / 128;
-    k_build_L<<<blocks, 128, 0, st>>>(sd, w.rowidx, w.rowptr, w.cell3, w.w3, w.active_index, w.Lidx, w.Lval, w.cidx,
+    // a thread per masked pixel, each a long serial merge: 32-thread CTAs spread
+    // the few warps over all SMs
+    int blocks = (sd.n_mask + 31) / 32;
+    k_build_L<<<blocks, 32, 0, st>>>(sd, w.rowidx, w.rowptr, w.cell3, w.w3, w.active_index, w.Lidx, w.Lval, w.cidx,
                                       w.cval, w.ccnt);
     count_launches(1);
 }

@@ -55,7 +55,7 @@ struct MixedWork {
     double* r = nullptr;     // M
     double* z = nullptr;     // M
     double* y = nullptr;     // M (solve scratch)
-    double* part = nullptr;
+    double* img = nullptr;   // npix_pad: dense padded image for the FP64 convolutions
     float* linvF = nullptr;  // per 128-block of F: inverse of its diagonal factor, then its transpose
     float* linv128 = nullptr; // the same for R's current diagonal block
     float* yf = nullptr;     // M_cap: forward-solve result
@@ -579,7 +579,7 @@ void mixed_free(Slot& c)
 {
     MixedWork* m = mw_of(c);
     if (!m) return;
-    void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->part,
+    void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->img,
                     m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
                     m->sqc, m->col_u, m->src_u, m->colval64, m->pixT, m->F0};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -615,6 +615,7 @@ int mixed_init(Slot& c)
     A((void**)&m->colval, sizeof(float) * (size_t)m->nnz_cap);
     A((void**)&m->col_u, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->pixT, sizeof(int2) * (size_t)c.npix_pad);
+    A((void**)&m->img, sizeof(double) * (size_t)c.npix_pad);
     A((void**)&m->src_u, sizeof(int) * (size_t)m->nnz_cap);
     A((void**)&m->colval64, sizeof(double) * (size_t)m->nnz_cap);
     A((void**)&m->sqc, sizeof(float) * (size_t)(c.N_cap + 64));
@@ -736,7 +737,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         n += 4;
     }
     // D = L^T P^T (C^-1 d), FP64
-    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, st);
+    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, m->img, st);
     k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, w.D);
     n++;
     // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
@@ -826,8 +827,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         n += 3;
         if (it == refine) break;
         op_Ls(w, N_cap, w.s, m->t, st);
-        op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, st);
-        op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, st);
+        op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, m->img, st);
+        op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, m->img, st);
         k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, m->v);
         n++;
         k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, regp,
@@ -836,7 +837,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     }
     // model image P L s in FP64 for chi^2
     op_Ls(w, N_cap, w.s, m->t, st);
-    op_conv(sd, w, N_cap, false, m->t, nullptr, w.model, st);
+    op_conv(sd, w, N_cap, false, m->t, nullptr, w.model, m->img, st);
     count_launches(n);
     return QLP_OK;
 }

@@ -178,9 +178,7 @@ void launch_rowpix(const StaticData& sd, Work& w, cudaStream_t st);
 void launch_psf(const StaticData& sd, const SrcOpts& so, Work& w, int M_max, cudaStream_t st);
 void op_Ls(Work& w, int N_cap, const double* s, double* t, cudaStream_t st);
 void op_conv(const StaticData& sd, Work& w, int N_cap, bool transpose, const double* in, const double* scale_in,
-             double* out, cudaStream_t st);
-void op_LTw(Work& w, int N_cap, int M_cap, const double* v, double* part, double* out, cudaStream_t st);
-int ltw_chunks(int N_cap);
+             double* out, double* img, cudaStream_t st);
 void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st);
 void launch_D(Work& w, int N_max, int M_max, cudaStream_t st);
 void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st);
