@@ -47,7 +47,7 @@ static void free_work(Work& w)
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
                     w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep,
-                    w.fb_ray, w.fb_xy, w.fb_count, w.F0};
+                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
@@ -99,6 +99,8 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     CK(dalloc(&w.model, n_mask), "alloc");
     const size_t part = std::max((size_t)((n_mask + 255) / 256 + 1) * Mc, (size_t)Mc * 4);
     CK(dalloc(&w.partial, part), "alloc");
+    CK(dalloc(&w.gpart, 4 * 1024), "alloc"); CK(dalloc(&w.gpart_cnt, 1024), "alloc");
+    CK(dalloc(&w.cpart, 3 * 1025), "alloc");
     CK(dalloc(&w.linv, (size_t)Mc * 64), "alloc");
     CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc"); CK(dalloc(&w.ep, 1), "alloc");
     CK(dalloc(&w.fb_ray, n_sub), "alloc"); CK(dalloc(&w.fb_xy, 2 * n_sub), "alloc"); CK(dalloc(&w.fb_count, 1), "alloc");

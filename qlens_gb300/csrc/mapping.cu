@@ -7,6 +7,7 @@
 // bit.
 #include "qlpix_internal.h"
 #include <cfloat>
+#include <algorithm>
 
 namespace qlpix {
 
@@ -16,24 +17,27 @@ namespace qlpix {
 //   srcgrid_size_scale widening                    lens.cpp:12459-12470
 //   SourcePixelGrid::create_pixel_grid            pixelgrid.cpp:401-472 (x += xstep accumulation)
 //   SourcePixel ctor: centre = mean of 4 corners   pixelgrid.cpp:761-783
-// One block: a min/max reduction over the per-pixel mean source points, then
-// thread 0 lays out the corners sequentially.  The clamp to the sourcegrid
-// limits is order independent: bound = (extreme beyond limit) ? limit : extreme.
+// k_grid_partial: per block, the min/max of the per-pixel mean source points
+// (each mean summed in sub-pixel order) over a share of the masked pixels;
+// k_grid: one block combines the partials (min and max are exact in any
+// order) and thread 0 lays out the corners sequentially.  The clamp to the
+// sourcegrid limits is order independent: bound = (extreme beyond limit) ?
+// limit : extreme.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, const double* __restrict__ spx,
-                                               const double* __restrict__ spy, double* cx, double* cy,
-                                               double* ccx, double* ccy, GridState* gs)
+#define GRID_PARTS 1024
+__global__ void __launch_bounds__(256) k_grid_partial(StaticData sd_, SrcOpts so, const double* __restrict__ spx,
+                                                      const double* __restrict__ spy, double* __restrict__ part,
+                                                      int* __restrict__ part_cnt)
 {
     const StaticData sd = eval_shape(sd_);
-    const SrcOpts so = eval_grid(so_, sd_);
-    __shared__ double red[4][32];
-    __shared__ int cnt_s[32];
+    __shared__ double red[4][8];
+    __shared__ int cnt_s[8];
     double xmn = DBL_MAX, xmx = -DBL_MAX, ymn = DBL_MAX, ymx = -DBL_MAX;
     int cnt = 0;
     if (so.auto_grid) {
         const int nsub = sd.nsub;
         const bool use_nt = so.noise_threshold > 0;
-        for (int m = threadIdx.x; m < sd.n_mask; m += blockDim.x) {
+        for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
             if (use_nt) {
                 int pix = sd.mpix[m];
                 double noise = sqrt(1.0 / sd.covinv[pix]);
@@ -48,7 +52,6 @@ __global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, cons
             cnt++;
         }
     }
-    // block reduction
     for (int o = 16; o > 0; o >>= 1) {
         xmn = fmin(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
         xmx = fmax(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
@@ -64,6 +67,37 @@ __global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, cons
             xmn = fmin(xmn, red[0][k]); xmx = fmax(xmx, red[1][k]);
             ymn = fmin(ymn, red[2][k]); ymx = fmax(ymx, red[3][k]);
             cnt += cnt_s[k];
+        }
+        part[4 * blockIdx.x] = xmn; part[4 * blockIdx.x + 1] = xmx;
+        part[4 * blockIdx.x + 2] = ymn; part[4 * blockIdx.x + 3] = ymx;
+        part_cnt[blockIdx.x] = cnt;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, int nparts,
+                                               const double* __restrict__ part, double* cx, double* cy,
+                                               double* ccx, double* ccy, GridState* gs)
+{
+    const SrcOpts so = eval_grid(so_, sd_);
+    __shared__ double red[4][32];
+    double xmn = DBL_MAX, xmx = -DBL_MAX, ymn = DBL_MAX, ymx = -DBL_MAX;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+        xmn = fmin(xmn, part[4 * k]); xmx = fmax(xmx, part[4 * k + 1]);
+        ymn = fmin(ymn, part[4 * k + 2]); ymx = fmax(ymx, part[4 * k + 3]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        xmn = fmin(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
+        xmx = fmax(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
+        ymn = fmin(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
+        ymx = fmax(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (lane == 0) { red[0][warp] = xmn; red[1][warp] = xmx; red[2][warp] = ymn; red[3][warp] = ymx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < nw; k++) {
+            xmn = fmin(xmn, red[0][k]); xmx = fmax(xmx, red[1][k]);
+            ymn = fmin(ymn, red[2][k]); ymx = fmax(ymx, red[3][k]);
         }
         double gxmin, gxmax, gymin, gymax;
         if (so.auto_grid) {
@@ -98,8 +132,10 @@ __global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, cons
 
 void launch_grid(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream_t st)
 {
-    k_grid<<<1, 1024, 0, st>>>(sd, so, w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.gs);
-    count_launches(1);
+    const int nparts = std::max(1, std::min(GRID_PARTS, (sd.n_mask + 255) / 256));
+    k_grid_partial<<<nparts, 256, 0, st>>>(sd, so, w.spx, w.spy, w.gpart, w.gpart_cnt);
+    k_grid<<<1, 1024, 0, st>>>(sd, so, nparts, w.gpart, w.cx, w.cy, w.ccx, w.ccy, w.gs);
+    count_launches(2);
 }
 
 // ---------------------------------------------------------------------------
@@ -209,68 +245,128 @@ __device__ int block_exclusive_scan(int v, int* warp_tot)
     return base + x - v;
 }
 
-__global__ void __launch_bounds__(1024) k_compact(StaticData sd_, SrcOpts so_, const int* __restrict__ mapped,
-                                                  int* __restrict__ active_index, const int* __restrict__ cell3,
-                                                  const int* __restrict__ pixmaps, int* __restrict__ rowidx,
-                                                  int* __restrict__ pixindex, int* __restrict__ rowptr,
-                                                  GridState* gs)
+// The compaction runs on COMPACT_BLOCKS-way contiguous shares of the cells and
+// of the masked pixels: k_compact_count counts, per share, the mapped cells,
+// the active pixels and their L entries; k_compact_scan turns the counts into
+// exclusive offsets (one block) and sets M, N, nnz; k_compact_write scans
+// within each share and writes.  Shares and offsets keep the order.
+__device__ __forceinline__ void compact_share(int len, int nshare, int b, int& b0, int& b1)
 {
-    __shared__ int wt[33];
-    __shared__ int tot_s;
+    const int per = (len + nshare - 1) / nshare;
+    b0 = min(len, b * per);
+    b1 = min(len, b0 + per);
+}
+
+__device__ __forceinline__ int pixel_entries(const int* __restrict__ cell3, int m, int nsub)
+{
+    int e = 0;
+    for (int k = 0; k < nsub; k++) e += (cell3[3 * (m * nsub + k)] >= 0) ? 3 : 0;
+    return e;
+}
+
+__global__ void __launch_bounds__(256) k_compact_count(StaticData sd_, SrcOpts so_, const int* __restrict__ mapped,
+                                                       const int* __restrict__ cell3,
+                                                       const int* __restrict__ pixmaps, int* __restrict__ cpart)
+{
     const StaticData sd = eval_shape(sd_);
     const SrcOpts so = eval_grid(so_, sd_);
-    const int T = blockDim.x;
-    // ---- source cells ----
-    const int ncell = so.snx * so.sny;
-    int chunk = (ncell + T - 1) / T;
-    int b0 = threadIdx.x * chunk, b1 = min(b0 + chunk, ncell);
-    int c = 0;
-    for (int k = b0; k < b1; k++) c += mapped[k] ? 1 : 0;
-    int off = block_exclusive_scan(c, wt);
-    if (threadIdx.x == 0) tot_s = wt[32];
-    for (int k = b0; k < b1; k++) active_index[k] = mapped[k] ? off++ : -1;
-    __syncthreads();
-    const int M = tot_s;
-    __syncthreads();
-    // ---- image pixels and L row pointers ----
-    const int nm = sd.n_mask, nsub = sd.nsub;
-    chunk = (nm + T - 1) / T;
-    b0 = threadIdx.x * chunk; b1 = min(b0 + chunk, nm);
-    c = 0;
-    int e = 0;
-    for (int m = b0; m < b1; m++) {
-        if (pixmaps[m]) {
-            c++;
-            for (int k = 0; k < nsub; k++) e += (cell3[3 * (m * nsub + k)] >= 0) ? 3 : 0;
-        }
+    __shared__ int red[3][8];
+    const int nshare = gridDim.x, b = blockIdx.x;
+    int c0, c1, p0, p1;
+    compact_share(so.snx * so.sny, nshare, b, c0, c1);
+    compact_share(sd.n_mask, nshare, b, p0, p1);
+    int nc = 0, np = 0, ne = 0;
+    for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) nc += mapped[k] ? 1 : 0;
+    for (int m = p0 + threadIdx.x; m < p1; m += blockDim.x)
+        if (pixmaps[m]) { np++; ne += pixel_entries(cell3, m, sd.nsub); }
+    for (int o = 16; o > 0; o >>= 1) {
+        nc += __shfl_xor_sync(0xffffffffu, nc, o);
+        np += __shfl_xor_sync(0xffffffffu, np, o);
+        ne += __shfl_xor_sync(0xffffffffu, ne, o);
     }
-    int roff = block_exclusive_scan(c, wt);
-    if (threadIdx.x == 0) tot_s = wt[32];
-    __syncthreads();
-    const int N = tot_s;
-    __syncthreads();
-    int eoff = block_exclusive_scan(e, wt);
-    if (threadIdx.x == 0) tot_s = wt[32];
-    for (int m = b0; m < b1; m++) {
-        int pix = sd.mpix[m];
-        if (pixmaps[m]) {
-            rowidx[m] = roff;
-            pixindex[pix] = roff;
-            rowptr[roff] = eoff;
-            roff++;
-            for (int k = 0; k < nsub; k++) eoff += (cell3[3 * (m * nsub + k)] >= 0) ? 3 : 0;
-        } else {
-            rowidx[m] = -1;
-            pixindex[pix] = -1;
-        }
-    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red[0][warp] = nc; red[1][warp] = np; red[2][warp] = ne; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        rowptr[N] = tot_s;
+        int a0 = 0, a1 = 0, a2 = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { a0 += red[0][k]; a1 += red[1][k]; a2 += red[2][k]; }
+        cpart[b] = a0;
+        cpart[1025 + b] = a1;
+        cpart[2050 + b] = a2;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_compact_scan(int nshare, int* __restrict__ cpart, int* __restrict__ rowptr,
+                                                       GridState* gs)
+{
+    __shared__ int wt[33];
+    __shared__ int tot[3];
+    for (int a = 0; a < 3; a++) {
+        int* v = cpart + 1025 * a;
+        const int x = (threadIdx.x < nshare) ? v[threadIdx.x] : 0;
+        const int off = block_exclusive_scan(x, wt);
+        if (threadIdx.x == 0) tot[a] = wt[32];
+        __syncthreads();
+        if (threadIdx.x < nshare) v[threadIdx.x] = off;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int M = tot[0], N = tot[1];
+        rowptr[N] = tot[2];
         gs->M = M;
         gs->N = N;
-        gs->nnz = tot_s;
+        gs->nnz = tot[2];
         if (M == 0) gs->status = QLP_ERR_NO_SOURCE_PIXELS;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_compact_write(StaticData sd_, SrcOpts so_, const int* __restrict__ mapped,
+                                                       int* __restrict__ active_index, const int* __restrict__ cell3,
+                                                       const int* __restrict__ pixmaps, int* __restrict__ rowidx,
+                                                       int* __restrict__ pixindex, int* __restrict__ rowptr,
+                                                       const int* __restrict__ cpart)
+{
+    const StaticData sd = eval_shape(sd_);
+    const SrcOpts so = eval_grid(so_, sd_);
+    __shared__ int wt[33];
+    const int nshare = gridDim.x, b = blockIdx.x, T = blockDim.x;
+    // ---- source cells: active index in cell order ----
+    {
+        int c0, c1;
+        compact_share(so.snx * so.sny, nshare, b, c0, c1);
+        const int chunk = (c1 - c0 + T - 1) / T;
+        const int k0 = min(c1, c0 + (int)threadIdx.x * chunk), k1 = min(c1, k0 + chunk);
+        int c = 0;
+        for (int k = k0; k < k1; k++) c += mapped[k] ? 1 : 0;
+        int off = cpart[b] + block_exclusive_scan(c, wt);
+        for (int k = k0; k < k1; k++) active_index[k] = mapped[k] ? off++ : -1;
+    }
+    __syncthreads();
+    // ---- image pixels: active rows in masked-pixel order, L row pointers ----
+    {
+        int p0, p1;
+        compact_share(sd.n_mask, nshare, b, p0, p1);
+        const int chunk = (p1 - p0 + T - 1) / T;
+        const int m0 = min(p1, p0 + (int)threadIdx.x * chunk), m1 = min(p1, m0 + chunk);
+        int c = 0, e = 0;
+        for (int m = m0; m < m1; m++)
+            if (pixmaps[m]) { c++; e += pixel_entries(cell3, m, sd.nsub); }
+        int roff = cpart[1025 + b] + block_exclusive_scan(c, wt);
+        __syncthreads();
+        int eoff = cpart[2050 + b] + block_exclusive_scan(e, wt);
+        for (int m = m0; m < m1; m++) {
+            const int pix = sd.mpix[m];
+            if (pixmaps[m]) {
+                rowidx[m] = roff;
+                pixindex[pix] = roff;
+                rowptr[roff] = eoff;
+                roff++;
+                eoff += pixel_entries(cell3, m, sd.nsub);
+            } else {
+                rowidx[m] = -1;
+                pixindex[pix] = -1;
+            }
+        }
     }
 }
 
@@ -278,9 +374,12 @@ void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream
 {
     // pixels outside the mask keep -1 in pixindex
     cudaMemsetAsync(w.pixindex, 0xff, sizeof(int) * sd.nx * sd.ny, st);
-    k_compact<<<1, 1024, 0, st>>>(sd, so, w.mapped, w.active_index, w.cell3, w.pixmaps, w.rowidx, w.pixindex,
-                                  w.rowptr, w.gs);
-    count_launches(1);
+    const int nshare = std::max(1, std::min(1024, std::max((sd.n_mask + 255) / 256, (so.snx * so.sny + 255) / 256)));
+    k_compact_count<<<nshare, 256, 0, st>>>(sd, so, w.mapped, w.cell3, w.pixmaps, w.cpart);
+    k_compact_scan<<<1, 1024, 0, st>>>(nshare, w.cpart, w.rowptr, w.gs);
+    k_compact_write<<<nshare, 256, 0, st>>>(sd, so, w.mapped, w.active_index, w.cell3, w.pixmaps, w.rowidx,
+                                            w.pixindex, w.rowptr, w.cpart);
+    count_launches(3);
 }
 
 // ---------------------------------------------------------------------------

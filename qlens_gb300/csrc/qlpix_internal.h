@@ -153,6 +153,8 @@ struct Work {
     double* s;   double* tmp;          // M
     double* model;                     // N
     double* partial;                   // reduction scratch
+    double* gpart;  int* gpart_cnt;    // source-grid bounds: per-block partials (1024 blocks at most)
+    int* cpart;                        // compaction: per-block counts (3 x 1025)
     double* linv;                      // 64x64 inverse of the current diagonal Cholesky block
     GridState* gs;
     EvalOut* out;                      // this slot's result (copied to the host after each evaluation)
