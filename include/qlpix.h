@@ -255,6 +255,13 @@ int qlp_brent_min(double (*f)(double x, void* user), void* user, double ax, doub
  * in the reference (it solves in FP64). */
 int qlp_set_refinement(qlp_ctx* ctx, int sweeps);
 
+/* QLens 'include_noise_term_in_loglike on' (commands.cpp:13597-13603,
+ * lens.cpp:13033-13043; default off, lens.cpp:303): -2 log(evidence) gains minus the log of C^-1 summed over the
+ * active pixels (noise map) or the masked-pixel count times log(1/sigma^2)
+ * (uniform noise), plus the masked-pixel count times log(2 pi).  Replaces the
+ * reference's QLens::include_noise_term_in_loglike flag (qlens.h:402). */
+int qlp_set_noise_term(qlp_ctx* ctx, int on);
+
 /* Number of doubles in one lens-parameter vector for the current model. */
 int qlp_n_params(const qlp_ctx* ctx);
 

@@ -52,6 +52,7 @@ def lib():
         _lib.oracle_get.argtypes = [C.c_char_p, C.c_void_p, C.c_long]
         _lib.oracle_threads.restype = C.c_int
         _lib.oracle_set_regopt.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
+        _lib.oracle_set_noise_term.argtypes = [C.c_int]
         _lib.oracle_brent_min.restype = C.c_double
         _lib.oracle_brent_min.argtypes = [BRENT_FN, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int,
                                           C.POINTER(C.c_int)]
@@ -79,10 +80,13 @@ def get(name):
     return out
 
 
-def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.0, planes=None, regopt=None):
+def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.0, planes=None, regopt=None,
+             noise_term=False):
     """Run the oracle; returns the qlp_result as a dict.  regopt: None, or
-    (minlog, maxlog, tol, max_iter) for QLens's 'optimize_regparam on'."""
+    (minlog, maxlog, tol, max_iter) for QLens's 'optimize_regparam on';
+    noise_term: QLens's 'include_noise_term_in_loglike on'."""
     L = lib()
+    L.oracle_set_noise_term(1 if noise_term else 0)
     if regopt is None:
         L.oracle_set_regopt(0, -3.0, 5.0, 0.01, 20)
     else:

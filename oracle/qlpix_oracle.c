@@ -374,6 +374,10 @@ double oracle_brent_min(double (*f)(double, void*), void* user, double ax, doubl
     return x;
 }
 
+/* 'include_noise_term_in_loglike on' (lens.cpp:303 default off) */
+static int g_noise_term = 0;
+void oracle_set_noise_term(int on) { g_noise_term = on; }
+
 /* 'optimize_regparam on' settings (lens.cpp:421-425 defaults) */
 static struct { int on; double minlog, maxlog, tol; int maxit; } g_regopt = {0, -3.0, 5.0, 0.01, 20};
 
@@ -826,6 +830,17 @@ int oracle_eval(const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts*
         loglike += logdetF;
     }
     loglike += chisq0;
+    /* the pixel noise term (lens.cpp:13033-13043): minus log C^-1 of each active
+       pixel in turn (noise map) or of the uniform noise times the masked-pixel
+       count, plus the masked-pixel count times log(2 pi) */
+    if (g_noise_term) {
+        if (use_noise_map) {
+            for (int r = 0; r < npix; r++) loglike -= log(cvec[r]);
+        } else {
+            loglike -= n_mask * log(cov_inverse);
+        }
+        loglike += n_mask * log(6.28318530717958647692);
+    }
 
     out->chisq0 = chisq0;
     out->logdet_F = logdetF;

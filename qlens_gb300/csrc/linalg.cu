@@ -263,9 +263,9 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
     const StaticData sd = eval_shape(sd_);
     const SrcOpts so = eval_grid(so_, sd_);
     const double regparam = *regp;
-    __shared__ double red[3][32];
+    __shared__ double red[4][32];
     const int M = gs->M;
-    double chi = 0, es = 0, chi_act = 0;
+    double chi = 0, es = 0, chi_act = 0, logc = 0;
     for (int m = threadIdx.x; m < sd.n_mask; m += blockDim.x) {
         const int pix = sd.mpix[m];
         const double c = sd.use_noise_map ? sd.covinv[pix] : sd.cov_inverse;
@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
         double dd = (r >= 0) ? model[r] - sd.data[pix] : sd.data[pix];
         chi += dd * dd * c;
         if (r >= 0) chi_act += dd * dd * c;     // the pixels the lambda optimisation's chi^2 runs over
+        if (r >= 0 && sd.noise_term && sd.use_noise_map) logc += log(c);
     }
     if (so.regularization && regparam != 0) {
         const int snx = so.snx, sny = so.sny;
@@ -297,16 +298,20 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
         chi += __shfl_xor_sync(0xffffffffu, chi, o);
         es += __shfl_xor_sync(0xffffffffu, es, o);
         chi_act += __shfl_xor_sync(0xffffffffu, chi_act, o);
+        logc += __shfl_xor_sync(0xffffffffu, logc, o);
     }
     if ((threadIdx.x & 31) == 0) {
         red[0][threadIdx.x >> 5] = chi;
         red[1][threadIdx.x >> 5] = es;
         red[2][threadIdx.x >> 5] = chi_act;
+        red[3][threadIdx.x >> 5] = logc;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double c2 = 0, e2 = 0, ca = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { c2 += red[0][k]; e2 += red[1][k]; ca += red[2][k]; }
+        double c2 = 0, e2 = 0, ca = 0, lc = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+            c2 += red[0][k]; e2 += red[1][k]; ca += red[2][k]; lc += red[3][k];
+        }
         double regterms = 0, loglike = 0;
         if (so.regularization && M > 0) {
             if (regparam != 0) {
@@ -316,6 +321,14 @@ __global__ void __launch_bounds__(1024) k_final(StaticData sd_, SrcOpts so_, con
             loglike += out->logdet_F;
         }
         loglike += c2;
+        // the pixel-noise normalisation, QLens 'include_noise_term_in_loglike'
+        // (lens.cpp:13033-13043): minus the log of C^-1 over the active pixels
+        // with a noise map, or the masked-pixel count times log(1/sigma^2)
+        // without one, plus the masked-pixel count times log(2 pi)
+        if (sd.noise_term) {
+            loglike -= sd.use_noise_map ? lc : sd.n_mask * log(sd.cov_inverse);
+            loglike += sd.n_mask * log(6.28318530717958647692);
+        }
         int status = gs->status;
         if (status == 0 && (gs->not_spd_F || gs->not_spd_R)) status = QLP_ERR_NOT_SPD;
         // QLens::chisq_regparam_dense (pixelgrid.cpp:16688-16692): Ed + prior + log det F

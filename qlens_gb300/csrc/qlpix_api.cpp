@@ -253,6 +253,14 @@ int qlp_set_refinement(qlp_ctx* c, int sweeps)
     return QLP_OK;
 }
 
+int qlp_set_noise_term(qlp_ctx* c, int on)
+{
+    if (!c) return fail(QLP_ERR_ARG, "null context");
+    c->sd.noise_term = on ? 1 : 0;
+    c->graph_gen++;     // the flag is a launch argument of the captured final reduction
+    return QLP_OK;
+}
+
 int qlp_last_transfer_bytes(const qlp_ctx* c, long long* h2d, long long* d2h)
 {
     if (!c || !h2d || !d2h) return fail(QLP_ERR_ARG, "bad arguments");

@@ -79,6 +79,7 @@ struct StaticData {            // per-context, uploaded once
     int pnx, pny;              // PSF size
     int use_noise_map;
     double cov_inverse;        // uniform 1/sigma^2 when !use_noise_map
+    int noise_term;            // add the pixel-noise normalisation to -2 log(evidence)
     const double* xvals;       // nx+1
     const double* yvals;       // ny+1
     const double* data;        // nx*ny

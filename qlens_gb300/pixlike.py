@@ -62,6 +62,7 @@ def load_library(build_if_missing=False):
     L.qlp_last_launch_count.argtypes = [C.c_void_p]
     L.qlp_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_refinement.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_set_noise_term.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_regparam_optimization.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
     L.qlp_brent_min.argtypes = [BRENT_FN, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double),
                                 P(C.c_int)]
@@ -234,6 +235,11 @@ class PixelLikelihood:
     def set_refinement(self, sweeps):
         """FP64 refinement sweeps of the mixed path (0..4, default 1)."""
         self._check(self.lib.qlp_set_refinement(self.ctx, int(sweeps)))
+
+    def set_noise_term(self, on):
+        """QLens's 'include_noise_term_in_loglike': add the pixel-noise
+        normalisation to -2 log(evidence)."""
+        self._check(self.lib.qlp_set_noise_term(self.ctx, 1 if on else 0))
 
     def last_transfer_bytes(self):
         """(host->device, device->host) bytes moved by the last call."""

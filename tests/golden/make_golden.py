@@ -241,6 +241,17 @@ for _base in ("tiny_sie", "powerlaw"):
     CASES["regopt_" + _base] = dict(CASES[_base], script=CASES[_base]["script"].replace(
         "inversion_method dense\n", "inversion_method dense\noptimize_regparam on\n"))
 assert all("optimize_regparam on" in CASES[k]["script"] for k in ("regopt_tiny_sie", "regopt_powerlaw"))
+# 'include_noise_term_in_loglike on': -2 log(evidence) gains the pixel noise
+# normalisation (lens.cpp:13033-13043).  Uniform noise without a noise map:
+# with a noise map the reference reads imgpixel_covinv_vector after
+# clear_pixel_matrices has freed it (pixelgrid.cpp:13107-13119) and crashes.
+# Without one its dense D loop reads an OpenMP-private covinv that is never
+# initialised (pixelgrid.cpp:15637-15653), so D, s and the model come out zero;
+# tests/test_noise_term.py pins the noise term from its scalars regardless.
+CASES["noise_tiny_sie"] = dict(CASES["tiny_sie"], script=CASES["tiny_sie"]["script"].replace(
+    "inversion_method dense\n", "inversion_method dense\ninclude_noise_term_in_loglike on\n").replace(
+    "sbmap generate_uniform_noisemap\n", ""))
+assert "include_noise_term_in_loglike on" in CASES["noise_tiny_sie"]["script"]
 
 ARRAYS_F64 = ["zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
               "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
