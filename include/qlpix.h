@@ -262,6 +262,51 @@ int qlp_set_refinement(qlp_ctx* ctx, int sweeps);
  * reference's QLens::include_noise_term_in_loglike flag (qlens.h:402). */
 int qlp_set_noise_term(qlp_ctx* ctx, int on);
 
+/* ---- FITS input (the reference reads these through CFITSIO; this library
+ * carries its own reader of FITS image HDUs: BITPIX 8/16/32/64/-32/-64,
+ * BSCALE/BZERO).  Pixel (i, j), i along FITS axis 1 and j along axis 2, goes
+ * to [i * ny + j].  No device is needed. ---- */
+typedef struct {
+    int bitpix, naxis;
+    int has_pxsize, has_pxnoise, has_psfsig, has_zsrc, has_zlens;
+    double pxsize;   /* PXSIZE: square pixel size (arcsec) */
+    double pxnoise;  /* PXNOISE: uniform pixel noise */
+    double psfsig;   /* PSFSIG: Gaussian PSF width */
+    double zsrc, zlens;
+} qlp_fits_info;
+
+/* The 2-D image of HDU `hdu` (1 = primary) and the header keywords QLens
+ * reads from data images (pixelgrid.cpp:6059-6116).  pix == NULL: sizes and
+ * keywords only. */
+int qlp_fits_read_image(const char* path, int hdu, double* pix, long cap, int* nx, int* ny, qlp_fits_info* info);
+
+/* 'sbmap loadimg <file.fits>': ImagePixelData::load_data_fits
+ * (pixelgrid.cpp:6016-6283).  The pixel grid: square pixels of the file's
+ * PXSIZE, else of pixel_size (> 0; QLens 'data_pixel_size'), centred on the
+ * origin; else the bounds [xmin, xmax] x [ymin, ymax] (QLens 'grid').  xvals
+ * and yvals get nx + 1 and ny + 1 pixel edges.  All three outputs NULL: sizes
+ * and keywords only. */
+int qlp_load_data_fits(const char* path, int hdu, double pixel_size, double xmin, double xmax, double ymin,
+                       double ymax, double* xvals, double* yvals, double* data, long cap, int* nx, int* ny,
+                       qlp_fits_info* info);
+
+/* 'sbmap loadmask <file.fits> [-add]': ImagePixelData::load_mask_fits
+ * (pixelgrid.cpp:6512-6650) on the current mask (in/out, nx * ny): zero
+ * pixels leave the mask (unless add), others join it; a smaller file is
+ * centred on the image, a larger one is an error. */
+int qlp_load_mask_fits(const char* path, int nx, int ny, int add, unsigned char* mask, int* n_in_mask);
+
+/* 'sbmap loadnoisemap': ImagePixelData::load_noise_map_fits
+ * (pixelgrid.cpp:6344-6430): covinv = 1/sigma^2 per pixel; noise_min gets
+ * the smallest sigma. */
+int qlp_load_noise_map_fits(const char* path, int hdu, int nx, int ny, double* covinv, double* noise_min);
+
+/* 'sbmap loadpsf <file.fits>': QLens::load_psf_fits (pixelgrid.cpp:6737-6870):
+ * the symmetric box about the central pixel holding every pixel above
+ * threshold x peak (QLens 'psf_threshold', default 0.01), normalised to unit
+ * sum.  psf == NULL: sizes only. */
+int qlp_load_psf_fits(const char* path, double threshold, double* psf, long cap, int* pnx, int* pny);
+
 /* Number of doubles in one lens-parameter vector for the current model. */
 int qlp_n_params(const qlp_ctx* ctx);
 

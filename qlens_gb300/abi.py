@@ -94,6 +94,15 @@ class qlp_tune_report(C.Structure):
                 "trials": [dict(self.trial[i].as_dict(), ms=self.trial_ms[i]) for i in range(n)]}
 
 
+class qlp_fits_info(C.Structure):
+    _fields_ = [("bitpix", C.c_int), ("naxis", C.c_int), ("has_pxsize", C.c_int), ("has_pxnoise", C.c_int),
+                ("has_psfsig", C.c_int), ("has_zsrc", C.c_int), ("has_zlens", C.c_int), ("pxsize", C.c_double),
+                ("pxnoise", C.c_double), ("psfsig", C.c_double), ("zsrc", C.c_double), ("zlens", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class qlp_surrogate_opts(C.Structure):
     _fields_ = [("n_train", C.c_int), ("batch", C.c_int), ("steps", C.c_int), ("lr", C.c_double),
                 ("seed", C.c_ulonglong)]

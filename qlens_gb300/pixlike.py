@@ -80,6 +80,14 @@ def load_library(build_if_missing=False):
                                            P(C.c_double), P(C.c_float)]
     L.qlp_surrogate_eval.argtypes = [C.c_int, P(C.c_double), C.c_int, P(C.c_double), P(C.c_double),
                                      P(C.c_double), P(C.c_double)]
+    L.qlp_fits_read_image.argtypes = [C.c_char_p, C.c_int, P(C.c_double), C.c_long, P(C.c_int), P(C.c_int),
+                                      P(abi.qlp_fits_info)]
+    L.qlp_load_data_fits.argtypes = [C.c_char_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     P(C.c_double), P(C.c_double), P(C.c_double), C.c_long, P(C.c_int), P(C.c_int),
+                                     P(abi.qlp_fits_info)]
+    L.qlp_load_mask_fits.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, P(C.c_ubyte), P(C.c_int)]
+    L.qlp_load_noise_map_fits.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
+    L.qlp_load_psf_fits.argtypes = [C.c_char_p, C.c_double, P(C.c_double), C.c_long, P(C.c_int), P(C.c_int)]
     L.qlp_last_error.restype = C.c_char_p
     L.qlp_destroy.argtypes = [C.c_void_p]
     _lib = L
@@ -409,3 +417,74 @@ def brent_min(f, ax, bx, tol, max_iter):
     if code != abi.QLP_OK:
         raise QLPixError(code, L.qlp_last_error().decode())
     return x.value, n.value, pts
+
+
+# ---- FITS input: the reference's 'sbmap loadimg / loadmask / loadnoisemap /
+# loadpsf' (pixelgrid.cpp:6016-6870), through the library's own reader.
+# Arrays are indexed [i, j] with i along FITS axis 1 (x) and j along axis 2.
+
+def _fits_call(L, code):
+    if code != abi.QLP_OK:
+        raise QLPixError(code, L.qlp_last_error().decode())
+
+
+def fits_read_image(path, hdu=1):
+    """The 2-D image of HDU `hdu` (1 = primary) as an (nx, ny) array, and the
+    header keywords QLens reads (PXSIZE, PXNOISE, PSFSIG, ZSRC, ZLENS)."""
+    L = load_library()
+    nx, ny, info = C.c_int(), C.c_int(), abi.qlp_fits_info()
+    _fits_call(L, L.qlp_fits_read_image(os.fsencode(path), int(hdu), None, 0, C.byref(nx), C.byref(ny),
+                                        C.byref(info)))
+    out = np.empty((nx.value, ny.value))
+    _fits_call(L, L.qlp_fits_read_image(os.fsencode(path), int(hdu), _dp(out), out.size, C.byref(nx), C.byref(ny),
+                                        None))
+    return out, info.as_dict()
+
+
+def load_data_fits(path, hdu=1, pixel_size=0.0, bounds=None):
+    """'sbmap loadimg <file.fits>' (ImagePixelData::load_data_fits): returns
+    (xvals, yvals, data[nx, ny], keywords).  Square pixels of the file's
+    PXSIZE, else of pixel_size (> 0, QLens 'data_pixel_size'), centred on the
+    origin; otherwise bounds = (xmin, xmax, ymin, ymax), QLens's 'grid'."""
+    L = load_library()
+    b = bounds if bounds is not None else (0.0, 0.0, 0.0, 0.0)
+    nx, ny, info = C.c_int(), C.c_int(), abi.qlp_fits_info()
+    args = (os.fsencode(path), int(hdu), float(pixel_size), float(b[0]), float(b[1]), float(b[2]), float(b[3]))
+    _fits_call(L, L.qlp_load_data_fits(*args, None, None, None, 0, C.byref(nx), C.byref(ny), C.byref(info)))
+    xv, yv = np.empty(nx.value + 1), np.empty(ny.value + 1)
+    data = np.empty((nx.value, ny.value))
+    _fits_call(L, L.qlp_load_data_fits(*args, _dp(xv), _dp(yv), _dp(data), data.size, C.byref(nx), C.byref(ny),
+                                       None))
+    return xv, yv, data, info.as_dict()
+
+
+def load_mask_fits(path, mask, add=False):
+    """'sbmap loadmask <file.fits> [-add]' applied to `mask` (bool or uint8
+    array [nx, ny]); returns the new mask as uint8."""
+    L = load_library()
+    m = np.ascontiguousarray(mask, dtype=np.uint8).copy()
+    n = C.c_int()
+    _fits_call(L, L.qlp_load_mask_fits(os.fsencode(path), m.shape[0], m.shape[1], 1 if add else 0,
+                                       m.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(n)))
+    return m
+
+
+def load_noise_map_fits(path, shape, hdu=1):
+    """'sbmap loadnoisemap <file.fits>': returns (covinv[nx, ny], smallest sigma)."""
+    L = load_library()
+    cov = np.empty(shape)
+    mn = C.c_double()
+    _fits_call(L, L.qlp_load_noise_map_fits(os.fsencode(path), int(hdu), shape[0], shape[1], _dp(cov), C.byref(mn)))
+    return cov, mn.value
+
+
+def load_psf_fits(path, psf_threshold=0.01):
+    """'sbmap loadpsf <file.fits>' (QLens::load_psf_fits): the thresholded,
+    symmetric, unit-sum PSF matrix [pnx, pny]."""
+    L = load_library()
+    pnx, pny = C.c_int(), C.c_int()
+    _fits_call(L, L.qlp_load_psf_fits(os.fsencode(path), float(psf_threshold), None, 0, C.byref(pnx), C.byref(pny)))
+    psf = np.empty((pnx.value, pny.value))
+    _fits_call(L, L.qlp_load_psf_fits(os.fsencode(path), float(psf_threshold), _dp(psf), psf.size, C.byref(pnx),
+                                      C.byref(pny)))
+    return psf

@@ -253,6 +253,62 @@ CASES["noise_tiny_sie"] = dict(CASES["tiny_sie"], script=CASES["tiny_sie"]["scri
     "sbmap generate_uniform_noisemap\n", ""))
 assert "include_noise_term_in_loglike on" in CASES["noise_tiny_sie"]["script"]
 
+# FITS input through the reference's own loaders (ImagePixelData::load_data_fits,
+# load_mask_fits, QLens::load_psf_fits), run by the harness built against the
+# CFITSIO stand-in (oracle/fitsio_shim).  fits_synth: this repository's
+# fixtures (tests/golden/fits, written by make_fits.py: a 32-bit float image in
+# HDU 2 with PXSIZE/PXNOISE cards, a smaller 16-bit mask, a 9x9 PSF cropped at
+# the threshold).  hst_fits: the FITS files the reference ships with its pixel
+# fitting demo (81x81 at 0.049", 37x37 PSF, mask), in Cartesian mode.
+FITS_FIXTURES = os.path.join(HERE, "fits")
+REF_DIR = "/root/reference"
+CASES["fits_synth"] = dict(
+    script="""emode 1
+sbmap loadimg image.fits -hdu=2
+sbmap generate_uniform_noisemap
+psf_threshold 1e-2
+sbmap loadpsf psf.fits
+sbmap loadmask mask.fits
+lens sple 0.7 1 0 0.7 40 0.05 -0.03 shear=0.03 -20
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 8 8
+fit regularization curvature
+regparam 5
+imgpixel_nsplit 3
+split_imgpixels on
+inversion_method dense
+""",
+    lenses=[dict(type="sple", params=[0.7, 1.0, 0.0, 0.7, 40.0, 0.05, -0.03]),
+            dict(type="shear", params=[0.03, -20.0, 0.05, -0.03])],
+    dense_rows=-1, full_F=True, harness="fits",
+    files=[os.path.join(FITS_FIXTURES, f) for f in ("image.fits", "mask.fits", "psf.fits")])
+CASES["hst_fits"] = dict(
+    script="""emode 1
+data_pixel_size 0.049
+sbmap loadimg sim_hst_image.fits
+bg_pixel_noise 0.00941285
+sbmap generate_uniform_noisemap
+psf_threshold 1e-2
+sbmap loadpsf hst_psf.fits
+sbmap loadmask mask.fits
+lens sple 1.3634 1.17163 0 0.963867 81.9 0.0102892 0.00358392 shear=0.0866 -20.8
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 40 40
+fit regularization curvature
+regparam 20
+imgpixel_nsplit 2
+split_imgpixels on
+inversion_method dense
+""",
+    lenses=[dict(type="sple", params=[1.3634, 1.17163, 0.0, 0.963867, 81.9, 0.0102892, 0.00358392]),
+            dict(type="shear", params=[0.0866, -20.8, 0.0102892, 0.00358392])],
+    dense_rows=64, full_F=True, harness="fits",
+    files=[os.path.join(REF_DIR, f) for f in ("sim_hst_image.fits", "mask.fits", "hst_psf.fits")])
+
 ARRAYS_F64 = ["zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
               "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
               "F_diag", "F_packed_upper", "s", "model"]
@@ -266,10 +322,13 @@ def run_case(name, case, outdir):
         script = os.path.join(tmp, name + ".in")
         with open(script, "w") as f:
             f.write(case["script"])
+        for src in case.get("files", []):
+            shutil.copy(src, os.path.join(tmp, os.path.basename(src)))
         dump = os.path.join(tmp, "dump")
         os.makedirs(dump)
         env = dict(os.environ, OMP_NUM_THREADS="4")
-        r = subprocess.run([HARNESS, script, dump, str(case["dense_rows"])], cwd=tmp, env=env,
+        harness = HARNESS + "_fits" if case.get("harness") == "fits" else HARNESS
+        r = subprocess.run([harness, script, dump, str(case["dense_rows"])], cwd=tmp, env=env,
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("harness failed on %s:\n%s\n%s" % (name, r.stdout[-2000:], r.stderr[-2000:]))

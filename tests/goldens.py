@@ -7,7 +7,7 @@ import numpy as np
 from qlens_gb300 import abi
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["tiny_sie", "fixed_grid", "powerlaw", "nfw", "twoplane", "cfg1"]
+CASES = ["tiny_sie", "fixed_grid", "powerlaw", "nfw", "twoplane", "cfg1", "fits_synth", "hst_fits"]
 REGOPT_CASES = ["regopt_tiny_sie", "regopt_powerlaw"]
 
 
