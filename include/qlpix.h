@@ -262,6 +262,46 @@ int qlp_set_refinement(qlp_ctx* ctx, int sweeps);
  * reference's QLens::include_noise_term_in_loglike flag (qlens.h:402). */
 int qlp_set_noise_term(qlp_ctx* ctx, int on);
 
+/* ---- sampler-side batching (no counterpart in the reference's serial
+ * loops; its MPI groups do the same one candidate per group,
+ * mcmchdr.cpp:3076-3090) ----
+ * The speculative first-accept search: candidates are proposed in index order
+ * (0, 1, 2, ... within one search), K at a time, evaluated in one batch, and
+ * examined in index order; the search stops at the first accepted one.  It
+ * gives the candidate a one-at-a-time rejection loop (UCMC::MonoSample's
+ * "draw until the likelihood beats the worst live point",
+ * mcmchdr.cpp:3063-3098, 3192-3248; a Metropolis step's "propose until
+ * accepted", mcmchdr.cpp:439-483) would accept, provided that:
+ *   - propose(i) draws everything random about candidate i (its point and any
+ *     acceptance variate) and nothing else;
+ *   - accept(i) only decides from what propose drew and the result;
+ *   - rewind(next) puts the caller's random state back to where it was just
+ *     after propose(next - 1); it is called once, when candidates at or past
+ *     `next` were proposed but are discarded.
+ * K is the smallest batch holding an accepted candidate with 90% chance at
+ * the acceptance rate in *st (0: unknown, use k_max), clamped to
+ * [k_min, k_max]; *st accumulates over searches.  accepted = -1 when none of
+ * max_candidates was accepted.  A callback returning nonzero (propose) or
+ * negative (accept) ends the search with QLP_ERR_ARG. */
+typedef int (*qlp_propose_fn)(void* user, long index, double* lens_params, double* regparam);
+typedef int (*qlp_accept_fn)(void* user, long index, const qlp_result* result);
+typedef void (*qlp_rewind_fn)(void* user, long next_index);
+typedef struct {
+    double accept_rate;            /* accepted / examined so far (in/out) */
+    long proposed, evaluated, examined, accepted, discarded, batches;
+} qlp_search_state;
+int qlp_speculative_search(qlp_ctx* ctx, qlp_propose_fn propose, qlp_accept_fn accept, qlp_rewind_fn rewind,
+                           void* user, int k_min, int k_max, long max_candidates, qlp_search_state* st,
+                           long* accepted);
+
+/* The same search over a caller-supplied batched likelihood (n results for n
+ * candidates of n_params doubles each); no device is needed. */
+typedef int (*qlp_batch_eval_fn)(void* user, const double* params, const double* regparams, int n,
+                                 qlp_result* out);
+int qlp_speculative_search_fn(qlp_batch_eval_fn eval, void* eval_user, int n_params, qlp_propose_fn propose,
+                              qlp_accept_fn accept, qlp_rewind_fn rewind, void* user, int k_min, int k_max,
+                              long max_candidates, qlp_search_state* st, long* accepted);
+
 /* ---- FITS input (the reference reads these through CFITSIO; this library
  * carries its own reader of FITS image HDUs: BITPIX 8/16/32/64/-32/-64,
  * BSCALE/BZERO).  Pixel (i, j), i along FITS axis 1 and j along axis 2, goes

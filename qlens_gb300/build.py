@@ -34,6 +34,7 @@ UNITS = [
     ("ctx.cpp", []),
     ("autotune.cpp", []),
     ("fits.cpp", []),
+    ("sampler.cpp", []),
     ("qlpix_api.cpp", []),
 ]
 HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_common.cuh", "tc_syrk.cuh", "brent.h"]
