@@ -122,6 +122,8 @@ typedef struct {
     double regparam;      /* the regularisation parameter used (the optimised one with
                              qlp_set_regparam_optimization on) */
     int regopt_evals;     /* -2 log(evidence) evaluations of the lambda optimisation (0 = off) */
+    double outside_sb_penalty;  /* the outside-surface-brightness prior's penalty, included in
+                                   m2logev (0 when the prior is off or not triggered) */
 } qlp_result;
 
 /* Training of the NFW deflection surrogate (qlp_nfw_surrogate_train). */
@@ -346,6 +348,20 @@ int qlp_load_noise_map_fits(const char* path, int hdu, int nx, int ny, double* c
  * threshold x peak (QLens 'psf_threshold', default 0.01), normalised to unit
  * sum.  psf == NULL: sizes only. */
 int qlp_load_psf_fits(const char* path, double threshold, double* psf, long cap, int* pnx, int* pny);
+
+/* QLens 'outside_sb_prior on' (lens.cpp:13063-13158; settings
+ * 'outside_sb_frac_threshold' (default 0.3), 'outside_sb_noise_threshold'
+ * (default -1e30: unused), 'emask_nsplit' (default 1), lens.cpp:294-296, 498).
+ * After the inversion the model is re-made over the extended mask `emask`
+ * (uint8 [nx*ny], ImagePixelData::extended_mask; NULL: every pixel), whose
+ * pixels outside the mask split emask_nsplit ways, and PSF-convolved; the
+ * largest |sb| outside the mask at or above t = max(noise_frac sigma_bg,
+ * frac_threshold x the in-mask peak) adds (1 + |(sb - t)/t|)^60 - 1 to
+ * m2logev (qlp_result.outside_sb_penalty).  Uses the context's own mask: a
+ * batch with per-instance masks (qlp_instance.mask_id >= 0) is refused while
+ * it is on. */
+int qlp_set_outside_sb_prior(qlp_ctx* ctx, int on, double frac_threshold, double noise_frac,
+                             const unsigned char* emask, int emask_nsplit);
 
 /* Number of doubles in one lens-parameter vector for the current model. */
 int qlp_n_params(const qlp_ctx* ctx);

@@ -53,6 +53,7 @@ def lib():
         _lib.oracle_threads.restype = C.c_int
         _lib.oracle_set_regopt.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
         _lib.oracle_set_noise_term.argtypes = [C.c_int]
+        _lib.oracle_set_outside_sb.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_long]
         _lib.oracle_brent_min.restype = C.c_double
         _lib.oracle_brent_min.argtypes = [BRENT_FN, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int,
                                           C.POINTER(C.c_int)]
@@ -66,7 +67,8 @@ def lib():
 
 _DT = {"srcpt": np.float64, "L_rowptr": np.int32, "L_index": np.int32, "L_value": np.float64,
        "active_index": np.int32, "Lpsf": np.float64, "D": np.float64, "s": np.float64,
-       "model": np.float64, "F_diag": np.float64, "grid": np.float64}
+       "model": np.float64, "F_diag": np.float64, "grid": np.float64, "osb_sb": np.float64, "osb_maps": np.uint8,
+       "osb_penalty": np.float64}
 
 
 def get(name):
@@ -81,12 +83,22 @@ def get(name):
 
 
 def evaluate(image_bufs, psf_buf, opts, lens_spec, lens_params=None, regparam=0.0, planes=None, regopt=None,
-             noise_term=False):
+             noise_term=False, outside_sb=None):
     """Run the oracle; returns the qlp_result as a dict.  regopt: None, or
     (minlog, maxlog, tol, max_iter) for QLens's 'optimize_regparam on';
-    noise_term: QLens's 'include_noise_term_in_loglike on'."""
+    noise_term: QLens's 'include_noise_term_in_loglike on'; outside_sb: None,
+    or dict(frac, noise_frac, emask_nsplit, emask) for 'outside_sb_prior on'
+    (emask: uint8 [nx*ny] or None for every pixel)."""
     L = lib()
     L.oracle_set_noise_term(1 if noise_term else 0)
+    if outside_sb is None:
+        L.oracle_set_outside_sb(0, 0.3, -1e30, 1, None, 0)
+    else:
+        em = outside_sb.get("emask")
+        em = None if em is None else np.ascontiguousarray(em, dtype=np.uint8)
+        L.oracle_set_outside_sb(1, float(outside_sb.get("frac", 0.3)), float(outside_sb.get("noise_frac", -1e30)),
+                                int(outside_sb.get("emask_nsplit", 1)), None if em is None else em.ctypes.data,
+                                0 if em is None else em.size)
     if regopt is None:
         L.oracle_set_regopt(0, -3.0, 5.0, 0.01, 20)
     else:

@@ -240,13 +240,17 @@ static struct {
     double* D; double* s; double* model;
     double* Fdiag;
     double grid[4];
+    int nx, ny;
+    double* osb_sb;              /* [nx*ny] outside-SB pass: PSF-convolved model */
+    unsigned char* osb_maps;     /* [nx*ny] its mapping flags */
+    double osb_penalty;
 } g_last;
 
 static void free_last(void)
 {
     free(g_last.srcpt); free(g_last.L_rowptr); free(g_last.L_index); free(g_last.L_value);
     free(g_last.active_index); free(g_last.Lpsf); free(g_last.D); free(g_last.s); free(g_last.model);
-    free(g_last.Fdiag);
+    free(g_last.Fdiag); free(g_last.osb_sb); free(g_last.osb_maps);
     memset(&g_last, 0, sizeof(g_last));
 }
 
@@ -372,6 +376,219 @@ double oracle_brent_min(double (*f)(double, void*), void* user, double ax, doubl
     }
     if (nevals) *nevals = n;
     return x;
+}
+
+/* 'outside_sb_prior on' (lens.cpp:294-296 defaults: off, fraction 0.3 of the
+   in-mask peak, noise multiple -1e30 i.e. unused; emask_nsplit 1, lens.cpp:498).
+   emask: the extended mask [nx*ny] (NULL: every pixel). */
+static struct {
+    int on, emask_nsplit;
+    double frac, noise_frac;
+    unsigned char* emask;
+    long emask_n;
+} g_osb = {0, 1, 0.3, -1e30, NULL, 0};
+
+void oracle_set_outside_sb(int on, double frac, double noise_frac, int emask_nsplit, const unsigned char* emask,
+                           long n)
+{
+    g_osb.on = on;
+    g_osb.frac = frac;
+    g_osb.noise_frac = noise_frac;
+    g_osb.emask_nsplit = emask_nsplit;
+    free(g_osb.emask);
+    g_osb.emask = NULL;
+    g_osb.emask_n = 0;
+    if (emask && n > 0) {
+        g_osb.emask = (unsigned char*)malloc(n);
+        memcpy(g_osb.emask, emask, n);
+        g_osb.emask_n = n;
+    }
+}
+
+static int cmp_int(const void* a, const void* b) { int x = *(const int*)a, y = *(const int*)b; return (x > y) - (x < y); }
+
+/* The outside-surface-brightness pass (lens.cpp:13063-13158, Cartesian branch)
+   after the inversion: the pixel grid switches to the extended mask
+   (ImagePixelGrid::activate_extended_mask, pixelgrid.cpp:10833-10852), whose
+   pixels outside the mask split emask_nsplit ways (set_nsplits 10898-10938);
+   they are ray-traced and mapped onto the same source grid (assign_pixel_mappings
+   12777-12910), the cells any of them maps to become the new active set (in
+   cell order) holding the inverted amplitudes where the inversion had them and
+   zero elsewhere (SourcePixel::update_surface_brightness 817-831,
+   fill_surface_brightness_vector 833-851), the model is the dense L times
+   those amplitudes in column order (convert_Lmatrix_to_dense 13717-13747,
+   calculate_image_pixel_surface_brightness_dense 18268-18290), then
+   PSF-convolved over the active extended-mask pixels
+   (PSF_convolution_pixel_vector, direct branch 14409-14493).  A neighbour in
+   the extended mask that maps nowhere has pixel index -1 there, which the
+   reference reads as element -1 of its vector; it is taken as 0 here.  The
+   penalty: with the peak over masked mapped pixels and threshold
+   max(noise_frac sigma, frac peak), the largest |sb| >= threshold over mapped
+   extended-mask pixels outside the mask adds (1 + |(sb - t)/t|)^60 - 1. */
+static double outside_sb_penalty(const qlp_image* im, const qlp_psf* psf, const olens* lenses, int nlens,
+                                 const qlp_planes* planes, int ns, const double* cx, const double* cy,
+                                 const double* ccx, const double* ccy, int snx, int sny, const int* aidx,
+                                 const double* s)
+{
+    const int nx = im->npixels_x, ny = im->npixels_y;
+    const int ens = g_osb.emask_nsplit;
+    unsigned char* em = (unsigned char*)malloc((size_t)nx * ny);
+    for (long t = 0; t < (long)nx * ny; t++)
+        em[t] = (g_osb.emask && t < g_osb.emask_n) ? (g_osb.emask[t] != 0) : 1;
+    /* extended-mask pixels, j-outer / i-inner, and their sub-pixel offsets */
+    int ne = 0;
+    for (long t = 0; t < (long)nx * ny; t++) ne += em[t];
+    int* epix = (int*)malloc(sizeof(int) * (ne > 0 ? ne : 1));
+    long* eoff = (long*)malloc(sizeof(long) * (ne + 1));
+    {
+        int c = 0;
+        long o = 0;
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                const int t = i * ny + j;
+                if (!em[t]) continue;
+                const int nsp = im->in_mask[t] ? ns : ens;
+                epix[c] = t;
+                eoff[c++] = o;
+                o += (long)nsp * nsp;
+            }
+        eoff[ne] = o;
+    }
+    const long nsub_e = eoff[ne];
+    double* sp = (double*)malloc(sizeof(double) * 2 * (nsub_e > 0 ? nsub_e : 1));
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int e = 0; e < ne; e++) {
+        const int i = epix[e] / ny, j = epix[e] % ny;
+        const int nsp = im->in_mask[epix[e]] ? ns : ens;
+        const double x0 = im->xvals[i], x1 = im->xvals[i + 1], y0 = im->yvals[j], y1 = im->yvals[j + 1];
+        long k = eoff[e];
+        for (int ii = 0; ii < nsp; ii++)
+            for (int jj = 0; jj < nsp; jj++) {
+                const double u0 = ((double)(1 + 2 * ii)) / (2 * nsp);
+                const double w0 = ((double)(1 + 2 * jj)) / (2 * nsp);
+                double bx, by;
+                find_sourcept(lenses, nlens, planes, (1 - u0) * x0 + u0 * x1, (1 - w0) * y0 + w0 * y1, &bx, &by);
+                sp[2 * k] = bx;
+                sp[2 * k + 1] = by;
+                k++;
+            }
+    }
+    /* cells and weights per sub-pixel, as in the inversion's mapping */
+    int* cell3 = (int*)malloc(sizeof(int) * 3 * (nsub_e > 0 ? nsub_e : 1));
+    double* w3 = (double*)malloc(sizeof(double) * 3 * (nsub_e > 0 ? nsub_e : 1));
+    unsigned char* mapped = (unsigned char*)calloc((size_t)snx * sny, 1);
+    unsigned char* pmaps = (unsigned char*)calloc(ne > 0 ? ne : 1, 1);
+    for (int e = 0; e < ne; e++) {
+        const int nsp = im->in_mask[epix[e]] ? ns : ens;
+        const double weight = 1.0 / (nsp * nsp);
+        for (long t = eoff[e]; t < eoff[e + 1]; t++) {
+            const double px = sp[2 * t], py = sp[2 * t + 1];
+            cell3[3 * t] = -1;
+            if (!(px >= cx[0] && px < cx[snx] && py >= cy[0] && py < cy[sny])) continue;
+            int lo = 0, hi = snx - 1;
+            while (lo < hi) { int mid = (lo + hi + 1) / 2; if (cx[mid] <= px) lo = mid; else hi = mid - 1; }
+            const int ci = lo;
+            lo = 0; hi = sny - 1;
+            while (lo < hi) { int mid = (lo + hi + 1) / 2; if (cy[mid] <= py) lo = mid; else hi = mid - 1; }
+            const int cj = lo;
+            const int xn = ((px > ccx[ci] && ci < snx - 1) || ci == 0) ? ci + 1 : ci - 1;
+            const int yn = ((py > ccy[cj] && cj < sny - 1) || cj == 0) ? cj + 1 : cj - 1;
+            const int c0 = cj * snx + ci, c1 = cj * snx + xn, c2 = yn * snx + ci;
+            cell3[3 * t] = c0; cell3[3 * t + 1] = c1; cell3[3 * t + 2] = c2;
+            mapped[c0] = mapped[c1] = mapped[c2] = 1;
+            pmaps[e] = 1;
+            const double p0x = ccx[ci], p0y = ccy[cj], p1x = ccx[xn], p1y = ccy[cj], p2x = ccx[ci], p2y = ccy[yn];
+            const double d = (p0x - p1x) * (p1y - p2y) - (p1x - p2x) * (p0y - p1y);
+            w3[3 * t] = weight * (px * (p1y - p2y) + py * (p2x - p1x) + p1x * p2y - p1y * p2x) / d;
+            w3[3 * t + 1] = weight * (px * (p2y - p0y) + py * (p0x - p2x) + p0y * p2x - p0x * p2y) / d;
+            w3[3 * t + 2] = weight * (px * (p0y - p1y) + py * (p1x - p0x) + p0x * p1y - p0y * p1x) / d;
+        }
+    }
+    /* model per mapped pixel: the row's entries merged per cell in CSR order,
+       then summed over cells in ascending order (= ascending new active index) */
+    int* pidx = (int*)malloc(sizeof(int) * nx * ny);
+    for (long t = 0; t < (long)nx * ny; t++) pidx[t] = -1;
+    int na = 0;
+    for (int e = 0; e < ne; e++) if (pmaps[e]) pidx[epix[e]] = na++;
+    double* model = (double*)malloc(sizeof(double) * (na > 0 ? na : 1));
+    int* act = (int*)malloc(sizeof(int) * (na > 0 ? na : 1));
+    {
+        int r = 0;
+        for (int e = 0; e < ne; e++) {
+            if (!pmaps[e]) continue;
+            act[r] = epix[e];
+            const long n3 = 3 * (eoff[e + 1] - eoff[e]);
+            int* cells = (int*)malloc(sizeof(int) * (n3 > 0 ? n3 : 1));
+            int nc = 0;
+            for (long t = eoff[e]; t < eoff[e + 1]; t++) {
+                if (cell3[3 * t] < 0) continue;
+                for (int u = 0; u < 3; u++) {
+                    int seen = 0;
+                    for (int q = 0; q < nc; q++) if (cells[q] == cell3[3 * t + u]) { seen = 1; break; }
+                    if (!seen) cells[nc++] = cell3[3 * t + u];
+                }
+            }
+            qsort(cells, nc, sizeof(int), cmp_int);
+            double acc = 0;
+            for (int q = 0; q < nc; q++) {
+                double v = 0;
+                for (long t = eoff[e]; t < eoff[e + 1]; t++) {
+                    if (cell3[3 * t] < 0) continue;
+                    for (int u = 0; u < 3; u++) if (cell3[3 * t + u] == cells[q]) v += w3[3 * t + u];
+                }
+                const int a = aidx[cells[q]];
+                acc += v * (a >= 0 ? s[a] : 0.0);
+            }
+            model[r++] = acc;
+            free(cells);
+        }
+    }
+    /* PSF convolution over the mapped extended-mask pixels */
+    double* sb = (double*)calloc((size_t)nx * ny, sizeof(double));
+    {
+        const int pnx = psf->nx, pny = psf->ny, nxh = pnx / 2, nyh = pny / 2;
+        for (int r = 0; r < na; r++) {
+            const int k = act[r] / ny, l = act[r] % ny;
+            double v = 0;
+            for (int pk = 0; pk < pnx; pk++) {
+                const int ii = k + nxh - pk;
+                if (ii < 0 || ii >= nx) continue;
+                for (int pl = 0; pl < pny; pl++) {
+                    const int jj = l + nyh - pl;
+                    if (jj < 0 || jj >= ny) continue;
+                    if (!em[ii * ny + jj]) continue;
+                    const int q = pidx[ii * ny + jj];
+                    if (q < 0) continue;
+                    v += psf->matrix[pk * pny + pl] * model[q];
+                }
+            }
+            sb[act[r]] = v;
+        }
+    }
+    double max_sb = -1e30, max_ext = -1e30;
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++) {
+            const int t = i * ny + j;
+            if (im->in_mask[t] && pidx[t] >= 0 && sb[t] > max_sb) max_sb = sb[t];
+        }
+    const double a = g_osb.noise_frac * im->background_pixel_noise, b = g_osb.frac * max_sb;
+    const double thr = (a > b) ? a : b;
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++) {
+            const int t = i * ny + j;
+            if (!im->in_mask[t] && em[t] && pidx[t] >= 0 && fabs(sb[t]) >= thr && fabs(sb[t]) > max_ext)
+                max_ext = fabs(sb[t]);
+        }
+    double penalty = 0;
+    if (max_ext > 0) penalty = pow(1 + fabs((max_ext - thr) / thr), 60) - 1.0;
+    unsigned char* maps = (unsigned char*)calloc((size_t)nx * ny, 1);
+    for (long t = 0; t < (long)nx * ny; t++) maps[t] = pidx[t] >= 0;
+    free(g_last.osb_sb); free(g_last.osb_maps);
+    g_last.osb_sb = sb; g_last.osb_maps = maps; g_last.nx = nx; g_last.ny = ny;
+    g_last.osb_penalty = penalty;
+    free(em); free(epix); free(eoff); free(sp); free(cell3); free(w3); free(mapped); free(pmaps); free(pidx);
+    free(model); free(act);
+    return penalty;
 }
 
 /* 'include_noise_term_in_loglike on' (lens.cpp:303 default off) */
@@ -841,6 +1058,8 @@ int oracle_eval(const qlp_image* im, const qlp_psf* psf, const qlp_srcgrid_opts*
         }
         loglike += n_mask * log(6.28318530717958647692);
     }
+    if (g_osb.on && out->status == 0)
+        loglike += outside_sb_penalty(im, psf, lenses, nlens, &planes, ns, cx, cy, ccx, ccy, snx, sny, aidx, s);
 
     out->chisq0 = chisq0;
     out->logdet_F = logdetF;
@@ -878,6 +1097,9 @@ long oracle_get(const char* name, void* buf, long cap)
     else if (!strcmp(name, "model")) { src = g_last.model; n = g_last.n_pix; }
     else if (!strcmp(name, "F_diag")) { src = g_last.Fdiag; n = g_last.M; }
     else if (!strcmp(name, "grid")) { src = g_last.grid; n = 4; }
+    else if (!strcmp(name, "osb_sb")) { src = g_last.osb_sb; n = g_last.osb_sb ? (long)g_last.nx * g_last.ny : 0; }
+    else if (!strcmp(name, "osb_maps")) { src = g_last.osb_maps; n = g_last.osb_maps ? (long)g_last.nx * g_last.ny : 0; es = 1; }
+    else if (!strcmp(name, "osb_penalty")) { src = &g_last.osb_penalty; n = 1; }
     else return -1;
     if (buf && src) memcpy(buf, src, es * (size_t)(n < cap ? n : cap));
     return n;

@@ -13,6 +13,8 @@ int oracle_n_params(const qlp_lens* lenses, int nlens);
 long oracle_get(const char* name, void* buf, long cap);
 int oracle_threads(void);
 void oracle_set_noise_term(int on);
+void oracle_set_outside_sb(int on, double frac, double noise_frac, int emask_nsplit, const unsigned char* emask,
+                           long n);
 void oracle_set_regopt(int on, double minlog, double maxlog, double tol, int maxit);
 double oracle_brent_min(double (*f)(double, void*), void* user, double ax, double bx, double tol, int maxit,
                         int* nevals);

@@ -56,6 +56,8 @@ GRAB(G_act_i, ImagePixelGrid, int*, active_image_pixel_i)
 GRAB(G_act_j, ImagePixelGrid, int*, active_image_pixel_j)
 GRAB(G_zfac, ImagePixelGrid, double*, imggrid_zfactors)
 GRAB(G_beta, ImagePixelGrid, double**, imggrid_betafactors)
+GRAB(G_sb, ImagePixelGrid, double**, surface_brightness)
+GRAB(G_maps, ImagePixelGrid, bool**, maps_to_source_pixel)
 
 static std::string g_out;
 
@@ -109,14 +111,15 @@ int main(int argc, char** argv)
 		std::vector<double> xv(d->xvals, d->xvals + nx + 1), yv(d->yvals, d->yvals + ny + 1);
 		dumpd("xvals", xv); dumpd("yvals", yv);
 		std::vector<double> sb(nx * ny), cov(nx * ny);
-		std::vector<unsigned char> mk(nx * ny);
+		std::vector<unsigned char> mk(nx * ny), em(nx * ny);
 		for (int i = 0; i < nx; i++)
 			for (int j = 0; j < ny; j++) {
 				sb[i * ny + j] = d->surface_brightness[i][j];
 				cov[i * ny + j] = (d->covinv_map != NULL) ? d->covinv_map[i][j] : 0.0;
 				mk[i * ny + j] = d->in_mask[mask_k][i][j] ? 1 : 0;
+				em[i * ny + j] = (d->extended_mask && d->extended_mask[mask_k][i][j]) ? 1 : 0;
 			}
-		dumpd("data", sb); dumpd("covinv", cov); dumpu("mask", mk);
+		dumpd("data", sb); dumpd("covinv", cov); dumpu("mask", mk); dumpu("emask", em);
 	}
 
 	// ---------- 1. the entry point itself ----------
@@ -272,6 +275,36 @@ int main(int argc, char** argv)
 	}
 	lens.store_image_pixel_surface_brightness(0);
 	double regterms = lens.calculate_regularization_prior_term(lens.regparam_ptr);
+	// 'outside_sb_prior on': the entry point ends with a pass over the
+	// extended mask (lens.cpp:13063-13158).  Its model image does not survive
+	// the call, so the pass is run again here with the same calls in the same
+	// order (lens.cpp:13067-13086, Cartesian branch) and its PSF-convolved
+	// model and mapping flags are written out.
+	if (lens.outside_sb_prior) {
+		lens.clear_pixel_matrices(0);          // as at the end of the Cartesian branch (lens.cpp:12623)
+		bool supersampling_orig = lens.psf_supersampling;
+		lens.psf_supersampling = false;
+		g->activate_extended_mask();
+		g->redo_lensing_calculations(false);
+		lens.assign_pixel_mappings(0, false);
+		lens.initialize_pixel_matrices(0, false);
+		lens.convert_Lmatrix_to_dense();
+		sg->fill_surface_brightness_vector();
+		lens.calculate_image_pixel_surface_brightness_dense();
+		lens.PSF_convolution_pixel_vector(0, false, false, false);
+		lens.store_image_pixel_surface_brightness(0);
+		double** sbp = g->*grab(G_sb());
+		bool** mp = g->*grab(G_maps());
+		std::vector<double> osb(nx * ny);
+		std::vector<unsigned char> om(nx * ny);
+		for (int i = 0; i < nx; i++)
+			for (int j = 0; j < ny; j++) { osb[i * ny + j] = sbp[i][j]; om[i * ny + j] = mp[i][j] ? 1 : 0; }
+		dumpd("osb_sb", osb); dumpu("osb_maps", om);
+		lens.clear_sparse_lensing_matrices();
+		lens.clear_pixel_matrices(0);
+		g->set_fit_window(*lens.image_pixel_data, false, mask_k);
+		lens.psf_supersampling = supersampling_orig;
+	}
 	const double regparam = *lens.regparam_ptr;
 
 	std::ofstream sc((g_out + "/scalars.txt").c_str());
@@ -296,6 +329,10 @@ int main(int argc, char** argv)
 	sc << "use_noise_map " << (lens.use_noise_map ? 1 : 0) << "\n";
 	sc << "background_pixel_noise " << lens.background_pixel_noise << "\n";
 	sc << "nthreads " << nthreads << "\n";
+	sc << "outside_sb_prior " << (lens.outside_sb_prior ? 1 : 0) << "\n";
+	sc << "outside_sb_prior_threshold " << lens.outside_sb_prior_threshold << "\n";
+	sc << "outside_sb_prior_noise_frac " << lens.outside_sb_prior_noise_frac << "\n";
+	sc << "emask_nsplit " << lens.emask_imgpixel_nsplit << "\n";
 	sc.close();
 	printf("m2logev=%.17g chisq0=%.17g logdetF=%.17g logdetR=%.17g npix=%d nsrc=%d nnz=%d\n",
 		m2logev_entry, chisq0_entry, logdetF_entry, logdetR_entry, npix, nsrc, nnz);

@@ -31,6 +31,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("mixed.cu", []),
     ("surrogate.cu", ["--fmad=false"]),
+    ("outside.cu", ["--fmad=false"]),
     ("ctx.cpp", []),
     ("autotune.cpp", []),
     ("fits.cpp", []),

@@ -67,6 +67,11 @@ static void free_slot(Slot& s)
     drop_graph(s);
     mixed_free(s);
     free_work(s.w);
+    OsbWork& o = s.osb;
+    void* op[] = {o.sp, o.cell3, o.w3, o.model, o.act, o.sb};
+    for (void* p : op) if (p) cudaFree(p);
+    o = OsbWork{};
+    s.osb_nsub = 0;
     s.M_cap = s.N_cap = s.nsub_cap = s.snx_cap = s.sny_cap = 0;
     s.fp64_mats = false;
 }
@@ -186,6 +191,7 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     if (c->psfx_mode < 0) c->psfx_mode = (psf->nx * psf->ny >= 500) ? 1 : 0;
     sd.use_noise_map = noise_map ? 1 : 0;
     sd.cov_inverse = cov_inverse;
+    c->bg_noise = im->background_pixel_noise;
     sd.xvals = c->d_xvals; sd.yvals = c->d_yvals; sd.data = c->d_data; sd.covinv = c->d_covinv;
     sd.mpix = c->d_mpix; sd.psf = c->d_psf;
     {
@@ -225,7 +231,8 @@ void ctx_free(qlp_ctx* c)
         if (s.side_join) cudaEventDestroy(s.side_join);
     }
     c->slots.clear();
-    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix};
+    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix,
+                    c->d_emask, c->d_inmask, c->d_epix, c->d_eoff};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);
     if (c->h_ep) cudaFreeHost(c->h_ep);
@@ -299,6 +306,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
             launch_solve_fp64(w, Mc, st);
         }
         launch_model_chi2(sd, so, w, N_max, Mc, regp, st, mixed);
+        if (c->osb_on) launch_outside_sb(sd, so, c->osb, slot.osb, model_has_nfw(c), w, st);
         return QLP_OK;
     }
     cudaMemsetAsync(w.out, 0, sizeof(EvalOut), st);
@@ -349,14 +357,36 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     }
     if (ev) cudaEventRecord(ev[5], st);
     launch_model_chi2(sd, so, w, N_max, Mc, regp, st, mixed);
+    if (c->osb_on) launch_outside_sb(sd, so, c->osb, slot.osb, model_has_nfw(c), w, st);
     if (ev) cudaEventRecord(ev[6], st);
     return QLP_OK;
 }
 
 // Make the slot's workspace ready for the pipeline without allocating during
 // a stream capture.
+static int ensure_osb(qlp_ctx* c, Slot& s)
+{
+    if (!c->osb_on || (s.osb.sp && s.osb_nsub >= c->osb.nsub_e)) return QLP_OK;
+    OsbWork& o = s.osb;
+    cudaFree(o.sp); cudaFree(o.cell3); cudaFree(o.w3); cudaFree(o.model); cudaFree(o.act); cudaFree(o.sb);
+    o = OsbWork{};
+    const size_t n = (size_t)std::max(c->osb.nsub_e, 1), np = (size_t)c->nx * c->ny;
+    CK(dalloc(&o.sp, 2 * n), "alloc osb");
+    CK(cudaMalloc((void**)&o.cell3, sizeof(int) * 3 * n), "alloc osb");
+    CK(dalloc(&o.w3, 3 * n), "alloc osb");
+    CK(dalloc(&o.model, np), "alloc osb");
+    CK(cudaMalloc((void**)&o.act, sizeof(int) * np), "alloc osb");
+    CK(dalloc(&o.sb, np), "alloc osb");
+    s.osb_nsub = c->osb.nsub_e;
+    return QLP_OK;
+}
+
 static int prepare_slot(qlp_ctx* c, Slot& s)
 {
+    {
+        int e = ensure_osb(c, s);
+        if (e != QLP_OK) return e;
+    }
     const bool regopt = c->regopt && c->so.regularization;
     if (c->precision == QLP_MIXED) return regopt ? mixed_ensure_f0(s) : mixed_init(s);
     int r = ensure_fp64_mats(s);
@@ -450,6 +480,7 @@ static void fill_result(const EvalOut& o, qlp_result* out)
     out->status = o.status;
     out->refine_iters = o.refine_iters;
     out->nfw_fallbacks = o.pad;
+    out->outside_sb_penalty = o.osb_penalty;
 }
 
 static int ensure_results(qlp_ctx* c, int n)
@@ -625,6 +656,11 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
             set_error("%s %d", "bad mask id", inst[i].mask_id);
             return QLP_ERR_ARG;
         }
+        if (inst[i].mask_id >= 0 && c->osb_on) {
+            set_error("%s %d", "the outside-surface-brightness prior uses the image mask; refused mask id",
+                      inst[i].mask_id);
+            return QLP_ERR_ARG;
+        }
         if (inst[i].mask_id >= 0) nmask_max = std::max(nmask_max, c->mask_cnt[inst[i].mask_id]);
         if (inst[i].src_npixels_x < 2 || inst[i].src_npixels_y < 2) continue;
         cells_max = std::max(cells_max, inst[i].src_npixels_x * inst[i].src_npixels_y);
@@ -732,6 +768,64 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
         out[i].regopt_evals = c->regopt_evals[i];
     }
     return rc;
+}
+
+// The outside-surface-brightness prior's tables: the extended-mask pixels in
+// the reference's j-outer / i-inner order with their sub-pixel offsets (the
+// mask's pixels split nsplit ways, the others ens ways, set_nsplits,
+// pixelgrid.cpp:10898-10938).
+int ctx_set_outside_sb(qlp_ctx* c, int on, double frac, double noise_frac, const unsigned char* emask, int ens)
+{
+    cudaSetDevice(c->device);
+    if (on && (ens < 1 || ens > 16 || !(frac >= 0))) {
+        set_error("%s (%d)", "bad outside-surface-brightness settings", ens);
+        return QLP_ERR_ARG;
+    }
+    c->graph_gen++;                    // the pass is part of the captured sequence
+    c->osb_on = 0;
+    if (!on) return QLP_OK;
+    const int nx = c->nx, ny = c->ny;
+    std::vector<unsigned char> em((size_t)nx * ny, 1), in((size_t)nx * ny, 0);
+    if (emask) for (size_t t = 0; t < em.size(); t++) em[t] = emask[t] ? 1 : 0;
+    for (int p : c->mpix) in[p] = 1;
+    std::vector<int> epix, eoff;
+    long o = 0;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const int t = i * ny + j;
+            if (!em[t]) continue;
+            const int ns = in[t] ? c->sd.nsplit : ens;
+            epix.push_back(t);
+            eoff.push_back((int)o);
+            o += (long)ns * ns;
+        }
+    eoff.push_back((int)o);
+    if (o > (1L << 30)) { set_error("%s (%d)", "extended mask too large", 0); return QLP_ERR_ARG; }
+    void* old[] = {c->d_emask, c->d_inmask, c->d_epix, c->d_eoff};
+    for (void* p : old) if (p) cudaFree(p);
+    c->d_emask = c->d_inmask = nullptr;
+    c->d_epix = c->d_eoff = nullptr;
+    CK(cudaMalloc((void**)&c->d_emask, em.size()), "alloc");
+    CK(cudaMalloc((void**)&c->d_inmask, in.size()), "alloc");
+    CK(cudaMalloc((void**)&c->d_epix, sizeof(int) * std::max<size_t>(epix.size(), 1)), "alloc");
+    CK(cudaMalloc((void**)&c->d_eoff, sizeof(int) * eoff.size()), "alloc");
+    CK(cudaMemcpy(c->d_emask, em.data(), em.size(), cudaMemcpyHostToDevice), "h2d");
+    CK(cudaMemcpy(c->d_inmask, in.data(), in.size(), cudaMemcpyHostToDevice), "h2d");
+    if (!epix.empty()) CK(cudaMemcpy(c->d_epix, epix.data(), sizeof(int) * epix.size(), cudaMemcpyHostToDevice), "h2d");
+    CK(cudaMemcpy(c->d_eoff, eoff.data(), sizeof(int) * eoff.size(), cudaMemcpyHostToDevice), "h2d");
+    OsbStatic& os = c->osb;
+    os.emask = c->d_emask;
+    os.inmask = c->d_inmask;
+    os.epix = c->d_epix;
+    os.eoff = c->d_eoff;
+    os.ne = (int)epix.size();
+    os.nsub_e = (int)o;
+    os.ens = ens;
+    os.frac = frac;
+    os.noise_frac = noise_frac;
+    os.bg_noise = c->bg_noise;
+    c->osb_on = 1;
+    return QLP_OK;
 }
 
 int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value, int* active_index,

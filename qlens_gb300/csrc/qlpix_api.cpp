@@ -261,6 +261,13 @@ int qlp_set_noise_term(qlp_ctx* c, int on)
     return QLP_OK;
 }
 
+int qlp_set_outside_sb_prior(qlp_ctx* c, int on, double frac_threshold, double noise_frac,
+                             const unsigned char* emask, int emask_nsplit)
+{
+    if (!c) return fail(QLP_ERR_ARG, "null context");
+    return ctx_set_outside_sb(c, on, frac_threshold, noise_frac, emask, emask_nsplit);
+}
+
 int qlp_last_transfer_bytes(const qlp_ctx* c, long long* h2d, long long* d2h)
 {
     if (!c || !h2d || !d2h) return fail(QLP_ERR_ARG, "bad arguments");

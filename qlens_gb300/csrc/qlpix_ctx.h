@@ -41,6 +41,8 @@ struct Slot {
     int trial_key[7] = {0, 0, 0, 0, 0, 0, 0};
     long long trial_gen = 0;
     long long trial_launches = 0;
+    OsbWork osb{};                  // outside-surface-brightness pass (allocated when the prior is on)
+    int osb_nsub = 0;               // its capacity in sub-pixels
 };
 
 }  // namespace qlpix
@@ -101,6 +103,15 @@ struct qlp_ctx {
     int regopt_maxit = 20;
     int nfw_mode = QLP_NFW_QUADRATURE;    // NFW deflection: quadrature or trained surrogate
     double nfw_threshold = 2e-5;          // surrogate error bound (arcsec) above which a ray falls back
+    // outside-surface-brightness prior (QLens 'outside_sb_prior'): settings,
+    // device tables of the extended mask, background noise of the image
+    int osb_on = 0;
+    qlpix::OsbStatic osb{};
+    unsigned char* d_emask = nullptr;
+    unsigned char* d_inmask = nullptr;
+    int* d_epix = nullptr;
+    int* d_eoff = nullptr;
+    double bg_noise = 0;
     long long graph_gen = 1;              // bumped whenever captured graphs go stale
     long long last_h2d = 0, last_d2h = 0; // bytes moved by the last call
     float stage_ms[QLP_N_STAGES] = {};
@@ -136,6 +147,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
                         cudaEvent_t* ev);
 // autotune.cpp
 int ctx_get_schedule(const qlp_ctx* c, qlp_schedule* out);
+// outside.cu / ctx.cpp: the outside-surface-brightness prior
+int ctx_set_outside_sb(qlp_ctx* c, int on, double frac, double noise_frac, const unsigned char* emask, int ens);
 int ctx_set_schedule(qlp_ctx* c, const qlp_schedule* s);
 int ctx_autotune(qlp_ctx* c, const double* params, const double* lambdas, const qlp_instance* inst, int n, int reps,
                  qlp_tune_report* rep);

@@ -69,6 +69,24 @@ struct EvalOut {
                                        // pixels + regularisation terms + log det F
     int n_active_pixels, n_active_src, L_nnz, status, refine_iters;
     int pad;                           // rays that took the NFW quadrature instead of the surrogate
+    double osb_penalty;                // the outside-surface-brightness prior's penalty (0 when off)
+};
+
+// The outside-surface-brightness prior (QLens 'outside_sb_prior'): static
+// tables of the extended mask, uploaded once per setting.
+struct OsbStatic {
+    const unsigned char* emask;        // nx*ny extended mask
+    const unsigned char* inmask;       // nx*ny the context's mask
+    const int* epix;                   // ne extended-mask pixels, j-outer / i-inner
+    const int* eoff;                   // ne+1 sub-pixel offsets (mask pixels split nsplit ways, others ens)
+    int ne, nsub_e, ens;
+    double frac, noise_frac, bg_noise; // threshold max(noise_frac bg_noise, frac peak)
+};
+// ... and its per-slot workspace
+struct OsbWork {
+    double* sp;                        // 2 nsub_e source points
+    int* cell3;  double* w3;           // 3 nsub_e
+    double* model;  int* act;  double* sb;   // nx*ny
 };
 
 struct StaticData {            // per-context, uploaded once
@@ -195,6 +213,8 @@ void launch_logdet(const double* A, int ld, int M_max, Work& w, int which, cudaS
 void launch_solve_fp64(Work& w, int M_max, cudaStream_t st);
 void launch_model_chi2(const StaticData& sd, const SrcOpts& so, Work& w, int N_max, int M_max,
                        const double* regp, cudaStream_t st, bool model_ready = false);
+void launch_outside_sb(const StaticData& sd, const SrcOpts& so, const OsbStatic& os, const OsbWork& ow, bool nfw,
+                       Work& w, cudaStream_t st);
 void init_kernel_attributes();
 long long kernel_launch_counter();
 void count_launches(int n);

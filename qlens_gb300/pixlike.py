@@ -63,6 +63,7 @@ def load_library(build_if_missing=False):
     L.qlp_set_graphs.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_refinement.argtypes = [C.c_void_p, C.c_int]
     L.qlp_set_noise_term.argtypes = [C.c_void_p, C.c_int]
+    L.qlp_set_outside_sb_prior.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_int]
     L.qlp_set_regparam_optimization.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
     L.qlp_brent_min.argtypes = [BRENT_FN, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double),
                                 P(C.c_int)]
@@ -248,6 +249,16 @@ class PixelLikelihood:
         """QLens's 'include_noise_term_in_loglike': add the pixel-noise
         normalisation to -2 log(evidence)."""
         self._check(self.lib.qlp_set_noise_term(self.ctx, 1 if on else 0))
+
+    def set_outside_sb_prior(self, on, frac_threshold=0.3, noise_frac=-1e30, emask=None, emask_nsplit=1):
+        """QLens's 'outside_sb_prior': penalise model surface brightness
+        outside the mask (over the extended mask `emask`, uint8 [nx, ny] or
+        None for every pixel)."""
+        em = None if emask is None else np.ascontiguousarray(emask, dtype=np.uint8).ravel()
+        self._keep_emask = em
+        self._check(self.lib.qlp_set_outside_sb_prior(self.ctx, 1 if on else 0, float(frac_threshold),
+                                                      float(noise_frac), None if em is None else em.ctypes.data,
+                                                      int(emask_nsplit)))
 
     def last_transfer_bytes(self):
         """(host->device, device->host) bytes moved by the last call."""

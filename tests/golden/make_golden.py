@@ -253,6 +253,22 @@ CASES["noise_tiny_sie"] = dict(CASES["tiny_sie"], script=CASES["tiny_sie"]["scri
     "sbmap generate_uniform_noisemap\n", ""))
 assert "include_noise_term_in_loglike on" in CASES["noise_tiny_sie"]["script"]
 
+# 'outside_sb_prior on': after the inversion the model is re-made over the
+# extended mask (every pixel by default; pixels outside the mask split
+# emask_nsplit = 1 ways), PSF-convolved, and a penalty added where it exceeds
+# a fraction of the in-mask peak outside the mask (lens.cpp:13063-13158).
+# The thresholds are set so that one case pays a penalty and one does not.
+# The extended mask: 'sbmap unset_all_pixels' empties it and
+# 'set_data_annulus' does not touch it, so 'emask_n_neighbors n' grows it from
+# the mask by n rings of pixels.
+CASES["osb_tiny_sie"] = dict(CASES["tiny_sie"], script=CASES["tiny_sie"]["script"].replace(
+    "fit source_mode cartesian\n", "emask_n_neighbors 3\nfit source_mode cartesian\n").replace(
+    "inversion_method dense\n", "inversion_method dense\noutside_sb_prior on\noutside_sb_frac_threshold 0.15\n"))
+CASES["osb_powerlaw"] = dict(CASES["powerlaw"], script=CASES["powerlaw"]["script"].replace(
+    "fit source_mode cartesian\n", "emask_n_neighbors 2\nfit source_mode cartesian\n").replace(
+    "inversion_method dense\n", "inversion_method dense\noutside_sb_prior on\n"))
+assert all("emask_n_neighbors" in CASES[k]["script"] for k in ("osb_tiny_sie", "osb_powerlaw"))
+
 # FITS input through the reference's own loaders (ImagePixelData::load_data_fits,
 # load_mask_fits, QLens::load_psf_fits), run by the harness built against the
 # CFITSIO stand-in (oracle/fitsio_shim).  fits_synth: this repository's
@@ -311,9 +327,9 @@ inversion_method dense
 
 ARRAYS_F64 = ["zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
               "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
-              "F_diag", "F_packed_upper", "s", "model"]
+              "F_diag", "F_packed_upper", "s", "model", "osb_sb"]
 ARRAYS_I32 = ["lens_plane", "masked_pixels", "active_index", "active_pixels", "L_rowptr", "L_index", "R_index"]
-ARRAYS_U8 = ["mask"]
+ARRAYS_U8 = ["mask", "emask", "osb_maps"]
 
 
 def run_case(name, case, outdir):
