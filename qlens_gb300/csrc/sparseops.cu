@@ -55,25 +55,37 @@ __global__ void __launch_bounds__(256) k_conv(StaticData sd, const GridState* __
                                               const int* __restrict__ rowpix, const double* __restrict__ img,
                                               double* __restrict__ out)
 {
+    // the taps' PSF values and offsets from the output pixel in the padded
+    // image, tabulated once per CTA: a tap is then one shared load, one image
+    // load and one multiply-add (no index arithmetic per tap)
+    extern __shared__ __align__(16) unsigned char conv_smem[];
     const int N = gs->N;
     const int lane = threadIdx.x & 31;
     const int nT = sd.pnx * sd.pny, nxh = sd.pnx / 2, nyh = sd.pny / 2, nxp = sd.nx + 2 * nxh;
+    double* tpsf = reinterpret_cast<double*>(conv_smem);
+    int* toff = reinterpret_cast<int*>(tpsf + nT);
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        const int pk = t / sd.pny, pl = t - pk * sd.pny;
+        tpsf[t] = sd.psf[t];
+        toff[t] = TRANSPOSE ? pl * nxp + pk : (2 * nyh - pl) * nxp + (2 * nxh - pk);
+    }
+    __syncthreads();
     for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < N; r += gridDim.x * (blockDim.x >> 5)) {
         const int pix = rowpix[r];
         const int k = pix / sd.ny, l = pix - k * sd.ny;
+        const double* base = img + (size_t)l * nxp + k;
         double acc = 0;
-        for (int t = lane; t < nT; t += 32) {
-            const int pk = t / sd.pny, pl = t - pk * sd.pny;
-            const int ii = TRANSPOSE ? k - nxh + pk : k + nxh - pk;
-            const int jj = TRANSPOSE ? l - nyh + pl : l + nyh - pl;
-            acc += sd.psf[t] * img[(size_t)(jj + nyh) * nxp + ii + nxh];
-        }
+        for (int t = lane; t < nT; t += 32) acc += tpsf[t] * base[toff[t]];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) out[r] = acc;
     }
 }
 
-void sparseops_init_attributes() {}
+void sparseops_init_attributes()
+{
+    cudaFuncSetAttribute(k_conv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_conv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
 
 // t = L s (image plane, active rows)
 void op_Ls(Work& w, int N_cap, const double* s, double* t, cudaStream_t st)
@@ -91,12 +103,15 @@ void op_conv(const StaticData& sd, Work& w, int N_cap, bool transpose, const dou
     cudaMemsetAsync(img, 0, sizeof(double) * npad, st);
     k_scatter_img<<<std::max(1, std::min((N_cap + 255) / 256, 152 * 8)), 256, 0, st>>>(sd, w.gs, w.rowpix, in,
                                                                                      scale_in, img);
+    // the tap tables are staged once per CTA: CTAs that loop over several
+    // rows amortise them (eight CTAs per SM resident)
+    const size_t smem = (sizeof(double) + sizeof(int)) * (size_t)sd.pnx * sd.pny;
     int blocks = (N_cap + 7) / 8;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > 152 * 8) blocks = 152 * 8;
     if (transpose)
-        k_conv<true><<<std::max(blocks, 1), 256, 0, st>>>(sd, w.gs, w.rowpix, img, out);
+        k_conv<true><<<std::max(blocks, 1), 256, smem, st>>>(sd, w.gs, w.rowpix, img, out);
     else
-        k_conv<false><<<std::max(blocks, 1), 256, 0, st>>>(sd, w.gs, w.rowpix, img, out);
+        k_conv<false><<<std::max(blocks, 1), 256, smem, st>>>(sd, w.gs, w.rowpix, img, out);
     count_launches(2);
 }
 
