@@ -384,18 +384,12 @@ void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream
 
 // ---------------------------------------------------------------------------
 // L in CSR (assign_Lmatrix, pixelgrid.cpp:13259-13321): per active row, the
-// mapped sub-pixels in sub-cell order, 3 entries each.  The row is also
-// written with duplicate source indices merged (summed in CSR order, i.e.
-// exactly the row of convert_Lmatrix_to_dense, pixelgrid.cpp:13734-13739),
+// mapped sub-pixels in sub-cell order, 3 entries each.  The same thread also
+// writes the row with duplicate source indices merged (summed in CSR order,
+// i.e. exactly the row of convert_Lmatrix_to_dense, pixelgrid.cpp:13734-13739),
 // which the PSF kernel gathers from.
-// One warp per row: the lanes place the sub-pixels' entries (a ballot prefix
-// keeps sub-cell order), then each lane takes entries a = lane, lane + 32, ...
-// and, if a is the first occurrence of its source index, sums that index's
-// values from a onwards in CSR order; a second ballot prefix writes the
-// merged entries in first-occurrence order.  The sums run in the same order
-// as a serial merge, so the bits do not depend on the lane split.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_build_L(StaticData sd_, const int* __restrict__ rowidx,
+__global__ void __launch_bounds__(128) k_build_L(StaticData sd_, const int* __restrict__ rowidx,
                                                  const int* __restrict__ rowptr, const int* __restrict__ cell3,
                                                  const double* __restrict__ w3, const int* __restrict__ active_index,
                                                  int* __restrict__ Lidx, double* __restrict__ Lval,
@@ -404,52 +398,34 @@ __global__ void __launch_bounds__(256) k_build_L(StaticData sd_, const int* __re
 {
     const StaticData sd = eval_shape(sd_);
     const int nsub = sd.nsub;
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); m < sd.n_mask; m += warps) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
         const int r = rowidx[m];
-        if (r < 0) continue;                           // warp-uniform
+        if (r < 0) continue;
         const int e0 = rowptr[r];
-        // entries of the mapped sub-pixels, in sub-cell order
-        int n = 0;
-        for (int k0 = 0; k0 < nsub; k0 += 32) {
-            const int k = k0 + lane;
+        int e = e0;
+        for (int k = 0; k < nsub; k++) {
             const int t = m * nsub + k;
-            const bool mapped = (k < nsub) && cell3[3 * t] >= 0;
-            const unsigned b = __ballot_sync(0xffffffffu, mapped);
-            if (mapped) {
-                const int e = e0 + n + 3 * __popc(b & below);
-                for (int u = 0; u < 3; u++) {
-                    Lidx[e + u] = active_index[cell3[3 * t + u]];
-                    Lval[e + u] = w3[3 * t + u];
-                }
+            if (cell3[3 * t] < 0) continue;
+            for (int u = 0; u < 3; u++) {
+                Lidx[e] = active_index[cell3[3 * t + u]];
+                Lval[e] = w3[3 * t + u];
+                e++;
             }
-            n += 3 * __popc(b);
         }
-        __syncwarp();
-        // merged row: first occurrences in order, each summed from 0 in CSR order
+        // merged row: first occurrence order, values summed in CSR order from 0
         int nc = 0;
-        for (int a0 = 0; a0 < n; a0 += 32) {
-            const int a = a0 + lane;
-            int idx = -1;
-            bool first = false;
+        for (int a = e0; a < e; a++) {
+            const int idx = Lidx[a];
+            bool first = true;
+            for (int b = e0; b < a; b++) if (Lidx[b] == idx) { first = false; break; }
+            if (!first) continue;
             double v = 0.0;
-            if (a < n) {
-                idx = Lidx[e0 + a];
-                first = true;
-                for (int b = 0; b < a; b++) if (Lidx[e0 + b] == idx) { first = false; break; }
-                if (first) for (int b = a; b < n; b++) if (Lidx[e0 + b] == idx) v += Lval[e0 + b];
-            }
-            const unsigned fb = __ballot_sync(0xffffffffu, first);
-            if (first) {
-                const int o = e0 + nc + __popc(fb & below);
-                cidx[o] = idx;
-                cval[o] = v;
-            }
-            nc += __popc(fb);
+            for (int b = a; b < e; b++) if (Lidx[b] == idx) v += Lval[b];
+            cidx[e0 + nc] = idx;
+            cval[e0 + nc] = v;
+            nc++;
         }
-        if (lane == 0) ccnt[r] = nc;
+        ccnt[r] = nc;
     }
 }
 
@@ -457,10 +433,11 @@ void launch_build_L(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream
 {
     (void)so;
     if (sd.n_mask == 0) return;
-    int blocks = (sd.n_mask + 7) / 8;                  // a warp per masked pixel
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    k_build_L<<<blocks, 256, 0, st>>>(sd, w.rowidx, w.rowptr, w.cell3, w.w3, w.active_index, w.Lidx, w.Lval, w.cidx,
-                                       w.cval, w.ccnt);
+    // a thread per masked pixel, each a long serial merge: 32-thread CTAs spread
+    // the few warps over all SMs
+    int blocks = (sd.n_mask + 31) / 32;
+    k_build_L<<<blocks, 32, 0, st>>>(sd, w.rowidx, w.rowptr, w.cell3, w.w3, w.active_index, w.Lidx, w.Lval, w.cidx,
+                                      w.cval, w.ccnt);
     count_launches(1);
 }
 
