@@ -111,6 +111,45 @@ def whole_job_evals(batch, steps, world):
     return batch * steps * world
 
 
+def write_trace(pl, run_step, k, path):
+    """One batched step (step k's parameters), kernel by kernel, under
+    torch.profiler's CUPTI activity records; per kernel: launches, summed
+    duration, and duration x min(1, CTAs / 152), a proxy for its share of the
+    SMs while the evaluations' kernels overlap.  Untimed, after the measured
+    region."""
+    import collections
+    import json
+    import tempfile
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    pl.set_graphs(False)                 # CUPTI reports kernels launched one by one
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        run_step(k)
+        torch.cuda.synchronize()
+    pl.set_graphs(True)
+    with tempfile.NamedTemporaryFile(suffix=".json", delete=False) as f:
+        tmp = f.name
+    prof.export_chrome_trace(tmp)
+    ev = [e for e in json.load(open(tmp))["traceEvents"] if e.get("cat") == "kernel"]
+    os.remove(tmp)
+    t0 = min(e["ts"] for e in ev)
+    t1 = max(e["ts"] + e["dur"] for e in ev)
+    agg = collections.defaultdict(lambda: [0, 0.0, 0.0])
+    for e in ev:
+        g = e["args"].get("grid", [1, 1, 1])
+        ctas = g[0] * g[1] * g[2]
+        a = agg[e["name"].split("(")[0]]
+        a[0] += 1
+        a[1] += e["dur"]
+        a[2] += e["dur"] * min(1.0, ctas / 152.0)
+    tot = sum(a[2] for a in agg.values())
+    rows = [{"kernel": n, "launches": a[0], "us": a[1], "sm_weighted_us": a[2], "sm_weighted_share": a[2] / tot}
+            for n, a in sorted(agg.items(), key=lambda x: -x[1][2])]
+    json.dump({"span_us": t1 - t0, "kernels": len(ev), "sm_weighted_us": tot, "rows": rows}, open(path, "w"),
+              indent=1)
+
+
 def make_context(wl, precision):
     from qlens_gb300 import PixelLikelihood, abi
     prec = abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64
@@ -188,6 +227,9 @@ def main():
     ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--trace", default="",
+                    help="after the measurement, record one more step's kernel timeline (launched kernel by kernel, "
+                         "through torch.profiler) and write a per-kernel summary to this JSON file")
     ap.add_argument("--regopt", action="store_true",
                     help="choose lambda per evaluation by Brent's method (QLens 'optimize_regparam on')")
     ap.add_argument("--no-autotune", action="store_true",
@@ -340,6 +382,9 @@ def main():
                 "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_note, "algorithmic_flops_per_launch": flops,
                 "timing": "CUDA events around the SYRK launch of single evaluations after the timed region"}
+
+    if args.trace and rank == 0:
+        write_trace(pl, run_step, args.warmup, args.trace)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
