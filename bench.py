@@ -123,16 +123,23 @@ def write_trace(pl, run_step, k, path):
     import torch
     from torch.profiler import ProfilerActivity, profile
     pl.set_graphs(False)                 # CUPTI reports kernels launched one by one
-    torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CUDA]) as prof:
-        run_step(k)
+    ev = []
+    for attempt in range(2):             # the first session of a process may come back empty
         torch.cuda.synchronize()
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            run_step(k)
+            torch.cuda.synchronize()
+        with tempfile.NamedTemporaryFile(suffix=".json", delete=False) as f:
+            tmp = f.name
+        prof.export_chrome_trace(tmp)
+        ev = [e for e in json.load(open(tmp))["traceEvents"] if e.get("cat") == "kernel"]
+        os.remove(tmp)
+        if ev:
+            break
     pl.set_graphs(True)
-    with tempfile.NamedTemporaryFile(suffix=".json", delete=False) as f:
-        tmp = f.name
-    prof.export_chrome_trace(tmp)
-    ev = [e for e in json.load(open(tmp))["traceEvents"] if e.get("cat") == "kernel"]
-    os.remove(tmp)
+    if not ev:
+        json.dump({"unavailable": "the profiler recorded no kernels"}, open(path, "w"))
+        return
     t0 = min(e["ts"] for e in ev)
     t1 = max(e["ts"] + e["dur"] for e in ev)
     agg = collections.defaultdict(lambda: [0, 0.0, 0.0])
