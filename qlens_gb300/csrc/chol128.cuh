@@ -27,7 +27,7 @@ namespace qlpix {
 
 #define C2 128
 #define P128_SMEM (2 * C2 * (C2 + 1) * 4 + 32 * 33 * 4 + C2 * 4)         // S, V, T, 1/diag
-#define T128_SMEM (8 * TC_TILE_BYTES + 1024)                             // [A/B][kb][hi/lo], one K half
+#define T128_SMEM (4 * TC_TILE_BYTES + 1024)                             // [A/B][hi/lo], one K quarter
 
 __device__ __forceinline__ int cpad128(int M) { return (M + C2 - 1) / C2 * C2; }
 
@@ -209,48 +209,45 @@ __global__ void __launch_bounds__(256, 1) k_potrf128(float* __restrict__ A, int 
     }
 }
 
-// Load rows [g0, g0+128) x columns [col, col+64) of `src` (row stride lds),
-// split into TF32 hi + lo, into the two kb tiles (128 rows x 32 floats,
-// 128-byte swizzle) of operand `op`.
-__device__ __forceinline__ void load_split_half(const float* __restrict__ src, size_t lds, int g0, int col,
-                                                unsigned char* t_hi0, unsigned char* t_lo0, unsigned char* t_hi1,
-                                                unsigned char* t_lo1)
+// One K quarter (32 columns from col) of 128 rows from g0: split into TF32
+// hi + lo, stored in the SW128 layout of one K block.
+__device__ __forceinline__ void load_split_quarter(const float* __restrict__ src, size_t lds, int g0, int col,
+                                                   unsigned char* t_hi, unsigned char* t_lo)
 {
-    #pragma unroll 1
-    for (int base_idx = threadIdx.x; base_idx < TC_TILE * 16; base_idx += 8 * 128) {
-        float4 vv[8];
+    float4 vv[8];
+    #pragma unroll
+    for (int u = 0; u < 8; u++) {
+        const int idx = threadIdx.x + u * 128;
+        const int row = idx >> 3, q = idx & 7;
+        vv[u] = *reinterpret_cast<const float4*>(src + (size_t)(g0 + row) * lds + col + q * 4);
+    }
+    #pragma unroll
+    for (int u = 0; u < 8; u++) {
+        const int idx = threadIdx.x + u * 128;
+        const int row = idx >> 3, kcol = (idx & 7) * 4;
+        float x[4] = {vv[u].x, vv[u].y, vv[u].z, vv[u].w};
+        float h[4], l[4];
         #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const int idx = base_idx + u * 128;
-            const int row = idx >> 4, q = idx & 15;
-            vv[u] = *reinterpret_cast<const float4*>(src + (size_t)(g0 + row) * lds + col + q * 4);
+        for (int e = 0; e < 4; e++) {
+            uint32_t uu;
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(uu) : "f"(x[e]));
+            h[e] = __uint_as_float(uu);
+            const float lo = x[e] - h[e];
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(uu) : "f"(lo));
+            l[e] = __uint_as_float(uu);
         }
-        #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const int idx = base_idx + u * 128;
-            const int row = idx >> 4, q = idx & 15;
-            const int kb = q >> 3, kcol = (q & 7) * 4;
-            float x[4] = {vv[u].x, vv[u].y, vv[u].z, vv[u].w};
-            float h[4], l[4];
-            #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                uint32_t uu;
-                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(uu) : "f"(x[e]));
-                h[e] = __uint_as_float(uu);
-                const float lo = x[e] - h[e];
-                asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(uu) : "f"(lo));
-                l[e] = __uint_as_float(uu);
-            }
-            const uint32_t off = sw128_offset(row, kcol);
-            *reinterpret_cast<float4*>((kb ? t_hi1 : t_hi0) + off) = make_float4(h[0], h[1], h[2], h[3]);
-            *reinterpret_cast<float4*>((kb ? t_lo1 : t_lo0) + off) = make_float4(l[0], l[1], l[2], l[3]);
-        }
+        const uint32_t off = sw128_offset(row, kcol);
+        *reinterpret_cast<float4*>(t_hi + off) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(t_lo + off) = make_float4(l[0], l[1], l[2], l[3]);
     }
 }
 
 // mode 0: A_IJ -= P_I P_J^T (grid: lower-triangle tiles of the first `band`
 // block rows below step k); mode 1: P_I <- P_I Linv^T (grid: block rows).
-__global__ void __launch_bounds__(128, 1) k_chol_tile128(float* __restrict__ A, int ld, int k, GridState* gs, int mode,
+// K runs in four quarters of 32 columns (the same MMAs in the same order as
+// one pass over 128), so a CTA needs 65 KB of shared memory and three fit on
+// an SM: while one waits on its loads, the others' MMAs run.
+__global__ void __launch_bounds__(128, 3) k_chol_tile128(float* __restrict__ A, int ld, int k, GridState* gs, int mode,
                                                          const float* __restrict__ Linv, int band)
 {
     extern __shared__ unsigned char smem_raw[];
@@ -269,7 +266,7 @@ __global__ void __launch_bounds__(128, 1) k_chol_tile128(float* __restrict__ A, 
     const int o = k * C2;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    auto tile = [&](int op, int kb, int part) { return smem + ((op * 2 + kb) * 2 + part) * TC_TILE_BYTES; };
+    auto tile = [&](int op, int part) { return smem + (op * 2 + part) * TC_TILE_BYTES; };
 
     if (threadIdx.x == 0) {
         mbar_init(&done_bar, 1);
@@ -284,14 +281,12 @@ __global__ void __launch_bounds__(128, 1) k_chol_tile128(float* __restrict__ A, 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     bool ok = true;
-    for (int half = 0; half < 2 && ok; half++) {
-        load_split_half(A, (size_t)ld, r0, o + half * 64, tile(0, 0, 0), tile(0, 0, 1), tile(0, 1, 0), tile(0, 1, 1));
+    for (int qt = 0; qt < 4 && ok; qt++) {
+        load_split_quarter(A, (size_t)ld, r0, o + qt * 32, tile(0, 0), tile(0, 1));
         if (mode == 0)
-            load_split_half(A, (size_t)ld, c0, o + half * 64, tile(1, 0, 0), tile(1, 0, 1), tile(1, 1, 0),
-                            tile(1, 1, 1));
+            load_split_quarter(A, (size_t)ld, c0, o + qt * 32, tile(1, 0), tile(1, 1));
         else
-            load_split_half(Linv, (size_t)C2, 0, half * 64, tile(1, 0, 0), tile(1, 0, 1), tile(1, 1, 0),
-                            tile(1, 1, 1));
+            load_split_quarter(Linv, (size_t)C2, 0, qt * 32, tile(1, 0), tile(1, 1));
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
         __syncthreads();
@@ -299,25 +294,22 @@ __global__ void __launch_bounds__(128, 1) k_chol_tile128(float* __restrict__ A, 
         if (warp == 1 && lane == 0) {
             const uint32_t tmem = tmem_slot;
             const uint32_t idesc = idesc_tf32_128x128();
+            const uint64_t a_hi = sdesc_sw128(smem_u32(tile(0, 0)));
+            const uint64_t a_lo = sdesc_sw128(smem_u32(tile(0, 1)));
+            const uint64_t b_hi = sdesc_sw128(smem_u32(tile(1, 0)));
+            const uint64_t b_lo = sdesc_sw128(smem_u32(tile(1, 1)));
             #pragma unroll
-            for (int kb = 0; kb < 2; kb++) {
-                const uint64_t a_hi = sdesc_sw128(smem_u32(tile(0, kb, 0)));
-                const uint64_t a_lo = sdesc_sw128(smem_u32(tile(0, kb, 1)));
-                const uint64_t b_hi = sdesc_sw128(smem_u32(tile(1, kb, 0)));
-                const uint64_t b_lo = sdesc_sw128(smem_u32(tile(1, kb, 1)));
-                #pragma unroll
-                for (int kk = 0; kk < TC_KB / 8; kk++) {
-                    const uint64_t off = (uint64_t)((kk * 32) >> 4);
-                    mma_tf32(tmem, a_hi + off, b_hi + off, idesc, (half > 0 || kb > 0 || kk > 0) ? 1u : 0u);
-                    mma_tf32(tmem, a_hi + off, b_lo + off, idesc, 1u);
-                    mma_tf32(tmem, a_lo + off, b_hi + off, idesc, 1u);
-                }
+            for (int kk = 0; kk < TC_KB / 8; kk++) {
+                const uint64_t off = (uint64_t)((kk * 32) >> 4);
+                mma_tf32(tmem, a_hi + off, b_hi + off, idesc, (qt > 0 || kk > 0) ? 1u : 0u);
+                mma_tf32(tmem, a_hi + off, b_lo + off, idesc, 1u);
+                mma_tf32(tmem, a_lo + off, b_hi + off, idesc, 1u);
             }
             mma_commit(&done_bar);
         }
         __syncthreads();
         // the MMAs read shared memory asynchronously: wait before it is reused
-        ok = mbar_wait_bounded(&done_bar, (uint32_t)half, &abort_flag, false);
+        ok = mbar_wait_bounded(&done_bar, (uint32_t)(qt & 1), &abort_flag, false);
         tc_fence_after();
         __syncthreads();
     }
