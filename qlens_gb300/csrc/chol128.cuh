@@ -209,18 +209,22 @@ __global__ void __launch_bounds__(256, 1) k_potrf128(float* __restrict__ A, int 
     }
 }
 
-// One K quarter (32 columns from col) of 128 rows from g0: split into TF32
-// hi + lo, stored in the SW128 layout of one K block.
-__device__ __forceinline__ void load_split_quarter(const float* __restrict__ src, size_t lds, int g0, int col,
-                                                   unsigned char* t_hi, unsigned char* t_lo)
+// One K quarter (32 columns from col) of 128 rows from g0, eight float4 per
+// thread, into registers ...
+__device__ __forceinline__ void load_quarter(const float* __restrict__ src, size_t lds, int g0, int col,
+                                             float4 (&vv)[8])
 {
-    float4 vv[8];
     #pragma unroll
     for (int u = 0; u < 8; u++) {
         const int idx = threadIdx.x + u * 128;
         const int row = idx >> 3, q = idx & 7;
         vv[u] = *reinterpret_cast<const float4*>(src + (size_t)(g0 + row) * lds + col + q * 4);
     }
+}
+
+// ... then split into TF32 hi + lo and stored in the SW128 layout of one K block.
+__device__ __forceinline__ void store_split_quarter(const float4 (&vv)[8], unsigned char* t_hi, unsigned char* t_lo)
+{
     #pragma unroll
     for (int u = 0; u < 8; u++) {
         const int idx = threadIdx.x + u * 128;
@@ -246,7 +250,8 @@ __device__ __forceinline__ void load_split_quarter(const float* __restrict__ src
 // block rows below step k); mode 1: P_I <- P_I Linv^T (grid: block rows).
 // K runs in four quarters of 32 columns (the same MMAs in the same order as
 // one pass over 128), so a CTA needs 65 KB of shared memory and three fit on
-// an SM: while one waits on its loads, the others' MMAs run.
+// an SM: while one waits on its loads, the others' MMAs run.  Each quarter's
+// global loads are issued while the previous quarter's MMAs run.
 __global__ void __launch_bounds__(128, 3) k_chol_tile128(float* __restrict__ A, int ld, int k, GridState* gs, int mode,
                                                          const float* __restrict__ Linv, int band)
 {
@@ -281,12 +286,13 @@ __global__ void __launch_bounds__(128, 3) k_chol_tile128(float* __restrict__ A, 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     bool ok = true;
+    float4 ra[8], rb[8];
+    load_quarter(A, (size_t)ld, r0, o, ra);
+    if (mode == 0) load_quarter(A, (size_t)ld, c0, o, rb);
+    else load_quarter(Linv, (size_t)C2, 0, 0, rb);
     for (int qt = 0; qt < 4 && ok; qt++) {
-        load_split_quarter(A, (size_t)ld, r0, o + qt * 32, tile(0, 0), tile(0, 1));
-        if (mode == 0)
-            load_split_quarter(A, (size_t)ld, c0, o + qt * 32, tile(1, 0), tile(1, 1));
-        else
-            load_split_quarter(Linv, (size_t)C2, 0, qt * 32, tile(1, 0), tile(1, 1));
+        store_split_quarter(ra, tile(0, 0), tile(0, 1));
+        store_split_quarter(rb, tile(1, 0), tile(1, 1));
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
         __syncthreads();
@@ -306,6 +312,12 @@ __global__ void __launch_bounds__(128, 3) k_chol_tile128(float* __restrict__ A, 
                 mma_tf32(tmem, a_lo + off, b_hi + off, idesc, 1u);
             }
             mma_commit(&done_bar);
+        }
+        // the next quarter's loads fly while the MMAs run
+        if (qt + 1 < 4) {
+            load_quarter(A, (size_t)ld, r0, o + (qt + 1) * 32, ra);
+            if (mode == 0) load_quarter(A, (size_t)ld, c0, o + (qt + 1) * 32, rb);
+            else load_quarter(Linv, (size_t)C2, 0, (qt + 1) * 32, rb);
         }
         __syncthreads();
         // the MMAs read shared memory asynchronously: wait before it is reused
