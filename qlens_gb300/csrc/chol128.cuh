@@ -12,7 +12,7 @@
 //                    blocks below, mode 0 (trailing update): A_IJ -= P_I P_J^T
 //                    for the lower-triangle tiles -- both as 128x128x128
 //                    products on the tensor cores (tcgen05 kind::tf32, 3xTF32
-//                    split, accumulator in TMEM), K in two halves of 64.
+//                    split, accumulator in TMEM), K in four quarters of 32.
 // `band` limits both to the tiles within that many 128-blocks of the
 // diagonal: the curvature matrix R couples a cell only to cells at most two
 // grid rows away, so its factor stays inside that band (dense F passes a
