@@ -126,7 +126,7 @@ int ctx_autotune(qlp_ctx* c, const double* params, const double* lambdas, const 
     }
     r.start_ms = best_ms;
     const std::vector<Knob> knobs = {
-        {&qlp_schedule::slots, {8, 16, 32, 64}},
+        {&qlp_schedule::slots, {8, 16, 32, 48, 64}},
         {&qlp_schedule::psfx_mode, {0, 1}},
         {&qlp_schedule::psfx_threads, {128, 256, 512}},
         {&qlp_schedule::psfx_split, {1, 2, 4}},
