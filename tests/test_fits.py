@@ -120,3 +120,29 @@ def test_errors(tmp_path):
     (tmp_path / "edge.fits").write_bytes(make_fits.hdu_bytes(p, -64, True))
     with pytest.raises(QLPixError):
         pl.load_psf_fits(str(tmp_path / "edge.fits"), 1e-2)
+
+
+def test_header_keyword_rules(tmp_path):
+    """QLens's scan of a data image's header (pixelgrid.cpp:6059-6116): a card
+    holding 'ql: ' opens a run of COMMENT cards that the scan reads as text,
+    and the first card after the run that is not a COMMENT ends the scan --
+    keywords after it are not read; keywords before it are."""
+    pl = _pl()
+    img = np.arange(12, dtype=np.float64).reshape(4, 3)
+    extra = [make_fits.card("PXNOISE", 0.5), make_fits.card("ZLENS", 0.3),
+             make_fits.comment_card("ql: model description"), make_fits.comment_card("second line"),
+             make_fits.card("PXSIZE", 0.07), make_fits.card("ZSRC", 2.0)]
+    f = tmp_path / "hdr.fits"
+    f.write_bytes(make_fits.hdu_bytes(img, -64, True, extra=extra))
+    data, info = pl.fits_read_image(str(f))
+    assert np.array_equal(data, img)
+    assert info["has_pxnoise"] and info["pxnoise"] == 0.5
+    assert info["has_zlens"] and info["zlens"] == 0.3
+    assert not info["has_pxsize"] and not info["has_zsrc"]
+    # without the comment run every keyword is read, and PXSIZE sets the grid
+    f2 = tmp_path / "hdr2.fits"
+    f2.write_bytes(make_fits.hdu_bytes(img, -64, True, extra=[make_fits.card("PXSIZE", 0.07),
+                                                              make_fits.card("ZSRC", 2.0)]))
+    xv, yv, d, info = pl.load_data_fits(str(f2), pixel_size=0.5)
+    assert info["has_pxsize"] and info["pxsize"] == 0.07 and info["zsrc"] == 2.0
+    assert xv[0] == -0.5 * 4 * 0.07 and yv[0] == -0.5 * 3 * 0.07      # the file's PXSIZE wins
