@@ -134,3 +134,25 @@ def test_batch_size_follows_acceptance_rate():
         assert sizes[0] == want, (rate, sizes)
         assert sum(sizes) == 100                 # never past max_candidates
         assert sizes[1] == min(64, 100 - sizes[0])   # nothing accepted: the rate drops to 0
+
+
+def test_prior_term_and_flat_likelihood_plateaus():
+    """A non-flat prior term (QLens's LogPrior added to -log L) and a
+    likelihood with exact ties: the batched run still equals the serial one,
+    and every accepted replacement beats the point it replaced."""
+    def lp(x):
+        return 0.5 * float(np.sum((x / 3.0) ** 2))
+
+    def stepped(X):
+        return np.floor(4 * gauss_nll(X)) / 4           # ties between candidates
+
+    runs = []
+    for batch in [(1, 1), (2, 16)]:
+        ns = NestedSampler(FunctionTarget(stepped, 2), [-5, -5], [5, 5], 40, seed=9, log_prior=lp, batch=batch)
+        runs.append(ns.run(max_dead=400))
+    a, b = runs
+    assert a["count"] == b["count"] and a["tries"] == b["tries"] and a["lnZ"] == b["lnZ"]
+    for (xa, la, pa), (xb, lb, pb) in zip(a["dead"], b["dead"]):
+        assert np.array_equal(xa, xb) and la == lb and pa == pb
+    L = [d[1] for d in a["dead"]]
+    assert all(L[k + 1] <= L[k] for k in range(len(L) - 1))   # dead points in decreasing -log L order
