@@ -41,3 +41,29 @@ def test_noise_term_vs_oracle(name, precision):
     again = pl.invert_image_surface_brightness_map()
     assert abs(again["m2logev"] - off["m2logev"]) <= 1e-12 * abs(off["m2logev"]) + (0 if precision == 0 else 1e-9)
     pl.close()
+
+
+def test_noise_term_with_lambda_optimisation_and_outside_prior():
+    """The options together, as a fit script would set them: the noise term,
+    the lambda optimisation and the outside-surface-brightness prior, plain
+    FP64 against the oracle with the same three settings."""
+    from qlens_gb300 import PixelLikelihood
+    g = Golden("osb_tiny_sie")
+    osb = dict(frac=g.sc["outside_sb_prior_threshold"], noise_frac=g.sc["outside_sb_prior_noise_frac"],
+               emask_nsplit=int(g.sc["emask_nsplit"]), emask=g.arr["emask"])
+    want = O.evaluate(g.image, g.psf, g.opts, g.lenses, planes=g.planes(), noise_term=True,
+                      regopt=(-3.0, 5.0, 0.01, 20), outside_sb=osb)
+    pl = PixelLikelihood.from_opts(g.image, g.psf, g.opts, precision=0)
+    pl.set_lens_model(g.lenses, *g.zbeta())
+    pl.set_noise_term(True)
+    pl.set_regparam_optimization(True)
+    pl.set_outside_sb_prior(True, osb["frac"], osb["noise_frac"], osb["emask"].reshape(g.nx, g.ny),
+                            osb["emask_nsplit"])
+    r = pl.invert_image_surface_brightness_map()
+    assert r["status"] == want["status"] == 0
+    assert abs(r["regparam"] - want["regparam"]) <= 1e-6 * want["regparam"]
+    assert abs(r["m2logev"] - want["m2logev"]) <= 1e-6 * abs(want["m2logev"]), (r["m2logev"], want["m2logev"])
+    b = pl.eval_batch(np.tile(np.array(g.params()), (2, 1)))
+    for x in b:
+        assert abs(x["m2logev"] - r["m2logev"]) <= 1e-9 * abs(r["m2logev"])
+    pl.close()
