@@ -422,6 +422,15 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "stage_ms_single_eval": [float(x) for x in stage],
+            # the factorisation stage of one evaluation (stage 4: Cholesky of F and of R's band, the
+            # triangular solves, the refinement): algorithmic M^3/3 multiply-adds of F's Cholesky
+            # over the stage's event time -- a pivot chain of M/128 steps, latency-bound for one
+            # evaluation; the batch overlaps 32 of them
+            "cholesky_stage": {
+                "ms": float(stage[4]),
+                "algorithmic_tflop": float(np.mean([2.0 * r["n_active_src"] ** 3 / 3.0 for r in iso_res])) / 1e12,
+                "achieved_tflops": (float(np.mean([2.0 * r["n_active_src"] ** 3 / 3.0 for r in iso_res]))
+                                    / (stage[4] / 1e3) / 1e12) if stage[4] > 0 else None},
             "graphs": not args.no_graphs,
             "failed_evals": len(bad),
             "regopt": ({"lambda_trials_per_eval": float(np.mean([r["regopt_evals"] for r in results])),
