@@ -10,7 +10,7 @@ from goldens import Golden
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = {"slots": {1, 2, 3, 4, 8, 16, 32, 64}, "ray_threads": {64, 128, 256},
+CANDIDATES = {"slots": {1, 2, 3, 4, 8, 16, 32, 48, 64}, "ray_threads": {64, 128, 256},
               "psfx_threads": {128, 256, 512}, "psfx_split": {1, 2, 4}, "psfx_mode": {0, 1}}
 
 
