@@ -33,9 +33,12 @@ struct NoAllocScratch {
 };
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-// Single block: copy the lower triangle of F, right-looking Cholesky
-// (Cholesky_dcmp_packed semantics: a negative pivot is recorded and sqrt(|d|)
-// used), log det = 2 sum log L_ii, then L y = D and L^T s = y.
+// Single block: copy the lower triangle of F, right-looking Cholesky, log det
+// = 2 sum log L_ii, then L y = D and L^T s = y.  A pivot d <= 0 is recorded in
+// the status (the first one's index + 1) and the factorisation continues with
+// sqrt(|d|), so the call always ends; the reference's Cholesky_dcmp_packed
+// (pixelgrid.cpp:17071-17105) flags only d < 0 and would divide by a zero
+// pivot.  After a recorded pivot the outputs are not meaningful.
 __global__ void __launch_bounds__(1024) k_spd_solve_logdet_noalloc(NoAllocScratch* __restrict__ scr,
                                                                    const double* __restrict__ F, int n, int ld,
                                                                    const double* __restrict__ D,
@@ -101,7 +104,9 @@ __global__ void __launch_bounds__(1024) k_spd_solve_logdet_noalloc(NoAllocScratc
     for (int i = tid; i < n; i += nth) s[i] = y[i];
 }
 
-// Device address of the scratch, looked up once per device.
+// Device address of the scratch, looked up once per device (on the first call
+// made with that device current) and kept: a cudaDeviceReset by the caller
+// would leave it stale, so the entry point is not for use after one.
 static std::mutex g_noalloc_mu;
 static NoAllocScratch* g_noalloc_ptr[64];
 static bool g_noalloc_ready[64];
@@ -146,15 +151,13 @@ int spd_solve_logdet_noalloc(const double* F, int n, int ld, const double* D, do
     cudaStream_t st = (cudaStream_t)stream;
     k_spd_solve_logdet_noalloc<<<1, 1024, 0, st>>>(scr, F, n, ld, D, s, logdet);
     count_launches(1);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-        err = std::string("qlp_spd_solve_logdet_noalloc: ") + cudaGetErrorString(e);
-        return QLP_ERR_CUDA;
-    }
+    // the status word follows the kernel on the same stream; one wait for both
     int status = 0;
-    e = cudaMemcpyFromSymbol(&status, g_noalloc_scratch, sizeof(int), offsetof(NoAllocScratch, status),
-                             cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyFromSymbolAsync(&status, g_noalloc_scratch, sizeof(int), offsetof(NoAllocScratch, status),
+                                      cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         err = std::string("qlp_spd_solve_logdet_noalloc: ") + cudaGetErrorString(e);
         return QLP_ERR_CUDA;
