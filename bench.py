@@ -1,19 +1,26 @@
 """Throughput of the GB300 pixel-image likelihood (evaluations per second).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl qlpix|reference]
-                    [--config cfg2] [--batch B] [--precision mixed|fp64]
+                    [--config cfg5] [--batch B] [--precision mixed|fp64]
 
 A step is one batch of B likelihood evaluations: B lens-parameter vectors are
 drawn from the configuration's prior box and evaluated through the public C
-ABI (qlp_eval_batch).  The default workload is the reference's larger
-single-likelihood configuration (200x200 pixels at 0.04", annular mask,
-4x4 split, 21x21 Airy-like PSF, 64x64 source grid, power-law lens + shear),
-on seeded synthetic data.  `value` is evaluations per second of device time
-(inputs resident: image, mask and PSF are uploaded once when the context is
-created); `e2e` is the same metric through the public call with the step's
+ABI (qlp_eval_batch).  The default workload is the metric's own: the two-plane
+subhalo configuration (300x300 pixels at 0.03", annulus 0.3"-3.5", 4x4 split,
+31x31 Airy-like PSF; SIE + shear at z = 0.5, an elliptical NFW subhalo at
+z = 0.8 given by its mass, 1e8-1e10 M_sun; source at z = 2), 1024 vectors per
+step, each with its own source grid (side 32-64), on seeded synthetic data,
+evaluated in mixed precision with the NFW deflection from the trained
+surrogate (quadrature fallback).  `value` is evaluations per second of device
+time (inputs resident: image, mask and PSF are uploaded once when the context
+is created); `e2e` is the same metric through the public call with the step's
 parameter vectors in pinned host memory and the results read back, timed on
-the host.  Under torchrun every rank evaluates its own batches (replicas, weak
-scaling) and the slowest rank's time counts.
+the host.  After the timed region the same run evaluates a sample of the
+timed vectors on the plain FP64 path (NFW by quadrature) and reports its
+throughput, the ratio (`vs_plain_fp64`) and the largest |delta log L|
+between the two paths on that sample (`accuracy`).  Under torchrun every rank
+evaluates its own batches (replicas, weak scaling) and the slowest rank's
+time counts.
 
 --impl reference times the reference's CPU implementation of the same
 workload (the oracle port of QLens's dense inversion, OpenMP over all host
@@ -35,9 +42,6 @@ sys.path.insert(0, ROOT)
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
-
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_syrk_tc launch on cfg2 (ncu, GB300)
-SYRK_TC_DRAM_BYTES_CFG2 = 115.223e6 + 9.662e6
 
 METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 at |ΔlogL|<0.1"
 UNIT = "evals/s"
@@ -175,20 +179,56 @@ def algorithmic_syrk_flops(res):
     return tot
 
 
-def cpu_port_eval(wl, params, threads=None):
-    """One evaluation of the oracle port (CPU) on the workload; returns seconds."""
+def instance_of(wl, inst, i):
+    """(mask array, (src nx, src ny), lambda) of vector i of a batch drawn by
+    wl.draw_instances (inst = its (mask ids, source sizes, lambdas)), or the
+    workload's own for a batch without per-vector instances."""
+    ids, sizes, lam = inst
+    mask = wl.mask if ids is None or ids[i] < 0 else wl.instance_masks[ids[i]].reshape(wl.mask.shape)
+    src = tuple(wl.src_npixels) if sizes is None else tuple(int(v) for v in sizes[i])
+    reg = wl.regparam if lam is None else float(lam[i])
+    return mask, src, reg
+
+
+def cpu_port_eval(wl, params, inst=(None, None, None), i=0):
+    """One evaluation of the oracle port (CPU, OpenMP over the host's cores)
+    on vector i of a batch; returns (seconds, result)."""
     from oracle import oracle as O
     from qlens_gb300 import abi
-    img = abi.ImageBuffers(wl.xvals, wl.yvals, wl.data, wl.mask, None, wl.noise)
+    mask, src, reg = instance_of(wl, inst, i)
+    img = abi.ImageBuffers(wl.xvals, wl.yvals, wl.data, mask, None, wl.noise)
     psf = abi.PSFBuffer(wl.psf)
     o = abi.srcgrid_defaults()
     o.nsplit = wl.nsplit
-    o.npixels_x, o.npixels_y = wl.src_npixels
-    o.regparam = wl.regparam
-    t = time.perf_counter()
+    o.npixels_x, o.npixels_y = src
+    o.regparam = reg
     planes = abi.make_planes(getattr(wl, "zfac", None), getattr(wl, "beta", None))
+    t = time.perf_counter()
     r = O.evaluate(img, psf, o, wl.lenses, lens_params=params, planes=planes)
     return time.perf_counter() - t, r
+
+
+def draw_one(wl, rng):
+    p = wl.draw(rng, 1)
+    inst = wl.draw_instances(rng, 1) if wl.draw_instances is not None else (None, None, None)
+    return p[0], inst
+
+
+def cpu_sample(wl, rng, budget_s, max_n):
+    """Evaluations of the oracle port on fresh draws of the workload, one at a
+    time, until max_n are done or their time exceeds budget_s (at least one)."""
+    times = []
+    while len(times) < max_n:
+        p, inst = draw_one(wl, rng)
+        dt, _r = cpu_port_eval(wl, p, inst)
+        times.append(dt)
+        if sum(times) > budget_s:
+            break
+    return times
+
+
+REF_BUDGET_S = 150.0     # wall-clock bound of the reference arm's timed evaluations
+CPU_BUDGET_S = 30.0      # ... and of the cpu_baseline sample beside the GPU line
 
 
 def run_reference(args, rank, world):
@@ -200,40 +240,60 @@ def run_reference(args, rank, world):
     wl = synthetic.CONFIGS[args.config]()
     rng = np.random.default_rng(4321)
     cores = O.threads()
-    for _ in range(args.warmup):
-        cpu_port_eval(wl, wl.draw(rng, 1)[0])
-    times = []
-    for _ in range(args.steps):
-        dt, _r = cpu_port_eval(wl, wl.draw(rng, 1)[0])
-        times.append(dt)
+    # one untimed warm-up evaluation (page-in, thread start-up); more would
+    # only repeat it: the port keeps no state between evaluations
+    cpu_port_eval(wl, *draw_one(wl, rng))
+    times = cpu_sample(wl, rng, REF_BUDGET_S, max(1, args.steps))
     total = sum(times)
-    value = args.steps / total
+    value = len(times) / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl.name, "batch_per_step": 1, **wl.describe()},
+        "config": {**wl.describe(), "batch_per_step": 1},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d evaluations, one per step, OpenMP over %d host threads" % (args.steps, cores)},
+                         "sample": "%d evaluations of fresh draws, one per step (steps stop once their time "
+                                   "exceeds %.0f s), after 1 warm-up evaluation; OpenMP over %d host threads; "
+                                   "median %.2f s" % (len(times), REF_BUDGET_S, cores, statistics.median(times))},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
+def plain_fp64_arm(wl, params, inst, n, slots):
+    """The plain FP64 path (FP64 SYRK, Cholesky and solves; the NFW deflection
+    by quadrature) on the first n vectors of a timed batch: one warm-up batch
+    (graph capture), then the n vectors as one batch; returns (evaluations per
+    second of device time, results)."""
+    pl = make_context(wl, "fp64")
+    pl.set_batch_slots(slots)
+    pl.set_graphs(True)
+    ids, sizes, lam = inst
+    sl = lambda a, k: None if a is None else a[:k]   # noqa: E731
+    k0 = min(n, slots)
+    pl.eval_batch(params[:k0], regparams=sl(lam, k0), mask_ids=sl(ids, k0), src_sizes=sl(sizes, k0))
+    res = pl.eval_batch(params[:n], regparams=sl(lam, n), mask_ids=sl(ids, n), src_sizes=sl(sizes, n))
+    ms = pl.last_device_ms()
+    pl.close()
+    return n / (ms / 1e3), res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="qlpix", choices=["qlpix", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
-    ap.add_argument("--batch", type=int, default=0, help="evaluations per step (default per precision)")
+    ap.add_argument("--config", default="cfg5", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5", "cfg5_fixed"])
+    ap.add_argument("--batch", type=int, default=0, help="evaluations per step (default: the workload's)")
     ap.add_argument("--slots", type=int, default=0, help="concurrent evaluation slots (default min(batch, 32))")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernel by kernel instead of replaying graphs")
     ap.add_argument("--precision", default=os.environ.get("QLPIX_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=32,
+                    help="vectors of the first timed batch evaluated again on the plain FP64 path (0: skip)")
     ap.add_argument("--trace", default="",
                     help="after the measurement, record one more step's kernel timeline (launched kernel by kernel, "
                          "through torch.profiler) and write a per-kernel summary to this JSON file")
@@ -265,19 +325,16 @@ def main():
     wl = synthetic.CONFIGS[args.config]()
     precision = args.precision
     pl = make_context(wl, precision)
-    try:
-        pl.set_precision(abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64)
-        probe = pl.invert_image_surface_brightness_map(wl.draw(np.random.default_rng(0), 1)[0])
-        if probe["status"] != 0:
-            raise RuntimeError("mixed path status %d" % probe["status"])
-    except Exception:
-        precision = "fp64"
-        pl.set_precision(abi.QLP_FP64)
+    pl.set_precision(abi.QLP_MIXED if precision == "mixed" else abi.QLP_FP64)
+    probe = pl.invert_image_surface_brightness_map(wl.draw(np.random.default_rng(0), 1)[0])
+    if probe["status"] != 0:
+        raise RuntimeError("%s path status %d" % (precision, probe["status"]))
     # workloads with an elliptical NFW lens: train the deflection surrogate on
     # this GPU before the timed region (once per process), then ray-trace
     # through it with the default error gate
     nfw = None
-    if any(l["type"] == "nfw" for l in wl.lenses):
+    has_nfw = any(l["type"] in abi.NFW_TYPES for l in wl.lenses)
+    if has_nfw:
         nfw = {"mode": "quadrature"}
         if args.nfw == "surrogate":
             from qlens_gb300 import pixlike
@@ -287,10 +344,10 @@ def main():
                    "val_mean_rel": rep["val_mean_rel"], "n_params": rep["n_params"]}
     if args.regopt:
         pl.set_regparam_optimization(True)
-    uneven = wl.draw_instances is not None      # per-instance masks, source grids and lambdas
-    if uneven:
+    uneven = wl.draw_instances is not None      # per-vector masks, source grids or lambdas
+    if wl.instance_masks is not None:
         pl.set_instance_masks(wl.instance_masks)
-    B = args.batch or (4096 if uneven else 32 if precision == "mixed" else 4)
+    B = args.batch or wl.batch or (32 if precision == "mixed" else 4)
     pl.set_batch_slots(args.slots or min(B, 32))
     pl.set_graphs(not args.no_graphs)
     stream = torch.cuda.current_stream()
@@ -370,7 +427,7 @@ def main():
         stage += np.array(pl.stage_times())
     stage /= len(iso)
 
-    # roofline of the dominant tensor-core kernel: the F = L'^T C^-1 L' contraction
+    # roofline of the tensor-core contraction F = L'^T C^-1 L'
     peaks = _peaks()
     syrk_ms = stage[3]
     flops = algorithmic_syrk_flops(iso_res) / len(iso)
@@ -383,22 +440,40 @@ def main():
         peak = 1.25
         peak_note = "nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)"
         bound = "fp64"
-    # DRAM bytes of one k_syrk_tc launch on cfg2 from one ncu capture (profiles/k_syrk_tc_cfg2.md)
-    traffic = SYRK_TC_DRAM_BYTES_CFG2 if (precision == "mixed" and args.config == "cfg2") else None
     roofline = {"bound": bound, "kernel": "F = L'^T C^-1 L' (SYRK)", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
                 "peak_source": peak_note, "algorithmic_flops_per_launch": flops,
                 "timing": "CUDA events around the SYRK launch of single evaluations after the timed region"}
 
     if args.trace and rank == 0:
         write_trace(pl, run_step, args.warmup, args.trace)
 
+    # the plain FP64 path on the first vectors of the first timed batch: its
+    # throughput and the largest |delta log L| of the timed path against it
+    plain = None
+    accuracy = None
+    if args.plain_sample > 0 and precision == "mixed":
+        kfirst = args.warmup
+        n = min(args.plain_sample, B)
+        ids, sizes, lam = insts[kfirst]
+        pv, pres = plain_fp64_arm(wl, batches[kfirst], insts[kfirst], n, slots=min(n, 8))
+        ok = [(a, b) for a, b in zip(results[:n], pres) if a["status"] == 0 and b["status"] == 0]
+        d = [abs(a["m2logev"] - b["m2logev"]) / 2.0 for a, b in ok]
+        plain = {"value": pv, "unit": UNIT, "sample": "the first %d vectors of the first timed batch" % n,
+                 "path": "FP64 SYRK, Cholesky and solves" + ("; NFW deflection by quadrature" if has_nfw else ""),
+                 "slots": min(n, 8)}
+        accuracy = {"max_abs_dlogL": max(d) if d else None, "mean_abs_dlogL": float(np.mean(d)) if d else None,
+                    "n_draws": len(d), "vs": "plain FP64 path" + (" with NFW quadrature" if has_nfw else ""),
+                    "bound": 0.1}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        dt, _r = cpu_port_eval(wl, wl.draw(np.random.default_rng(99), 1)[0])
         from oracle import oracle as O
-        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": O.threads(), "kind": "port",
-               "sample": "1 evaluation of the same workload by the oracle port of QLens's dense inversion"}
+        times = cpu_sample(wl, np.random.default_rng(99), CPU_BUDGET_S, 5)
+        cpu = {"value": 1.0 / statistics.median(times), "unit": UNIT, "cores": O.threads(), "kind": "port",
+               "sample": "median of %d evaluations of fresh draws of the same workload by the oracle port of "
+                         "QLens's dense inversion (stopped once their time exceeded %.0f s)" % (len(times),
+                                                                                                CPU_BUDGET_S)}
 
     if rank == 0:
         line = {
@@ -408,28 +483,32 @@ def main():
             "dtype": "f32-tensor+f64" if precision == "mixed" else "f64",
             "data": "synthetic (seeded mock image; parameters drawn from the prior box)",
             "config": {**wl.describe(), "batch_per_step": B, "precision": precision,
+                       "nfw": nfw["mode"] if nfw else None,
                        "schedule": pl.schedule(),
                        "autotune": tune,
-                       "uneven": ("per vector: one of %d masks (r 1.5-3.0\"), source side 20-64, "
-                                  "log10 lambda 0-2" % len(wl.instance_masks)) if uneven else None,
+                       "uneven": wl.uneven_note if uneven else None,
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "working set (dense L' %.0f MB) exceeds the 129 MB L2" % (
-                           8e-6 * max(r["n_active_pixels"] for r in results) * max(r["n_active_src"] for r in results))},
+                       "l2": "working set (X, %.0f MB per evaluation) exceeds the 129 MB L2" % (
+                           4e-6 * max(r["n_active_pixels"] for r in results) * max(r["n_active_src"] for r in results))},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d // args.steps),
                     "d2h_bytes_per_step": int(d2h // args.steps)},
+            "vs_plain_fp64": (value / plain["value"]) if plain else None,
+            "plain_fp64": plain,
+            "accuracy": accuracy,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
+            "launches_per_eval": launches / float(B * args.steps),
             "clocks": clk,
             "stage_ms_single_eval": [float(x) for x in stage],
             # the factorisation stage of one evaluation (stage 4: Cholesky of F and of R's band, the
-            # triangular solves, the refinement): algorithmic M^3/3 multiply-adds of F's Cholesky
+            # triangular solves, the refinement): F's Cholesky is M^3/6 multiply-adds (M^3/3 FLOP),
             # over the stage's event time -- a pivot chain of M/128 steps, latency-bound for one
-            # evaluation; the batch overlaps 32 of them
+            # evaluation; the batch overlaps the slots' chains
             "cholesky_stage": {
                 "ms": float(stage[4]),
-                "algorithmic_tflop": float(np.mean([2.0 * r["n_active_src"] ** 3 / 3.0 for r in iso_res])) / 1e12,
-                "achieved_tflops": (float(np.mean([2.0 * r["n_active_src"] ** 3 / 3.0 for r in iso_res]))
+                "algorithmic_tflop": float(np.mean([r["n_active_src"] ** 3 / 3.0 for r in iso_res])) / 1e12,
+                "achieved_tflops": (float(np.mean([r["n_active_src"] ** 3 / 3.0 for r in iso_res]))
                                     / (stage[4] / 1e3) / 1e12) if stage[4] > 0 else None},
             "graphs": not args.no_graphs,
             "failed_evals": len(bad),

@@ -51,6 +51,13 @@ extern "C" {
 #define QLP_LENS_SPLE  0  /* p = b, alpha, s, q, theta_deg, xc, yc        (models.cpp SPLE_Lens) */
 #define QLP_LENS_SHEAR 1  /* p = shear, theta_deg, xc, yc                 (models.cpp Shear) */
 #define QLP_LENS_NFW   2  /* p = ks, rs, q, theta_deg, xc, yc             (models.cpp NFW) */
+/* The NFW lens in QLens's mass parameterisations ('lens nfw ... pmode=1|2',
+ * NFW::initialize_parameters, models.cpp:771-794): ks and rs follow from the
+ * mass by NFW::set_ks_rs_from_m200_c200 / set_ks_c200_from_m200_rs
+ * (models.cpp:959-976) with the lens's cosmology (qlp_lens.sigma_cr,
+ * .kpc_to_arcsec, .critical_density). */
+#define QLP_LENS_NFW_M200_C  3  /* p = m200 (M_sun), c200, q, theta_deg, xc, yc        (pmode=1) */
+#define QLP_LENS_NFW_M200_RS 4  /* p = m200 (M_sun), rs_kpc, q, theta_deg, xc, yc      (pmode=2) */
 #define QLP_MAX_LENSES 8
 #define QLP_MAX_PLANES 4
 #define QLP_MAX_PARAMS 8
@@ -68,6 +75,13 @@ typedef struct {
     int type;                    /* QLP_LENS_* */
     int plane;                   /* index into qlp_planes (0 for single-plane lensing) */
     double p[QLP_MAX_PARAMS];    /* default parameters, QLens order */
+    /* The cosmology at this lens's redshift, read only by the mass
+     * parameterisations QLP_LENS_NFW_M200_C / _RS: the lens's
+     * LensProfile::sigma_cr (M_sun/arcsec^2, for the reference source
+     * redshift) and LensProfile::kpc_to_arcsec (LensProfile::setup_cosmology,
+     * profile.cpp:83-91), and Cosmology::critical_density(zlens) (M_sun/Mpc^3,
+     * cosmo.cpp:515). */
+    double sigma_cr, kpc_to_arcsec, critical_density;
 } qlp_lens;
 
 /* Multi-plane redshift factors (QLens::deflection, lenscalc.cpp:41-80):
@@ -422,6 +436,13 @@ int qlp_nfw_surrogate_train(int device, const qlp_surrogate_opts* opts, qlp_surr
  * Applies to NFW lenses with q < 1. */
 int qlp_set_nfw_mode(qlp_ctx* ctx, int mode, double threshold_arcsec);
 
+/* QLens 'integral_tolerance' (default 1e-3, LensProfile::integral_tolerance,
+ * profile.cpp:1484): the relative tolerance at which the adaptive
+ * Gauss-Patterson quadrature of the NFW deflection stops
+ * (LensIntegral::PattersonIntegrate, profile.cpp:3830-3876).  tol <= 0
+ * restores the default. */
+int qlp_set_nfw_tolerance(qlp_ctx* ctx, double tol);
+
 /* Test hooks of the surrogate.  qlp_surrogate_grad_check: one forward and
  * backward pass of the training kernels (params [50306], x [batch][3],
  * t [batch][2], both as the network sees them) -> loss and grad [50306].
@@ -455,13 +476,65 @@ int qlp_last_transfer_bytes(const qlp_ctx* ctx, long long* h2d, long long* d2h);
  * device.  The only scratch is a static device array sized for
  * n <= 512 (about 2.1 MB per GPU, held until the process exits); larger n
  * returns QLP_ERR_ARG.  The first call on each device looks up that array's
- * address, so make it before any stream capture.  The call runs on `stream`
- * (cudaStream_t as void*, NULL = default stream) and waits for it; every
- * call shares the one array, so calls that overlap on the GPU (other host
- * threads, other streams) race -- serialise them.  Returns QLP_ERR_NOT_SPD
- * if a pivot is not positive. */
+ * address and keeps it, so the entry point is not for use after the caller
+ * resets the device (cudaDeviceReset).  The call runs on `stream`
+ * (cudaStream_t as void*, NULL = default stream) and waits for it, so no
+ * call may be made while any stream is being captured into a CUDA graph.
+ * Every call shares the one array, so calls that overlap on the GPU (other
+ * host threads, other streams) race -- serialise them.  Returns
+ * QLP_ERR_NOT_SPD, with the pivot's index in qlp_last_error, if a pivot is
+ * zero or negative (the reference's Cholesky_dcmp_packed,
+ * pixelgrid.cpp:17071-17105, flags only negative ones); s and logdet are then
+ * not meaningful. */
 int qlp_spd_solve_logdet_noalloc(const double* F, int n, int ld, const double* D, double* s, double* logdet,
                                  void* stream);
+
+/* ---- the fit drivers' likelihood (QLens::fitmodel_loglike_extended_source,
+ * lens.cpp:10657-10748) ----
+ * A fit parameter vector, as QLens's simplex, Powell, T-Walk and nested
+ * samplers move it, mapped to the lens parameters by QLens's ParamSettings
+ * (params.h): inverse transform (params.h:722-743), penalty limits (-log L =
+ * 1e30 outside them, lens.cpp:10671-10680), then the evaluation, then
+ *   -log L = m2logev / 2 + prior terms (params.h:810-840, of the fit
+ *            parameters) + Jacobian terms (params.h:884-893, of the
+ *            transformed ones).
+ * QLens's Gaussian transform is not offered (QLP_ERR_ARG). */
+#define QLP_TRANSFORM_NONE   0
+#define QLP_TRANSFORM_LOG    1   /* x = log10(value) */
+#define QLP_TRANSFORM_LINEAR 2   /* x = a value + b */
+#define QLP_TRANSFORM_RATIO  3   /* x = value / value[ratio_param] */
+#define QLP_PRIOR_UNIFORM 0
+#define QLP_PRIOR_LOG     1
+#define QLP_PRIOR_GAUSS   2
+#define QLP_FIT_REGPARAM (-1)    /* qlp_fit_param.target: the regularisation parameter lambda */
+typedef struct {
+    int target;                  /* index into the lens-parameter vector (qlp_n_params), or QLP_FIT_REGPARAM */
+    int transform;               /* QLP_TRANSFORM_* (ParamTransform::transform) */
+    double a, b;                 /* linear transform */
+    int ratio_param;             /* ratio transform: the fit parameter it divides by (not itself a ratio) */
+    int include_jacobian;        /* add the transform's Jacobian term (ParamTransform::include_jacobian) */
+    int prior;                   /* QLP_PRIOR_* (ParamPrior::prior) */
+    double prior_pos, prior_sig; /* Gaussian prior */
+    double prior_norm;           /* ParamSettings::prior_norms[i] (set_prior_norms, params.h:862-878), > 0
+                                    for non-uniform priors */
+    int use_penalty_limits;      /* ParamSettings::use_penalty_limits[i] */
+    double penalty_lo, penalty_hi;
+} qlp_fit_param;
+
+/* The fit parameters of the context (n in order); the lens parameters and
+ * lambda not named keep the lens model's defaults (qlp_lens.p) and
+ * opts->regparam. */
+int qlp_set_fit_params(qlp_ctx* ctx, const qlp_fit_param* params, int n);
+
+/* -log L of n fit vectors ([n][n_fit]) in one batch (penalised vectors are
+ * not evaluated: loglike 1e30, a zeroed result).  out may be NULL. */
+int qlp_fit_loglike_batch(qlp_ctx* ctx, const double* fit_params, int n, double* loglike, qlp_result* out);
+
+/* The host side of one fit vector, no device needed: the transformed values
+ * (transformed[n]), whether the penalty limits reject it, and the prior plus
+ * Jacobian terms that qlp_fit_loglike_batch adds to m2logev / 2. */
+int qlp_fit_terms(const qlp_fit_param* params, int n, const double* fit_params, double* transformed, int* penalised,
+                  double* terms);
 
 /* Message of the last error on this thread ("" if none). */
 const char* qlp_last_error(void);

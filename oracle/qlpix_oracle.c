@@ -28,6 +28,8 @@
 
 /* mathexpr.h:10 -- QLens's (truncated) half-pi constant */
 static const double QL_HALFPI = 1.57079632679;
+/* mathexpr.h:14 -- QLens's (truncated) 4 pi */
+static const double QL_4PI = 12.5663706144;
 /* mathexpr.h:27 */
 static double deg2rad(double t) { return 0.017453292519943295 * t; }
 
@@ -84,8 +86,27 @@ static int setup_lens(olens* L, const qlp_lens* d, const double* p)
         L->shear1 = shear * cos(2 * theta_eff);
         L->shear2 = shear * sin(2 * theta_eff);
         L->xc = p[2]; L->yc = p[3];
-    } else if (d->type == QLP_LENS_NFW) {
-        L->ks = p[0]; L->rs = p[1]; L->q = p[2];
+    } else if (d->type == QLP_LENS_NFW || d->type == QLP_LENS_NFW_M200_C || d->type == QLP_LENS_NFW_M200_RS) {
+        L->type = QLP_LENS_NFW;
+        if (d->type == QLP_LENS_NFW) {
+            L->ks = p[0]; L->rs = p[1];
+        } else {
+            /* NFW::update_meta_parameters (models.cpp:891-898) -> set_ks_rs_from_m200_c200 (pmode 1,
+               models.cpp:968-976) or set_ks_c200_from_m200_rs (pmode 2, models.cpp:959-966) */
+            double m200 = p[0], c200, rs_kpc;
+            double rvir_kpc = pow(m200 / (200.0 * QL_4PI / 3.0 * 1e-9 * d->critical_density), 0.333333333333);
+            if (d->type == QLP_LENS_NFW_M200_C) {
+                c200 = p[1];
+                rs_kpc = rvir_kpc / c200;
+                L->rs = rs_kpc * d->kpc_to_arcsec;
+            } else {
+                rs_kpc = p[1];
+                L->rs = rs_kpc * d->kpc_to_arcsec;
+                c200 = rvir_kpc / rs_kpc;
+            }
+            L->ks = m200 / (QL_4PI * L->rs * L->rs * d->sigma_cr * (log(1 + c200) - c200 / (1 + c200)));
+        }
+        L->q = p[2];
         set_angle(L, p[3]);
         L->xc = p[4]; L->yc = p[5];
         L->f_major_axis = 1.0 / sqrt(L->q);
@@ -102,7 +123,9 @@ static int n_params_of(int type)
     switch (type) {
         case QLP_LENS_SPLE: return 7;
         case QLP_LENS_SHEAR: return 4;
-        case QLP_LENS_NFW: return 6;
+        case QLP_LENS_NFW:
+        case QLP_LENS_NFW_M200_C:
+        case QLP_LENS_NFW_M200_RS: return 6;
     }
     return 0;
 }

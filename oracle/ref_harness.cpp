@@ -169,6 +169,26 @@ int main(int argc, char** argv)
 		std::vector<int> lp(lens.nlens);
 		for (int k = 0; k < lens.nlens; k++) lp[k] = lens.lens_redshift_idx[k];
 		dumpi("lens_plane", lp);
+		// per lens: the cosmology its meta-parameters were computed with
+		// (LensProfile::setup_cosmology, profile.cpp:83-91; Cosmology::critical_density,
+		// cosmo.cpp:515) and, for NFW lenses, the ks and rs the mass
+		// parameterisations derived (models.cpp:959-976); 0 elsewhere
+		std::vector<double> lc;
+		for (int k = 0; k < lens.nlens; k++) {
+			LensProfile* lp_k = lens.lens_list[k];
+			lc.push_back(lp_k->sigma_cr);
+			lc.push_back(lp_k->kpc_to_arcsec);
+			lc.push_back(lens.cosmo.critical_density(lp_k->zlens));
+			if (lp_k->lenstype == nfw) {
+				NFW* n = (NFW*) lp_k;
+				lc.push_back(n->ks);
+				lc.push_back(n->rs);
+			} else {
+				lc.push_back(0.0);
+				lc.push_back(0.0);
+			}
+		}
+		dumpd("lens_cosmo", lc);
 	}
 	bool** in_mask = g->*grab(G_in_mask());
 	int** nsplits = g->*grab(G_nsplits());

@@ -16,6 +16,8 @@ QLP_ERR_NO_DEVICE = 9
 QLP_LENS_SPLE = 0
 QLP_LENS_SHEAR = 1
 QLP_LENS_NFW = 2
+QLP_LENS_NFW_M200_C = 3
+QLP_LENS_NFW_M200_RS = 4
 QLP_MAX_LENSES = 8
 QLP_MAX_PLANES = 4
 QLP_MAX_PARAMS = 8
@@ -26,8 +28,10 @@ QLP_MIXED = 1
 QLP_NFW_QUADRATURE = 0
 QLP_NFW_SURROGATE = 1
 
-LENS_TYPES = {"sple": QLP_LENS_SPLE, "shear": QLP_LENS_SHEAR, "nfw": QLP_LENS_NFW}
-N_PARAMS = {QLP_LENS_SPLE: 7, QLP_LENS_SHEAR: 4, QLP_LENS_NFW: 6}
+LENS_TYPES = {"sple": QLP_LENS_SPLE, "shear": QLP_LENS_SHEAR, "nfw": QLP_LENS_NFW,
+              "nfw_m200_c": QLP_LENS_NFW_M200_C, "nfw_m200_rs": QLP_LENS_NFW_M200_RS}
+N_PARAMS = {QLP_LENS_SPLE: 7, QLP_LENS_SHEAR: 4, QLP_LENS_NFW: 6, QLP_LENS_NFW_M200_C: 6, QLP_LENS_NFW_M200_RS: 6}
+NFW_TYPES = ("nfw", "nfw_m200_c", "nfw_m200_rs")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -35,7 +39,8 @@ _up = C.POINTER(C.c_ubyte)
 
 
 class qlp_lens(C.Structure):
-    _fields_ = [("type", C.c_int), ("plane", C.c_int), ("p", C.c_double * QLP_MAX_PARAMS)]
+    _fields_ = [("type", C.c_int), ("plane", C.c_int), ("p", C.c_double * QLP_MAX_PARAMS),
+                ("sigma_cr", C.c_double), ("kpc_to_arcsec", C.c_double), ("critical_density", C.c_double)]
 
 
 class qlp_planes(C.Structure):
@@ -117,6 +122,34 @@ class qlp_surrogate_report(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+QLP_TRANSFORM_NONE = 0
+QLP_TRANSFORM_LOG = 1
+QLP_TRANSFORM_LINEAR = 2
+QLP_TRANSFORM_RATIO = 3
+QLP_PRIOR_UNIFORM = 0
+QLP_PRIOR_LOG = 1
+QLP_PRIOR_GAUSS = 2
+QLP_FIT_REGPARAM = -1
+
+
+class qlp_fit_param(C.Structure):
+    _fields_ = [("target", C.c_int), ("transform", C.c_int), ("a", C.c_double), ("b", C.c_double),
+                ("ratio_param", C.c_int), ("include_jacobian", C.c_int), ("prior", C.c_int),
+                ("prior_pos", C.c_double), ("prior_sig", C.c_double), ("prior_norm", C.c_double),
+                ("use_penalty_limits", C.c_int), ("penalty_lo", C.c_double), ("penalty_hi", C.c_double)]
+
+
+def make_fit_params(spec):
+    """spec: list of dicts with the qlp_fit_param fields (missing fields: 0,
+    prior_norm 1)."""
+    arr = (qlp_fit_param * len(spec))()
+    for k, d in enumerate(spec):
+        arr[k].prior_norm = 1.0
+        for key, v in d.items():
+            setattr(arr[k], key, v)
+    return arr
+
+
 class qlp_instance(C.Structure):
     _fields_ = [("mask_id", C.c_int), ("src_npixels_x", C.c_int), ("src_npixels_y", C.c_int)]
 
@@ -137,7 +170,8 @@ def srcgrid_defaults():
 
 
 def make_lenses(spec):
-    """spec: list of dict(type='sple'|'shear'|'nfw', params=[...], plane=0)."""
+    """spec: list of dict(type='sple'|'shear'|'nfw'|'nfw_m200_c'|'nfw_m200_rs', params=[...],
+    plane=0, cosmo=(sigma_cr, kpc_to_arcsec, critical_density) for the mass parameterisations)."""
     arr = (qlp_lens * len(spec))()
     for k, l in enumerate(spec):
         t = LENS_TYPES[l["type"]] if isinstance(l["type"], str) else int(l["type"])
@@ -145,6 +179,9 @@ def make_lenses(spec):
         arr[k].plane = int(l.get("plane", 0))
         for i, v in enumerate(l["params"]):
             arr[k].p[i] = float(v)
+        cosmo = l.get("cosmo")
+        if cosmo is not None:
+            arr[k].sigma_cr, arr[k].kpc_to_arcsec, arr[k].critical_density = (float(v) for v in cosmo)
     return arr
 
 

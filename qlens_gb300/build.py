@@ -36,6 +36,7 @@ UNITS = [
     ("autotune.cpp", []),
     ("fits.cpp", []),
     ("sampler.cpp", []),
+    ("fitparam.cpp", []),
     ("qlpix_api.cpp", []),
 ]
 HEADERS = ["qlpix_internal.h", "qlpix_ctx.h", "lens_device.cuh", "nfw_device.cuh", "patterson_rule.h", "chol.cuh", "chol128.cuh", "tc_common.cuh", "tc_syrk.cuh", "brent.h"]

@@ -9,10 +9,19 @@
 //                    inverses by forward substitution, off-diagonal blocks by
 //                    V_ij = -V_ii sum_k L_ik V_kj);
 //   k_chol_tile128   mode 1 (panel solve): P_I <- P_I L_kk^-T for the 128-row
-//                    blocks below, mode 0 (trailing update): A_IJ -= P_I P_J^T
-//                    for the lower-triangle tiles -- both as 128x128x128
-//                    products on the tensor cores (tcgen05 kind::tf32, 3xTF32
-//                    split, accumulator in TMEM), K in four quarters of 32.
+//                    blocks below, as 128x128x128 products on the tensor cores
+//                    (tcgen05 kind::tf32, 3xTF32 split, accumulator in TMEM),
+//                    K in four quarters of 32; its epilogue also writes each
+//                    solved block once as F16 hi + lo, each row scaled by a
+//                    power of two (its largest entry near 2^14), into the
+//                    panel buffer;
+//   k_chol_upd16     the trailing update A_IJ -= P_I P_J^T for the
+//                    lower-triangle tiles: TMA loads of the split panel
+//                    blocks (128-byte swizzle), tcgen05 kind::f16 at twice
+//                    the TF32 rate, three products (hi*hi + hi*lo + lo*hi,
+//                    ~22 significant bits), the scales undone in the
+//                    epilogue.  (mode 0 of k_chol_tile128 computes the same
+//                    update from the FP32 panel, re-split per tile.)
 // `band` limits both to the tiles within that many 128-blocks of the
 // diagonal: the curvature matrix R couples a cell only to cells at most two
 // grid rows away, so its factor stays inside that band (dense F passes a
@@ -21,6 +30,7 @@
 // negative pivot is recorded and sqrt(|d|) used; the first such pivot is
 // reported through GridState::not_spd_F / not_spd_R.
 #pragma once
+#include <cuda_fp16.h>
 #include "tc_common.cuh"
 
 namespace qlpix {
@@ -28,6 +38,7 @@ namespace qlpix {
 #define C2 128
 #define P128_SMEM (2 * C2 * (C2 + 1) * 4 + 32 * 33 * 4 + C2 * 4)         // S, V, T, 1/diag
 #define T128_SMEM (4 * TC_TILE_BYTES + 1024)                             // [A/B][hi/lo], one K quarter
+#define U16_SMEM (4 * TC_TILE_BYTES + 1024)                              // [A/B][hi/lo], one K half (64 F16)
 
 __device__ __forceinline__ int cpad128(int M) { return (M + C2 - 1) / C2 * C2; }
 
@@ -253,7 +264,9 @@ __device__ __forceinline__ void store_split_quarter(const float4 (&vv)[8], unsig
 // an SM: while one waits on its loads, the others' MMAs run.  Each quarter's
 // global loads are issued while the previous quarter's MMAs run.
 __global__ void __launch_bounds__(128, 3) k_chol_tile128(float* __restrict__ A, int ld, int k, GridState* gs, int mode,
-                                                         const float* __restrict__ Linv, int band)
+                                                         const float* __restrict__ Linv, int band,
+                                                         __half* __restrict__ P_hi, __half* __restrict__ P_lo,
+                                                         int* __restrict__ pexp)
 {
     extern __shared__ unsigned char smem_raw[];
     __shared__ uint64_t done_bar;
@@ -327,30 +340,181 @@ __global__ void __launch_bounds__(128, 3) k_chol_tile128(float* __restrict__ A, 
     }
     const uint32_t tmem = tmem_slot;
     const int row = r0 + warp * 32 + lane;
-    if (ok && !abort_flag) {
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    const bool good = __syncthreads_and(ok && !abort_flag) != 0;
+    if (good && mode == 0) {
         #pragma unroll 1
         for (int c = 0; c < TC_TILE; c += 32) {
             float v[32];
-            tmem_ld_32cols(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-            if (mode == 0) {
-                float* dst = A + (size_t)row * ld + c0 + c;
-                #pragma unroll
-                for (int i = 0; i < 32; i += 4) {
-                    float4 a = *reinterpret_cast<float4*>(dst + i);
-                    a.x -= v[i]; a.y -= v[i + 1]; a.z -= v[i + 2]; a.w -= v[i + 3];
-                    *reinterpret_cast<float4*>(dst + i) = a;
-                }
-            } else {
-                float* dst = A + (size_t)row * ld + o + c;
-                #pragma unroll
-                for (int i = 0; i < 32; i += 4)
-                    *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            tmem_ld_32cols(trow + (uint32_t)c, v);
+            float* dst = A + (size_t)row * ld + c0 + c;
+            #pragma unroll
+            for (int i = 0; i < 32; i += 4) {
+                float4 a = *reinterpret_cast<float4*>(dst + i);
+                a.x -= v[i]; a.y -= v[i + 1]; a.z -= v[i + 2]; a.w -= v[i + 3];
+                *reinterpret_cast<float4*>(dst + i) = a;
+            }
+        }
+    } else if (good) {
+        // the solved block: FP32 into A, and F16 hi + lo of 2^s x each row (s
+        // puts the row's largest entry just below 2^14) into rows 128 I.. of
+        // the panel buffer, with s in pexp, for k_chol_upd16
+        float mx = 0.f;
+        #pragma unroll 1
+        for (int c = 0; c < TC_TILE; c += 32) {
+            float v[32];
+            tmem_ld_32cols(trow + (uint32_t)c, v);
+            #pragma unroll
+            for (int i = 0; i < 32; i++) mx = fmaxf(mx, fabsf(v[i]));
+        }
+        int e = 0;
+        frexpf(mx, &e);                      // mx < 2^e
+        // kept within [-60, 60] so that 2^-(s_i + s_j) is a normal float
+        const int sc = (mx > 0.f) ? max(-60, min(60, 14 - e)) : 0;
+        pexp[I * C2 + warp * 32 + lane] = sc;
+        const float scf = __int_as_float((127 + sc) << 23);
+        const size_t prow = (size_t)(I * C2 + warp * 32 + lane) * C2;
+        #pragma unroll 1
+        for (int c = 0; c < TC_TILE; c += 32) {
+            float v[32];
+            tmem_ld_32cols(trow + (uint32_t)c, v);
+            float* dst = A + (size_t)row * ld + o + c;
+            #pragma unroll
+            for (int i = 0; i < 32; i += 4)
+                *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            uint32_t hw[16], lw[16];
+            #pragma unroll
+            for (int i = 0; i < 16; i++) {
+                const float a = v[2 * i] * scf, b = v[2 * i + 1] * scf;
+                const __half ah = __float2half_rn(a), bh = __float2half_rn(b);
+                const __half al = __float2half_rn(a - __half2float(ah)), bl = __float2half_rn(b - __half2float(bh));
+                hw[i] = (uint32_t)__half_as_ushort(ah) | ((uint32_t)__half_as_ushort(bh) << 16);
+                lw[i] = (uint32_t)__half_as_ushort(al) | ((uint32_t)__half_as_ushort(bl) << 16);
+            }
+            uint4* ph = reinterpret_cast<uint4*>(P_hi + prow + c);
+            uint4* pl = reinterpret_cast<uint4*>(P_lo + prow + c);
+            #pragma unroll
+            for (int q = 0; q < 4; q++) {
+                ph[q] = make_uint4(hw[4 * q], hw[4 * q + 1], hw[4 * q + 2], hw[4 * q + 3]);
+                pl[q] = make_uint4(lw[4 * q], lw[4 * q + 1], lw[4 * q + 2], lw[4 * q + 3]);
             }
         }
     }
     tc_fence_before();
     __syncthreads();
-    if ((!ok || abort_flag) && threadIdx.x == 0) atomicExch(&gs->status, QLP_ERR_TIMEOUT);
+    if (!good && threadIdx.x == 0) atomicExch(&gs->status, QLP_ERR_TIMEOUT);
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");
+    }
+}
+
+// The trailing update of step k, A_IJ -= P_I P_J^T over the lower-triangle
+// tiles of the first `band` block rows below the step, from the split panel
+// that k_chol_tile128 (mode 1) wrote: map_hi / map_lo address its F16 parts
+// ([M_cap rows][128], 64 x 128 boxes, 128-byte swizzle), pexp[row] the
+// power-of-two scale of each of its rows.
+// K = 128 runs in two halves of 64 (12 MMAs each) through one 64 KB buffer,
+// so three CTAs share an SM and overlap each other's loads, MMAs and
+// epilogues.
+__global__ void __launch_bounds__(128, 3) k_chol_upd16(const __grid_constant__ CUtensorMap map_hi,
+                                                       const __grid_constant__ CUtensorMap map_lo,
+                                                       float* __restrict__ A, int ld, int k, GridState* gs,
+                                                       const int* __restrict__ pexp, int band)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint64_t full_bar, done_bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    const int Mp = cpad128(gs->M);
+    const int base = (k + 1) * C2;
+    if (base >= Mp) return;
+    const int nt = (Mp - base) / C2;
+    int I, J;
+    tri_ij(blockIdx.x, I, J);
+    if (I >= nt || I >= band) return;
+    const int r0 = base + I * C2, c0 = base + J * C2;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    auto tile = [&](int op, int part) { return smem + (op * 2 + part) * TC_TILE_BYTES; };
+    if (threadIdx.x == 0) {
+        mbar_init(&full_bar, 1);
+        mbar_init(&done_bar, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(128)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    bool ok = true;
+    int issued = 0, landed = 0;      // K halves whose loads were issued / seen complete (thread 0)
+    for (int h = 0; h < 2; h++) {
+        if (threadIdx.x == 0 && !abort_flag) {
+            mbar_expect_tx(&full_bar, 4 * TC_TILE_BYTES);
+            tma_load_2d(&map_hi, &full_bar, tile(0, 0), h * 64, I * C2);
+            tma_load_2d(&map_lo, &full_bar, tile(0, 1), h * 64, I * C2);
+            tma_load_2d(&map_hi, &full_bar, tile(1, 0), h * 64, J * C2);
+            tma_load_2d(&map_lo, &full_bar, tile(1, 1), h * 64, J * C2);
+            issued++;
+            if (mbar_wait_bounded(&full_bar, (uint32_t)(h & 1), &abort_flag, false)) {
+                landed++;
+                tc_fence_after();
+                const uint32_t idesc = idesc_f16_128x128();
+                const uint64_t a_hi = sdesc_sw128(smem_u32(tile(0, 0)));
+                const uint64_t a_lo = sdesc_sw128(smem_u32(tile(0, 1)));
+                const uint64_t b_hi = sdesc_sw128(smem_u32(tile(1, 0)));
+                const uint64_t b_lo = sdesc_sw128(smem_u32(tile(1, 1)));
+                #pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t off = (uint64_t)((kk * 32) >> 4);     // 16 F16 = 32 bytes along K
+                    mma_f16(tmem, a_hi + off, b_hi + off, idesc, (h > 0 || kk > 0) ? 1u : 0u);
+                    mma_f16(tmem, a_hi + off, b_lo + off, idesc, 1u);
+                    mma_f16(tmem, a_lo + off, b_hi + off, idesc, 1u);
+                }
+            }
+            mma_commit(&done_bar);
+        }
+        __syncthreads();
+        // the MMAs read shared memory asynchronously: wait before the next half's loads reuse it
+        if (!mbar_wait_bounded(&done_bar, (uint32_t)(h & 1), &abort_flag, false)) ok = false;
+        tc_fence_after();
+        __syncthreads();
+    }
+    const bool good = __syncthreads_and(ok && !abort_flag) != 0;
+    if (good) {
+        const int row = r0 + warp * 32 + lane;
+        const int si = pexp[I * C2 + warp * 32 + lane];
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        #pragma unroll 1
+        for (int c = 0; c < TC_TILE; c += 32) {
+            float v[32];
+            tmem_ld_32cols(trow + (uint32_t)c, v);
+            const int sj = pexp[J * C2 + c + lane];      // column c + lane's row scale, shared through the warp
+            float* dst = A + (size_t)row * ld + c0 + c;
+            #pragma unroll
+            for (int i = 0; i < 32; i += 4) {
+                float4 a = *reinterpret_cast<float4*>(dst + i);
+                // 2^-(s_i + s_j), exact (|s_i + s_j| <= 120)
+                a.x -= v[i] * __int_as_float((127 - si - __shfl_sync(0xffffffffu, sj, i)) << 23);
+                a.y -= v[i + 1] * __int_as_float((127 - si - __shfl_sync(0xffffffffu, sj, i + 1)) << 23);
+                a.z -= v[i + 2] * __int_as_float((127 - si - __shfl_sync(0xffffffffu, sj, i + 2)) << 23);
+                a.w -= v[i + 3] * __int_as_float((127 - si - __shfl_sync(0xffffffffu, sj, i + 3)) << 23);
+                *reinterpret_cast<float4*>(dst + i) = a;
+            }
+        }
+    }
+    if (threadIdx.x == 0 && issued > landed)       // copies issued but never seen complete: let them land
+        mbar_wait_bounded(&full_bar, (uint32_t)(landed & 1), &abort_flag, false);
+    tc_fence_before();
+    __syncthreads();
+    if (!good && threadIdx.x == 0) atomicExch(&gs->status, QLP_ERR_TIMEOUT);
     if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");

@@ -47,7 +47,7 @@ static void free_work(Work& w)
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
                     w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep,
-                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart};
+                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart, w.lnz};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
@@ -124,6 +124,8 @@ static int ensure_fp64_mats(Slot& s)
     if (s.fp64_mats) return QLP_OK;
     CK(dalloc(&s.w.Lpsf, (size_t)s.N_cap * s.M_cap), "alloc L'");
     CK(cudaMemset(s.w.Lpsf, 0, sizeof(double) * (size_t)s.N_cap * s.M_cap), "memset");
+    s.w.lnz_chunks = (s.N_cap + 15) / 16;
+    CK(dalloc(&s.w.lnz, (size_t)s.w.lnz_chunks * (s.M_cap / 64)), "alloc L' flags");
     CK(dalloc(&s.w.F, (size_t)s.M_cap * s.M_cap), "alloc F");
     CK(dalloc(&s.w.R, (size_t)s.M_cap * s.M_cap), "alloc R");
     s.fp64_mats = true;
@@ -258,7 +260,8 @@ static int build_lens_model(qlp_ctx* c, const double* lens_params, LensModel& lm
     for (int k = 0; k < lm.nlens; k++) {
         const qlp_lens& d = c->lenses[k];
         const double* p = lens_params ? lens_params + off : d.p;
-        int r = make_lens_rec(lm.lens[k], d.type, d.plane, p);
+        int r = make_lens_rec(lm.lens[k], d, p);
+        lm.lens[k].tol = c->nfw_tol;
         if (r != QLP_OK) { set_error("%s (lens %d)", "unsupported lens parameters", k); return r; }
         off += n_params_of(d.type);
     }
@@ -268,7 +271,7 @@ static int build_lens_model(qlp_ctx* c, const double* lens_params, LensModel& lm
 static bool model_has_nfw(const qlp_ctx* c)
 {
     for (const qlp_lens& l : c->lenses)
-        if (l.type == QLP_LENS_NFW) return true;
+        if (is_nfw_type(l.type)) return true;
     return false;
 }
 
@@ -316,7 +319,7 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
         // afterwards in their own kernel (nothing downstream needs them)
         int defer = -1, n_nfw = 0;
         for (int k = 0; k < (int)c->lenses.size(); k++)
-            if (c->lenses[k].type == QLP_LENS_NFW) { n_nfw++; defer = k; }
+            if (is_nfw_type(c->lenses[k].type)) { n_nfw++; defer = k; }
         if (n_nfw != 1 || c->lenses[defer].plane != c->planes.n_planes - 1) defer = -1;
         int r = launch_raytrace_sur(sd, w, c->nfw_threshold, defer, st);
         if (r != QLP_OK) return r;

@@ -83,9 +83,34 @@ void launch_D(Work& w, int N_max, int M_max, cudaStream_t st)
 }
 
 // ---- F = L'^T C^-1 L', lower 64x64 tiles, FP64 ----
+// nz[cb * nchunks + c] != 0 when rows [16 c, 16 c + 16) of L' have a nonzero in
+// columns [64 cb, 64 cb + 64); one warp per (chunk, column block).
+__global__ void __launch_bounds__(256) k_lpsf_nzflags(const GridState* __restrict__ gs,
+                                                      const double* __restrict__ L, int ldL,
+                                                      unsigned char* __restrict__ nz, int nchunks)
+{
+    const int N = gs->N, ncb = mpad64(gs->M) / NB;
+    const int nch = (N + 15) / 16;
+    const int lane = threadIdx.x & 31;
+    const long task = (long)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (task >= (long)nch * ncb) return;
+    const int c = (int)(task % nch), cb = (int)(task / nch);
+    bool any = false;
+    for (int r = 16 * c; r < min(16 * c + 16, N); r++) {
+        const double* row = L + (size_t)r * ldL + cb * NB;
+        any |= (row[lane] != 0.0) | (row[lane + 32] != 0.0);
+    }
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0) nz[(size_t)cb * nchunks + c] = any ? 1 : 0;
+}
+
+// A 16-pixel step whose rows of L' are zero in either tile's 64 columns adds
+// only zero products, so it is skipped; the sums of the other steps run in
+// the same order, so F is bit-for-bit the dense contraction's.
 __global__ void __launch_bounds__(256) k_syrk64(const GridState* __restrict__ gs, const double* __restrict__ L,
                                                 int ldL, const double* __restrict__ cvec, int use_noise_map,
-                                                double cov_inverse, double* __restrict__ F, int ldF)
+                                                double cov_inverse, const unsigned char* __restrict__ nz, int nchunks,
+                                                double* __restrict__ F, int ldF)
 {
     __shared__ double As[16][NB + 1];
     __shared__ double Bs[16][NB + 1];
@@ -94,6 +119,8 @@ __global__ void __launch_bounds__(256) k_syrk64(const GridState* __restrict__ gs
     const int N = gs->N, Mp = mpad64(gs->M);
     if (bi * NB >= Mp) return;
     const int a0 = bi * NB, b0 = bj * NB;
+    const unsigned char* nza = nz + (size_t)bi * nchunks;
+    const unsigned char* nzb = nz + (size_t)bj * nchunks;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     double acc[4][4];
     #pragma unroll
@@ -101,6 +128,7 @@ __global__ void __launch_bounds__(256) k_syrk64(const GridState* __restrict__ gs
         #pragma unroll
         for (int v = 0; v < 4; v++) acc[u][v] = 0;
     for (int p0 = 0; p0 < N; p0 += 16) {
+        if (!(nza[p0 >> 4] && nzb[p0 >> 4])) continue;       // uniform over the block
         #pragma unroll
         for (int e = 0; e < 4; e++) {
             int idx = threadIdx.x + e * 256;   // 0..1023 over 16 x 64
@@ -139,11 +167,13 @@ __global__ void __launch_bounds__(256) k_syrk64(const GridState* __restrict__ gs
 
 void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st)
 {
-    (void)N_max;
     int nb = (M_max + NB - 1) / NB;
     int tiles = nb * (nb + 1) / 2;
-    k_syrk64<<<tiles, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.cvec, sd.use_noise_map, sd.cov_inverse, w.F, w.ldF);
-    count_launches(1);
+    const long tasks = (long)((N_max + 15) / 16) * nb;
+    k_lpsf_nzflags<<<(unsigned)((tasks + 7) / 8), 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.lnz, w.lnz_chunks);
+    k_syrk64<<<tiles, 256, 0, st>>>(w.gs, w.Lpsf, w.ldL, w.cvec, sd.use_noise_map, sd.cov_inverse, w.lnz,
+                                    w.lnz_chunks, w.F, w.ldF);
+    count_launches(2);
 }
 
 // ---- curvature R (dense lower) and F += lambda R ----

@@ -63,6 +63,12 @@ struct MixedWork {
     int* flags = nullptr;    // 2 x nb: per-block "published" flags of the two sweeps
     int nb = 0;              // 128-blocks of M_cap
     CUtensorMap map_hi, map_lo;
+    // the Cholesky's current panel, split for its trailing update (k_chol_upd16):
+    // F16 hi + lo [M_cap][128] and the scale exponent of each row;
+    // one set for F, one for R (factored concurrently on the side stream)
+    __half* Pf_hi = nullptr; __half* Pf_lo = nullptr; int* Pf_exp = nullptr;
+    __half* Pr_hi = nullptr; __half* Pr_lo = nullptr; int* Pr_exp = nullptr;
+    CUtensorMap map_pf_hi, map_pf_lo, map_pr_hi, map_pr_lo;
     bool ready = false;
 };
 
@@ -581,7 +587,8 @@ void mixed_free(Slot& c)
     if (!m) return;
     void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->img,
                     m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
-                    m->sqc, m->col_u, m->src_u, m->colval64, m->pixT, m->F0};
+                    m->sqc, m->col_u, m->src_u, m->colval64, m->pixT, m->F0, m->Pf_hi, m->Pf_lo, m->Pf_exp,
+                    m->Pr_hi, m->Pr_lo, m->Pr_exp};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
     c.mixed = nullptr;
@@ -631,6 +638,12 @@ int mixed_init(Slot& c)
     A((void**)&m->yf, sizeof(float) * (size_t)M_cap);
     A((void**)&m->zf, sizeof(float) * (size_t)M_cap);
     A((void**)&m->flags, sizeof(int) * (size_t)2 * m->nb);
+    A((void**)&m->Pf_hi, sizeof(__half) * (size_t)M_cap * C2);
+    A((void**)&m->Pf_lo, sizeof(__half) * (size_t)M_cap * C2);
+    A((void**)&m->Pr_hi, sizeof(__half) * (size_t)M_cap * C2);
+    A((void**)&m->Pr_lo, sizeof(__half) * (size_t)M_cap * C2);
+    A((void**)&m->Pf_exp, sizeof(int) * (size_t)M_cap);
+    A((void**)&m->Pr_exp, sizeof(int) * (size_t)M_cap);
     if (e != cudaSuccess) {
         set_error("%s (%d)", "mixed-precision workspace allocation failed", (int)e);
         return QLP_ERR_NOMEM;
@@ -638,7 +651,11 @@ int mixed_init(Slot& c)
     cudaMemset(m->X_hi, 0, xbytes);
     cudaMemset(m->X_lo, 0, xbytes);
     if (make_map(&m->map_hi, m->X_hi, M_cap, K_cap, m->half) != QLP_OK ||
-        make_map(&m->map_lo, m->X_lo, M_cap, K_cap, m->half) != QLP_OK) {
+        make_map(&m->map_lo, m->X_lo, M_cap, K_cap, m->half) != QLP_OK ||
+        make_map(&m->map_pf_hi, m->Pf_hi, M_cap, C2, true) != QLP_OK ||
+        make_map(&m->map_pf_lo, m->Pf_lo, M_cap, C2, true) != QLP_OK ||
+        make_map(&m->map_pr_hi, m->Pr_hi, M_cap, C2, true) != QLP_OK ||
+        make_map(&m->map_pr_lo, m->Pr_lo, M_cap, C2, true) != QLP_OK) {
         set_error("%s (%d)", "cuTensorMapEncodeTiled unavailable or failed", 0);
         return QLP_ERR_CUDA;
     }
@@ -646,6 +663,7 @@ int mixed_init(Slot& c)
     cudaFuncSetAttribute(k_psf_x_band, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
     cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
+    cudaFuncSetAttribute(k_chol_upd16, cudaFuncAttributeMaxDynamicSharedMemorySize, U16_SMEM);
     cudaFuncSetAttribute(k_syrk_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     cudaFuncSetAttribute(k_syrk_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     m->ready = true;
@@ -653,12 +671,15 @@ int mixed_init(Slot& c)
 }
 
 // FP32 blocked Cholesky for the mixed path (chol128.cuh): per 128-column step
-// the diagonal factor and its inverse in one CTA, the panel solve and the
-// trailing update on the tensor cores.  band: 128-blocks below the diagonal
+// the diagonal factor and its inverse in one CTA, the panel solve on the
+// tensor cores (which also leaves the panel split into F16 hi + lo in
+// P_hi / P_lo, addressed by map_hi / map_lo), and the trailing update from
+// that split panel on the tensor cores.  band: 128-blocks below the diagonal
 // that can be nonzero (the whole matrix for F).  The inverse of diagonal
 // block k goes to linv + k * linv_stride (stride 0: one scratch block).
 static int cholesky_mixed(float* A, int ld, int M_cap128, GridState* gs, int which, int band, float* linv,
-                          size_t linv_stride, cudaStream_t st)
+                          size_t linv_stride, __half* P_hi, __half* P_lo, int* pexp, const CUtensorMap& map_hi,
+                          const CUtensorMap& map_lo, cudaStream_t st)
 {
     const int nb = M_cap128 / C2;
     int n = 0;
@@ -669,8 +690,8 @@ static int cholesky_mixed(float* A, int ld, int M_cap128, GridState* gs, int whi
         const int rem = nb - k - 1;
         if (rem == 0) break;
         const int bt = std::min(rem, band);
-        k_chol_tile128<<<bt, 128, T128_SMEM, st>>>(A, ld, k, gs, 1, lk, band);
-        k_chol_tile128<<<bt * (bt + 1) / 2, 128, T128_SMEM, st>>>(A, ld, k, gs, 0, lk, band);
+        k_chol_tile128<<<bt, 128, T128_SMEM, st>>>(A, ld, k, gs, 1, lk, band, P_hi, P_lo, pexp);
+        k_chol_upd16<<<bt * (bt + 1) / 2, 128, U16_SMEM, st>>>(map_hi, map_lo, A, ld, k, gs, pexp, band);
         n += 2;
     }
     count_launches(n);
@@ -800,7 +821,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         cudaEventRecord(slot.side_fork, st);
         cudaStreamWaitEvent(slot.side, slot.side_fork, 0);
         const int band_R = (2 * so.snx - 1) / C2 + 1;
-        n += cholesky_mixed(m->R32, m->ld32, m->M_cap, w.gs, 1, band_R, m->linv128, 0, slot.side);
+        n += cholesky_mixed(m->R32, m->ld32, m->M_cap, w.gs, 1, band_R, m->linv128, 0, m->Pr_hi, m->Pr_lo,
+                            m->Pr_exp, m->map_pr_hi, m->map_pr_lo, slot.side);
         k_logdet_t<float><<<1, 1024, 0, slot.side>>>(m->R32, m->ld32, w.gs, w.out, 1);
         n++;
         cudaEventRecord(slot.side_join, slot.side);
@@ -811,7 +833,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         return QLP_OK;
     }
     }   // part != PIPE_TRIAL
-    n += cholesky_mixed(m->F32, m->ld32, m->M_cap, w.gs, 0, 1 << 20, m->linvF, (size_t)2 * C2 * C2, st);
+    n += cholesky_mixed(m->F32, m->ld32, m->M_cap, w.gs, 0, 1 << 20, m->linvF, (size_t)2 * C2 * C2, m->Pf_hi,
+                        m->Pf_lo, m->Pf_exp, m->map_pf_hi, m->map_pf_lo, st);
     k_logdet_t<float><<<1, 1024, 0, st>>>(m->F32, m->ld32, w.gs, w.out, 0);
     n++;
     if (so.regularization && part == PIPE_ALL) cudaStreamWaitEvent(st, slot.side_join, 0);

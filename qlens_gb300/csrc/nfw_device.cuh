@@ -31,7 +31,7 @@ namespace qlpix {
 static __constant__ double c_pat_points[QLP_PAT_N] = QLP_PAT_POINTS_INIT;
 static __constant__ double c_pat_weights[QLP_PAT_NW] = QLP_PAT_WEIGHTS_INIT;
 
-#define NFW_PAT_TOL 1e-3
+#define NFW_PAT_TOL 1e-3                 // QLens's default integral_tolerance (LensRec::tol)
 #define NFW_KEEP_LEVELS 6            // levels 0..5 keep their node values
 #define NFW_KEEP ((2 << (NFW_KEEP_LEVELS - 1)) - 1)   // 63
 
@@ -128,7 +128,7 @@ static __device__ void nfw_deflection(const LensRec& L, double x, double y, doub
         return;
     }
     double I0, I1;
-    nfw_integrals(L, x * x, y * y, NFW_PAT_TOL, I0, I1);
+    nfw_integrals(L, x * x, y * y, L.tol, I0, I1);
     const double sqe = sqrt(1 - L.epsilon);
     dx = x * (sqe * I0);
     dy = y * (sqe * I1);

@@ -42,9 +42,42 @@ int n_params_of(int type)
     switch (type) {
         case QLP_LENS_SPLE: return 7;
         case QLP_LENS_SHEAR: return 4;
-        case QLP_LENS_NFW: return 6;
+        case QLP_LENS_NFW:
+        case QLP_LENS_NFW_M200_C:
+        case QLP_LENS_NFW_M200_RS: return 6;
     }
     return 0;
+}
+
+bool is_nfw_type(int type)
+{
+    return type == QLP_LENS_NFW || type == QLP_LENS_NFW_M200_C || type == QLP_LENS_NFW_M200_RS;
+}
+
+static const double QL_4PI = 12.5663706144;                    // mathexpr.h:14
+
+// ks and rs of an NFW lens given by its mass: NFW::set_ks_rs_from_m200_c200
+// (pmode 1) and NFW::set_ks_c200_from_m200_rs (pmode 2), models.cpp:959-976,
+// in the reference's operation order (pow(., 0.333333333333), not cbrt).
+static int nfw_from_mass(const qlp_lens& d, const double* p, double& ks, double& rs)
+{
+    const double m200 = p[0];
+    if (!(m200 > 0) || !(d.sigma_cr > 0) || !(d.kpc_to_arcsec > 0) || !(d.critical_density > 0)) return QLP_ERR_ARG;
+    const double rvir_kpc = pow(m200 / (200.0 * QL_4PI / 3.0 * 1e-9 * d.critical_density), 0.333333333333);
+    double c200, rs_kpc;
+    if (d.type == QLP_LENS_NFW_M200_C) {
+        c200 = p[1];
+        if (!(c200 > 0)) return QLP_ERR_ARG;
+        rs_kpc = rvir_kpc / c200;
+        rs = rs_kpc * d.kpc_to_arcsec;
+    } else {
+        rs_kpc = p[1];
+        if (!(rs_kpc > 0)) return QLP_ERR_ARG;
+        rs = rs_kpc * d.kpc_to_arcsec;
+        c200 = rvir_kpc / rs_kpc;
+    }
+    ks = m200 / (QL_4PI * rs * rs * d.sigma_cr * (log(1 + c200) - c200 / (1 + c200)));
+    return QLP_OK;
 }
 
 // LensProfile::set_angle with orient_major_axis_north (profile.cpp:1625-1637)
@@ -56,11 +89,19 @@ static void set_angle(LensRec& L, double theta_deg)
     L.costheta = -s;
 }
 
-int make_lens_rec(LensRec& L, int type, int plane, const double* p)
+int make_lens_rec(LensRec& L, const qlp_lens& d, const double* p)
 {
     memset(&L, 0, sizeof(L));
+    int type = d.type;
     L.type = type;
-    L.plane = plane;
+    L.plane = d.plane;
+    double nfw_p[2];
+    if (type == QLP_LENS_NFW_M200_C || type == QLP_LENS_NFW_M200_RS) {
+        // the device sees an ordinary (ks, rs) NFW lens
+        int r = nfw_from_mass(d, p, nfw_p[0], nfw_p[1]);
+        if (r != QLP_OK) return r;
+        type = L.type = QLP_LENS_NFW;
+    }
     if (type == QLP_LENS_SPLE) {
         L.b = p[0]; L.alpha = p[1]; L.s = p[2]; L.q = p[3];
         if (L.s < 0) L.s = -L.s;
@@ -82,7 +123,9 @@ int make_lens_rec(LensRec& L, int type, int plane, const double* p)
         L.shear2 = p[0] * sin(2 * theta_eff);
         L.xc = p[2]; L.yc = p[3];
     } else if (type == QLP_LENS_NFW) {
-        L.ks = p[0]; L.rs = p[1]; L.q = p[2];
+        if (d.type == QLP_LENS_NFW) { L.ks = p[0]; L.rs = p[1]; }
+        else { L.ks = nfw_p[0]; L.rs = nfw_p[1]; }
+        L.q = p[2];
         if (!(L.q > 0) || L.q > 1 || !(L.rs > 0)) return QLP_ERR_ARG;
         set_angle(L, p[3]);
         L.xc = p[4]; L.yc = p[5];
@@ -134,6 +177,27 @@ void qlp_srcgrid_defaults(qlp_srcgrid_opts* o)
 }
 
 const char* qlp_last_error(void) { return t_err.c_str(); }
+
+int qlp_set_fit_params(qlp_ctx* c, const qlp_fit_param* fp, int n)
+{
+    if (!c || (n > 0 && !fp) || n < 0) return fail(QLP_ERR_ARG, "bad fit parameters");
+    if (fit_set(c, fp, n) != QLP_OK) return fail(QLP_ERR_ARG, "bad fit parameter (target, transform or prior)");
+    return QLP_OK;
+}
+
+int qlp_fit_terms(const qlp_fit_param* fp, int n, const double* x, double* transformed, int* penalised,
+                  double* terms)
+{
+    if (!fp || n < 1 || !x || !transformed || !penalised || !terms) return fail(QLP_ERR_ARG, "bad arguments");
+    return fit_terms(fp, n, x, transformed, penalised, terms);
+}
+
+int qlp_fit_loglike_batch(qlp_ctx* c, const double* x, int n, double* loglike, qlp_result* out)
+{
+    if (!c || !x || n < 1 || !loglike) return fail(QLP_ERR_ARG, "bad arguments");
+    if (c->fit.empty()) return fail(QLP_ERR_ARG, "no fit parameters set (qlp_set_fit_params)");
+    return fit_loglike_batch(c, x, n, loglike, out);
+}
 
 long long qlp_last_launch_count(const qlp_ctx* ctx) { return ctx ? ctx->last_launches : 0; }
 
@@ -294,6 +358,13 @@ int qlp_nfw_surrogate_train(int device, const qlp_surrogate_opts* opts, qlp_surr
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(QLP_ERR_NO_DEVICE, "no CUDA device");
     if (device < 0 || device >= n) return fail(QLP_ERR_ARG, "bad device");
     return surrogate_train(device, opts ? opts : &d, rep);
+}
+
+int qlp_set_nfw_tolerance(qlp_ctx* c, double tol)
+{
+    if (!c || !(tol < 1)) return fail(QLP_ERR_ARG, "bad NFW quadrature tolerance");
+    c->nfw_tol = (tol > 0) ? tol : 1e-3;
+    return QLP_OK;
 }
 
 int qlp_set_nfw_mode(qlp_ctx* c, int mode, double threshold_arcsec)

@@ -61,6 +61,7 @@ struct qlp_ctx {
 
     // lens model
     std::vector<qlp_lens> lenses;
+    std::vector<qlp_fit_param> fit;    // qlp_set_fit_params
     qlp_planes planes{};
 
     // host copies of the static inputs
@@ -103,6 +104,7 @@ struct qlp_ctx {
     int regopt_maxit = 20;
     int nfw_mode = QLP_NFW_QUADRATURE;    // NFW deflection: quadrature or trained surrogate
     double nfw_threshold = 2e-5;          // surrogate error bound (arcsec) above which a ray falls back
+    double nfw_tol = 1e-3;                // the NFW quadrature's tolerance (QLens integral_tolerance)
     // outside-surface-brightness prior (QLens 'outside_sb_prior'): settings,
     // device tables of the extended mask, background noise of the image
     int osb_on = 0;
@@ -129,7 +131,11 @@ int ctx_eval_batch(qlp_ctx* c, const double* params, const double* regparams, co
 int ctx_dump(qlp_ctx* c, double* srcpt_xy, int* L_rowptr, int* L_index, double* L_value, int* active_index,
              double* D, double* s, double* model);
 int ctx_dump_Lpsf(qlp_ctx* c, int rows, double* out);
-int make_lens_rec(LensRec& L, int type, int plane, const double* p);
+int make_lens_rec(LensRec& L, const qlp_lens& d, const double* p);
+int fit_set(qlp_ctx* c, const qlp_fit_param* fp, int n);
+int fit_loglike_batch(qlp_ctx* c, const double* x, int n, double* loglike, qlp_result* out);
+int fit_terms(const qlp_fit_param* fp, int n, const double* x, double* t, int* penalised, double* terms);
+bool is_nfw_type(int type);
 int n_params_of(int type);
 void set_error(const char* fmt, const char* a, int code);
 // mixed.cu

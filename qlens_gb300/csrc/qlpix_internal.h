@@ -20,6 +20,7 @@ struct LensRec {
     double q, qsq, b, bprime, s, sprime, ssq, alpha;
     double shear1, shear2;
     double ks, rs, f_major_axis, epsilon;   // NFW
+    double tol;                             // NFW: the quadrature's relative tolerance (QLens integral_tolerance)
 };
 
 struct LensModel {
@@ -163,6 +164,8 @@ struct Work {
     int* Lidx;    double* Lval;        // pre-PSF L, CSR
     int* cidx;    double* cval; int* ccnt;   // compressed rows (duplicates summed), same capacity
     double* Lpsf;                      // N x ldL, FP64
+    unsigned char* lnz;                // plain path: nonzero flags of L' per (64-column block, 16-row chunk)
+    int lnz_chunks;                    // row chunks per column block in lnz
     int ldL;                           // leading dimension of Lpsf (>= M_max)
     double* dvec; double* cvec;        // N: data and C^-1 per active row
     double* D;                         // M

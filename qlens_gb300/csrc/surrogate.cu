@@ -23,11 +23,12 @@
 // forward pass, the backward pass and the weight gradients (split over the
 // batch, reduced in a fixed order), Adam; the loss weights each sample by its
 // squared dimensionless deflection, since the error the gate tests is |alpha|
-// times the relative error.  Inference (sur_mlp_cta): 128 rays per CTA = the
-// 128 TMEM lanes; layer 0 (3 -> 128) on the CUDA cores, layers 1-3
-// (128 x 128) as tcgen05 kind::tf32 MMAs with the activations in TMEM
-// (A operand, TF32 hi + lo) and the weights TMA-loaded into shared memory
-// (B operand, hi + lo), 3xTF32; the output layer on the CUDA cores.
+// times the relative error.  Inference (sur_mlp_wg): 128 rays per warpgroup =
+// the 128 TMEM lanes, two warpgroups per persistent CTA; layer 0 (3 -> 128) on
+// the CUDA cores, layers 1-3 (128 x 128) as tcgen05 kind::f16 MMAs with the
+// activations in TMEM (A operand, F16 hi + lo) and the weights resident in
+// shared memory (B operand, F16 hi + lo), three products per K step; the
+// output layer on the CUDA cores.
 //
 // Error bound.  After training the surrogate is compared with the quadrature
 // (tolerance 1e-10) on 32 jittered points of every cell of a 64 x 16 x 16 grid
@@ -37,6 +38,7 @@
 // default) and its inputs lie inside the trained domain; every other ray
 // takes the quadrature.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -346,117 +348,142 @@ __global__ void k_sur_adam(int n, float* __restrict__ p, const float* __restrict
 // ---------------------------------------------------------------------------
 // inference on the tensor cores
 // ---------------------------------------------------------------------------
-struct SurMaps {
-    CUtensorMap m[6];     // layer 1..3, hi then lo: [128 out][128 in] FP32, 32x128 boxes, 128-byte swizzle
-};
-#define SUR_SMALL (3 * SUR_H + 4 * SUR_H + 2 * SUR_H + 2)   // W0, b0..b3, W4, b4
-#define SUR_TILE (SUR_H * 32 * 4)                            // 16 KB: 128 rows x 32 K
-#define SUR_SMEM (8 * SUR_TILE + 1024 + SUR_SMALL * 4)
+// Layers 1-3 (128 x 128) run as tcgen05 kind::f16 MMAs -- M = 128 rays,
+// N = 128 outputs, K = 128 inputs -- with both operands split into an F16
+// high part and an F16 remainder (hi*hi + hi*lo + lo*hi: ~22 significant
+// bits, as 3xTF32, at the F16 tensor rate).  The activations (tanh, |h| <= 1)
+// enter scaled by 2^SUR_ACT_EXP and each layer's weights by 2^s_l (largest
+// entry near 2^14), so both parts stay in F16's normal range; the epilogue
+// multiplies the accumulator by 2^-(SUR_ACT_EXP + s_l), which is exact.
+//   B (weights): resident in shared memory for the kernel's life -- the F16
+//     image [3 layers][hi, lo][2 K blocks][128 output rows][64 inputs] in the
+//     128-byte swizzled K-major layout the MMA descriptor reads (192 KB),
+//     built once after training (k_sur_prep) and copied in by bulk copies;
+//   A (activations): in TMEM, two F16 per 32-bit column (even k in the low
+//     half), hi and lo 64 columns each;
+//   D: 128 FP32 columns of TMEM.
+// Persistent CTAs, one per SM, two warpgroups: each owns 256 TMEM columns
+// (D | A_hi | A_lo) and runs 128-ray groups of its own, so one warpgroup's
+// epilogue and FP64 lens work overlap the other's MMAs.
+#define SUR_SMALL (3 * SUR_H + 4 * SUR_H + 2 * SUR_H + 2 + 3)   // W0, b0..b3, W4, b4, unscale of layers 1..3
+#define SUR_OPB (SUR_H * SUR_H * 2)                              // one F16 part of one layer: 32 KB
+#define SUR_WIMG (3 * 2 * SUR_OPB)                               // 192 KB
+#define SUR_ACT_EXP 14
+#define SUR_SMEM (SUR_WIMG + 1024 + SUR_SMALL * 4)
+#define SUR_THREADS 256
 
-__device__ __forceinline__ void mma_tf32_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
-                                            uint32_t acc)
+__device__ __forceinline__ void mma_f16_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t acc)
 {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
         "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(acc)
         : "memory");
 }
 
-__device__ __forceinline__ void tmem_st_32cols(uint32_t taddr, const float* v)
+__device__ __forceinline__ void tmem_st_32cols_u(uint32_t taddr, const uint32_t* v)
 {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
         "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
         "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
-        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
-        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-        "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
-        "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
-        "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
-        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
-        "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
-        "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
+        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
+        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
         : "memory");
 }
 
-__device__ __forceinline__ float tf32_round(float f)
+// (a, b) -> packed F16 high parts and packed F16 remainders, a in the low half
+__device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint32_t& lo)
 {
-    uint32_t u;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(f));
-    return __uint_as_float(u);
+    const __half ah = __float2half_rn(a), bh = __float2half_rn(b);
+    const __half al = __float2half_rn(a - __half2float(ah)), bl = __float2half_rn(b - __half2float(bh));
+    hi = (uint32_t)__half_as_ushort(ah) | ((uint32_t)__half_as_ushort(bh) << 16);
+    lo = (uint32_t)__half_as_ushort(al) | ((uint32_t)__half_as_ushort(bl) << 16);
 }
 
-// Per-CTA state of the tensor-core MLP.
-struct SurCta {
-    unsigned char* tiles;   // 8 x 16 KB, 1024-aligned
-    float* small;           // SUR_SMALL floats
-    uint64_t* tma_bar;
-    uint64_t* mma_bar;
+// named barrier of one warpgroup (ids 1, 2; 0 is __syncthreads)
+__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+
+// true on every thread of the warpgroup if p holds on any of them
+__device__ __forceinline__ bool wg_any(int wg, bool p)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred pi, po;\n\t"
+        "setp.ne.u32 pi, %1, 0;\n\t"
+        "bar.red.or.pred po, %2, 128, pi;\n\t"
+        "selp.u32 %0, 1, 0, po;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)p), "r"(1 + wg)
+        : "memory");
+    return r != 0;
+}
+
+// Per-warpgroup state of the tensor-core MLP.
+struct SurWG {
+    const unsigned char* w;   // weight image in shared memory (1024-aligned)
+    const float* small;       // SUR_SMALL floats in shared memory
+    uint64_t* mma_bar;        // this warpgroup's MMA-completion barrier
     volatile int* abort;
-    uint32_t tmem;          // 512 columns: D [0,128), A_hi [128,256), A_lo [256,384)
-    uint32_t phase;         // completed layers (mbarrier parity)
+    uint32_t tmem;            // this warpgroup's columns: D [0,128), A_hi [128,192), A_lo [192,256)
+    uint32_t phase;           // completed layers (mbarrier parity)
+    int wg;
 };
 
-// All 128 threads call this with their ray's inputs; returns the network's
-// two outputs.  ok is cleared if a bounded wait ran out.
-__device__ void sur_mlp_cta(SurCta& S, const SurMaps& maps, float f0, float f1, float f2, float& t0, float& t1,
-                            bool& ok)
+// The 128 threads of a warpgroup call this together, each with its ray's
+// inputs; returns the network's two outputs.  ok is cleared if a bounded wait
+// ran out.
+__device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, float& t1, bool& ok)
 {
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t lane_base = ((uint32_t)(warp * 32)) << 16;
+    const int tid = threadIdx.x & 127, warp = tid >> 5;
+    const uint32_t row = S.tmem + (((uint32_t)(warp * 32)) << 16);   // this warp's 32 lanes
     const float* W0 = S.small;
     const float* bb = S.small + 3 * SUR_H;          // b0, b1, b2, b3
     const float* W4 = S.small + 7 * SUR_H;
     const float* b4 = S.small + 9 * SUR_H;
-    // layer 0 on the CUDA cores, straight into TMEM as the next A operand (hi, lo)
+    const float* unscale = S.small + 9 * SUR_H + 2;
+    const float ascale = (float)(1 << SUR_ACT_EXP);
+    // layer 0 on the CUDA cores, straight into TMEM as the next A operand
     #pragma unroll 1
-    for (int c = 0; c < SUR_H; c += 32) {
-        float hi[32], lo[32];
+    for (int c = 0; c < SUR_H; c += 64) {
+        uint32_t hi[32], lo[32];
         #pragma unroll
         for (int j = 0; j < 32; j++) {
-            const int u = c + j;
-            const float h =
-                sur_tanh(__fmaf_rn(W0[2 * SUR_H + u], f2, __fmaf_rn(W0[SUR_H + u], f1, __fmaf_rn(W0[u], f0, bb[u]))));
-            hi[j] = tf32_round(h);
-            lo[j] = tf32_round(h - hi[j]);
+            const int u = c + 2 * j;
+            const float h0 = sur_tanh(
+                __fmaf_rn(W0[2 * SUR_H + u], f2, __fmaf_rn(W0[SUR_H + u], f1, __fmaf_rn(W0[u], f0, bb[u]))));
+            const float h1 = sur_tanh(__fmaf_rn(W0[2 * SUR_H + u + 1], f2,
+                                                __fmaf_rn(W0[SUR_H + u + 1], f1, __fmaf_rn(W0[u + 1], f0, bb[u + 1]))));
+            f16_split2(h0 * ascale, h1 * ascale, hi[j], lo[j]);
         }
-        tmem_st_32cols(S.tmem + lane_base + 128 + c, hi);
-        tmem_st_32cols(S.tmem + lane_base + 256 + c, lo);
+        tmem_st_32cols_u(row + 128 + c / 2, hi);
+        tmem_st_32cols_u(row + 192 + c / 2, lo);
     }
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     float o0 = 0.f, o1 = 0.f;
     for (int l = 1; l <= 3; l++) {
         tc_fence_before();
-        __syncthreads();
+        wg_sync(S.wg);
         tc_fence_after();
         if (tid == 0) {
-            mbar_expect_tx(S.tma_bar, 8 * SUR_TILE);
-            for (int kb = 0; kb < 4; kb++) {
-                tma_load_2d(&maps.m[2 * (l - 1)], S.tma_bar, S.tiles + (kb * 2 + 0) * SUR_TILE, kb * 32, 0);
-                tma_load_2d(&maps.m[2 * (l - 1) + 1], S.tma_bar, S.tiles + (kb * 2 + 1) * SUR_TILE, kb * 32, 0);
-            }
-        }
-        if (tid == 32) {
-            const bool w = mbar_wait_bounded(S.tma_bar, S.phase & 1, S.abort, false);
-            tc_fence_after();
-            if (w) {
-                const uint32_t idesc = idesc_tf32_128x128();
-                for (int kb = 0; kb < 4; kb++) {
-                    const uint64_t b_hi = sdesc_sw128(smem_u32(S.tiles + (kb * 2 + 0) * SUR_TILE));
-                    const uint64_t b_lo = sdesc_sw128(smem_u32(S.tiles + (kb * 2 + 1) * SUR_TILE));
-                    #pragma unroll
-                    for (int kk = 0; kk < 4; kk++) {
-                        const uint32_t ka = (uint32_t)(kb * 32 + kk * 8);
-                        const uint64_t off = (uint64_t)((kk * 32) >> 4);
-                        mma_tf32_ta(S.tmem, S.tmem + 128 + ka, b_hi + off, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32_ta(S.tmem, S.tmem + 128 + ka, b_lo + off, idesc, 1u);
-                        mma_tf32_ta(S.tmem, S.tmem + 256 + ka, b_hi + off, idesc, 1u);
-                    }
+            const uint32_t idesc = idesc_f16_128x128();
+            const unsigned char* wl = S.w + (size_t)(l - 1) * 2 * SUR_OPB;
+            #pragma unroll
+            for (int kb = 0; kb < 2; kb++) {
+                const uint64_t b_hi = sdesc_sw128(smem_u32(wl + kb * (SUR_OPB / 2)));
+                const uint64_t b_lo = sdesc_sw128(smem_u32(wl + SUR_OPB + kb * (SUR_OPB / 2)));
+                #pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    // 16 inputs per MMA: 32 bytes of a weight row, 8 TMEM columns of A
+                    const uint32_t ka = (uint32_t)(kb * 32 + kk * 8);
+                    const uint64_t off = (uint64_t)((kk * 32) >> 4);
+                    mma_f16_ta(S.tmem, S.tmem + 128 + ka, b_hi + off, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+                    mma_f16_ta(S.tmem, S.tmem + 128 + ka, b_lo + off, idesc, 1u);
+                    mma_f16_ta(S.tmem, S.tmem + 192 + ka, b_hi + off, idesc, 1u);
                 }
             }
             mma_commit(S.mma_bar);
@@ -466,23 +493,25 @@ __device__ void sur_mlp_cta(SurCta& S, const SurMaps& maps, float f0, float f1, 
         tc_fence_after();
         S.phase++;
         if (!done || *S.abort) ok = false;
-        // epilogue: bias, tanh; layers 1-2 back into TMEM, layer 3 into the output layer
+        // epilogue: unscale, bias, tanh; layers 1-2 back into TMEM as A, layer 3 into the output layer
+        const float us = unscale[l - 1];
         const float* bl = bb + l * SUR_H;
         #pragma unroll 1
-        for (int c = 0; c < SUR_H; c += 32) {
-            float v[32];
-            tmem_ld_32cols(S.tmem + lane_base + c, v);
+        for (int c = 0; c < SUR_H; c += 64) {
+            float v[64];
+            tmem_ld_32cols(row + c, v);
+            tmem_ld_32cols(row + c + 32, v + 32);
             #pragma unroll
-            for (int j = 0; j < 32; j++) v[j] = sur_tanh(v[j] + bl[c + j]);
+            for (int j = 0; j < 64; j++) v[j] = sur_tanh(__fmaf_rn(v[j], us, bl[c + j]));
             if (l < 3) {
-                float hi[32], lo[32];
+                uint32_t hi[32], lo[32];
                 #pragma unroll
-                for (int j = 0; j < 32; j++) { hi[j] = tf32_round(v[j]); lo[j] = tf32_round(v[j] - hi[j]); }
-                tmem_st_32cols(S.tmem + lane_base + 128 + c, hi);
-                tmem_st_32cols(S.tmem + lane_base + 256 + c, lo);
+                for (int j = 0; j < 32; j++) f16_split2(v[2 * j] * ascale, v[2 * j + 1] * ascale, hi[j], lo[j]);
+                tmem_st_32cols_u(row + 128 + c / 2, hi);
+                tmem_st_32cols_u(row + 192 + c / 2, lo);
             } else {
                 #pragma unroll
-                for (int j = 0; j < 32; j++) {
+                for (int j = 0; j < 64; j++) {
                     o0 = __fmaf_rn(v[j], W4[2 * (c + j)], o0);
                     o1 = __fmaf_rn(v[j], W4[2 * (c + j) + 1], o1);
                 }
@@ -494,23 +523,32 @@ __device__ void sur_mlp_cta(SurCta& S, const SurMaps& maps, float f0, float f1, 
     t1 = o1 + b4[1];
 }
 
-__device__ __forceinline__ void sur_cta_begin(SurCta& S, unsigned char* smem_raw, const float* __restrict__ small_g,
-                                              uint64_t* tma_bar, uint64_t* mma_bar, uint32_t* tmem_slot,
-                                              volatile int* abort)
+// CTA set-up of the persistent MLP kernels (all SUR_THREADS threads): the
+// weight image into shared memory by bulk copies, the small parameters, the
+// barriers and 512 TMEM columns; returns false if the weights did not arrive
+// within the bounded wait.
+__device__ __forceinline__ bool sur_cta_begin(SurWG& S, unsigned char* smem_raw, const unsigned char* __restrict__ wimg,
+                                              const float* __restrict__ small_g, uint64_t* w_bar, uint64_t* mma_bar,
+                                              uint32_t* tmem_slot, volatile int* abort)
 {
-    S.tiles = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    S.small = reinterpret_cast<float*>(S.tiles + 8 * SUR_TILE);
-    S.tma_bar = tma_bar;
-    S.mma_bar = mma_bar;
-    S.abort = abort;
-    S.phase = 0;
-    for (int i = threadIdx.x; i < SUR_SMALL; i += blockDim.x) S.small[i] = small_g[i];
+    unsigned char* w = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float* small = reinterpret_cast<float*>(w + SUR_WIMG);
+    const int wg = threadIdx.x >> 7;
     if (threadIdx.x == 0) {
-        mbar_init(tma_bar, 1);
-        mbar_init(mma_bar, 1);
+        mbar_init(w_bar, 1);
+        mbar_init(&mma_bar[0], 1);
+        mbar_init(&mma_bar[1], 1);
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_expect_tx(w_bar, SUR_WIMG);
+        for (int k = 0; k < 6; k++)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(w + k * SUR_OPB)),
+                "l"(wimg + (size_t)k * SUR_OPB), "r"((uint32_t)SUR_OPB), "r"(smem_u32(w_bar))
+                : "memory");
     }
+    for (int i = threadIdx.x; i < SUR_SMALL; i += blockDim.x) small[i] = small_g[i];
     if ((threadIdx.x >> 5) == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(512)
@@ -520,166 +558,182 @@ __device__ __forceinline__ void sur_cta_begin(SurCta& S, unsigned char* smem_raw
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    S.tmem = *tmem_slot;
+    S.w = w;
+    S.small = small;
+    S.mma_bar = &mma_bar[wg];
+    S.abort = abort;
+    S.tmem = *tmem_slot + (uint32_t)(wg * 256);
+    S.phase = 0;
+    S.wg = wg;
+    return mbar_wait_bounded(w_bar, 0, abort, false);
 }
 
-__device__ __forceinline__ void sur_cta_end(SurCta& S)
+__device__ __forceinline__ void sur_cta_end(const SurWG& S, uint32_t tmem_base)
 {
     tc_fence_before();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(512) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512) : "memory");
     }
 }
 
-// Batch inference for the error-bound table and the tests: T[i] = net(X[i]).
-__global__ void __launch_bounds__(128, 1) k_sur_infer(int n, const float* __restrict__ X, float* __restrict__ T,
-                                                      const __grid_constant__ SurMaps maps,
-                                                      const float* __restrict__ small_g, int* status)
+// Batch inference for the error-bound table and the tests: T[i] = net(X[i]),
+// persistent over 128-point groups.
+__global__ void __launch_bounds__(SUR_THREADS, 1) k_sur_infer(int n, const float* __restrict__ X,
+                                                              float* __restrict__ T,
+                                                              const unsigned char* __restrict__ wimg,
+                                                              const float* __restrict__ small_g, int* status)
 {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ uint64_t tma_bar, mma_bar;
+    __shared__ uint64_t w_bar, mma_bar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
-    SurCta S;
-    sur_cta_begin(S, smem_raw, small_g, &tma_bar, &mma_bar, &tmem_slot, &abort_flag);
-    const int i = blockIdx.x * 128 + threadIdx.x;
-    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-    if (i < n) { f0 = X[3 * (size_t)i]; f1 = X[3 * (size_t)i + 1]; f2 = X[3 * (size_t)i + 2]; }
-    float t0, t1;
-    bool ok = true;
-    sur_mlp_cta(S, maps, f0, f1, f2, t0, t1, ok);
-    if (i < n) { T[2 * (size_t)i] = t0; T[2 * (size_t)i + 1] = t1; }
-    if (!ok && threadIdx.x == 0) atomicExch(status, QLP_ERR_TIMEOUT);
-    sur_cta_end(S);
+    SurWG S;
+    bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag);
+    const int tid = threadIdx.x & 127;
+    for (int grp = blockIdx.x * 2 + S.wg; grp * 128 < n; grp += gridDim.x * 2) {
+        if (wg_any(S.wg, !ok || abort_flag)) { ok = false; break; }
+        const int i = grp * 128 + tid;
+        float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+        if (i < n) { f0 = X[3 * (size_t)i]; f1 = X[3 * (size_t)i + 1]; f2 = X[3 * (size_t)i + 2]; }
+        float t0, t1;
+        sur_mlp_wg(S, f0, f1, f2, t0, t1, ok);
+        if (i < n) { T[2 * (size_t)i] = t0; T[2 * (size_t)i + 1] = t1; }
+    }
+    if (!ok && tid == 0) atomicExch(status, QLP_ERR_TIMEOUT);
+    sur_cta_end(S, tmem_slot);
 }
 
 // Ray shooting with NFW lenses on the surrogate: k_raytrace's lens equation
-// (QLens::find_sourcept, lenscalc.cpp:81-113), 128 rays per CTA.  At every
-// NFW lens with q < 1 all 128 threads run the network together (unless no
-// ray of the CTA can pass the gate, then none does); a ray whose bound
-// exceeds `thresh` (or whose inputs leave the domain) takes the quadrature
-// instead -- right here, or, for the lens `defer_lens` (the only NFW lens, on
-// the last plane), later in k_nfw_fallback at full occupancy (its lens-frame
-// position is queued and its contribution left out here).  out->pad counts
-// the fallbacks.
-__global__ void __launch_bounds__(128, 1) k_raytrace_sur(StaticData sd_, const EvalParams* __restrict__ ep,
-                                                         double* __restrict__ spx, double* __restrict__ spy,
-                                                         const __grid_constant__ SurMaps maps,
-                                                         const float* __restrict__ small_g,
-                                                         const float* __restrict__ bound, double thresh,
-                                                         int defer_lens, int* __restrict__ fb_count,
-                                                         int* __restrict__ fb_ray, double* __restrict__ fb_xy,
-                                                         GridState* gs, EvalOut* out)
+// (QLens::find_sourcept, lenscalc.cpp:81-113), persistent over 128-ray groups,
+// one group per warpgroup at a time.  At every NFW lens with q < 1 the 128
+// threads of the warpgroup run the network together (unless no ray of the
+// group can pass the gate, then none does); a ray whose bound exceeds
+// `thresh` (or whose inputs leave the domain) takes the quadrature instead --
+// right here, or, for the lens `defer_lens` (the only NFW lens, on the last
+// plane), later in k_nfw_fallback at full occupancy (its lens-frame position
+// is queued and its contribution left out here).  out->pad counts the
+// fallbacks.
+__global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_, const EvalParams* __restrict__ ep,
+                                                                 double* __restrict__ spx, double* __restrict__ spy,
+                                                                 const unsigned char* __restrict__ wimg,
+                                                                 const float* __restrict__ small_g,
+                                                                 const float* __restrict__ bound, double thresh,
+                                                                 int defer_lens, int* __restrict__ fb_count,
+                                                                 int* __restrict__ fb_ray, double* __restrict__ fb_xy,
+                                                                 GridState* gs, EvalOut* out)
 {
     const StaticData sd = eval_shape(sd_);
-    if ((int)blockIdx.x * 128 >= sd.n_sub) return;      // launched for the slot's capacity
     extern __shared__ unsigned char smem_raw[];
-    __shared__ uint64_t tma_bar, mma_bar;
+    __shared__ uint64_t w_bar, mma_bar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
     __shared__ __align__(16) LensModel lm;
     __shared__ int n_fb;
+    if ((int)blockIdx.x * 2 * 128 >= sd.n_sub) return;     // launched for the slot's capacity
     {
         const double* src = reinterpret_cast<const double*>(&ep->lm);
         double* dst = reinterpret_cast<double*>(&lm);
         for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
         if (threadIdx.x == 0) n_fb = 0;
     }
-    SurCta S;
-    sur_cta_begin(S, smem_raw, small_g, &tma_bar, &mma_bar, &tmem_slot, &abort_flag);
-    const int t = blockIdx.x * 128 + threadIdx.x;
-    const bool valid = t < sd.n_sub;
-    double px = 0, py = 0;
-    if (valid) {
-        const int ns = sd.nsplit, nsub = sd.nsub;
-        const int m = t / nsub, k = t - m * nsub;
-        const int pix = sd.mpix[m];
-        const int i = pix / sd.ny, j = pix - i * sd.ny;
-        const int ii = k / ns, jj = k - ii * ns;
-        const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
-        const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
-        px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
-        py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
-    }
-    bool ok = true;
+    SurWG S;
+    bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag);
+    const int tid = threadIdx.x & 127;
     int fb = 0;
-    double defx = 0, defy = 0;
-    double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
-    for (int p = 0; p < lm.n_planes; p++) {
-        dsx[p] = 0; dsy[p] = 0;
-        if (lm.zfac[p] == 0.0) continue;
-        double xi = px, yi = py;
-        for (int jp = 0; jp < p; jp++) {
-            xi -= lm.beta[p - 1][jp] * dsx[jp];
-            yi -= lm.beta[p - 1][jp] * dsy[jp];
+    for (int grp = blockIdx.x * 2 + S.wg; grp * 128 < sd.n_sub; grp += gridDim.x * 2) {
+        if (wg_any(S.wg, !ok || abort_flag)) { ok = false; break; }
+        const int t = grp * 128 + tid;
+        const bool valid = t < sd.n_sub;
+        double px = 0, py = 0;
+        if (valid) {
+            const int ns = sd.nsplit, nsub = sd.nsub;
+            const int m = t / nsub, k = t - m * nsub;
+            const int pix = sd.mpix[m];
+            const int i = pix / sd.ny, j = pix - i * sd.ny;
+            const int ii = k / ns, jj = k - ii * ns;
+            const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
+            const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
+            px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
+            py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
         }
-        for (int k = 0; k < lm.nlens; k++) {
-            const LensRec& L = lm.lens[k];
-            if (L.plane != p) continue;
-            double ax, ay;
-            if (L.type == QLP_LENS_NFW && L.q != 1.0) {
-                // LensProfile::deflection: shift, rotate, deflect, rotate back
-                double x = xi - L.xc, y = yi - L.yc;
-                const bool rot = (L.sintheta != 0);
-                if (rot) {
-                    const double xp = x * L.costheta + y * L.sintheta;
-                    y = -x * L.sintheta + y * L.costheta;
-                    x = xp;
-                }
-                const SurIn in = sur_inputs(x / L.rs, y / L.rs, L.q);
-                const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
-                // before the network: |alpha| ~ ks B |(x, y)| (G is within a few
-                // tens of percent of B), so a CTA none of whose rays can pass the
-                // gate skips the network and sends every ray to the quadrature
-                const bool maybe = valid && !centre && in.bin >= 0 &&
-                                   L.ks * in.B * sqrt(x * x + y * y) * (double)bound[in.bin] <= 1.5 * thresh;
-                double bx = 0, by = 0;
-                bool use = false;
-                if (__syncthreads_or(maybe)) {
-                    float t0, t1;
-                    sur_mlp_cta(S, maps, in.f0, in.f1, in.f2, t0, t1, ok);
-                    const double G0 = in.B * exp((1.0 - L.q) * t0), G1 = in.B * exp((1.0 - L.q) * t1);
-                    bx = x * L.ks * G0;
-                    by = y * L.ks * G1;
-                    const double mag = sqrt(bx * bx + by * by);
-                    use = ok && !centre && in.bin >= 0 && mag * (double)bound[in.bin] <= thresh;
-                }
-                if (!use && valid) {
-                    fb++;
-                    if (k == defer_lens) {
-                        const int e = atomicAdd(fb_count, 1);
-                        fb_ray[e] = t;
-                        fb_xy[2 * (size_t)e] = x;
-                        fb_xy[2 * (size_t)e + 1] = y;
-                        bx = 0; by = 0;
-                    } else {
-                        nfw_deflection(L, x, y, bx, by);
-                    }
-                }
-                if (rot) {
-                    const double xp = bx * L.costheta - by * L.sintheta;
-                    by = bx * L.sintheta + by * L.costheta;
-                    bx = xp;
-                }
-                ax = bx; ay = by;
-            } else {
-                lens_deflection<true>(L, xi, yi, ax, ay);
+        double defx = 0, defy = 0;
+        double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
+        for (int p = 0; p < lm.n_planes; p++) {
+            dsx[p] = 0; dsy[p] = 0;
+            if (lm.zfac[p] == 0.0) continue;
+            double xi = px, yi = py;
+            for (int jp = 0; jp < p; jp++) {
+                xi -= lm.beta[p - 1][jp] * dsx[jp];
+                yi -= lm.beta[p - 1][jp] * dsy[jp];
             }
-            dsx[p] += ax; dsy[p] += ay;
+            for (int k = 0; k < lm.nlens; k++) {
+                const LensRec& L = lm.lens[k];
+                if (L.plane != p) continue;
+                double ax, ay;
+                if (L.type == QLP_LENS_NFW && L.q != 1.0) {
+                    // LensProfile::deflection: shift, rotate, deflect, rotate back
+                    double x = xi - L.xc, y = yi - L.yc;
+                    const bool rot = (L.sintheta != 0);
+                    if (rot) {
+                        const double xp = x * L.costheta + y * L.sintheta;
+                        y = -x * L.sintheta + y * L.costheta;
+                        x = xp;
+                    }
+                    const SurIn in = sur_inputs(x / L.rs, y / L.rs, L.q);
+                    const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
+                    // before the network: |alpha| ~ ks B |(x, y)| (G is within a few
+                    // tens of percent of B), so a group none of whose rays can pass
+                    // the gate skips the network and sends every ray to the quadrature
+                    const bool maybe = valid && !centre && in.bin >= 0 &&
+                                       L.ks * in.B * sqrt(x * x + y * y) * (double)bound[in.bin] <= 1.5 * thresh;
+                    double bx = 0, by = 0;
+                    bool use = false;
+                    if (wg_any(S.wg, maybe)) {
+                        float t0, t1;
+                        sur_mlp_wg(S, in.f0, in.f1, in.f2, t0, t1, ok);
+                        const double G0 = in.B * exp((1.0 - L.q) * t0), G1 = in.B * exp((1.0 - L.q) * t1);
+                        bx = x * L.ks * G0;
+                        by = y * L.ks * G1;
+                        const double mag = sqrt(bx * bx + by * by);
+                        use = ok && !centre && in.bin >= 0 && mag * (double)bound[in.bin] <= thresh;
+                    }
+                    if (!use && valid) {
+                        fb++;
+                        if (k == defer_lens) {
+                            const int e = atomicAdd(fb_count, 1);
+                            fb_ray[e] = t;
+                            fb_xy[2 * (size_t)e] = x;
+                            fb_xy[2 * (size_t)e + 1] = y;
+                            bx = 0; by = 0;
+                        } else {
+                            nfw_deflection(L, x, y, bx, by);
+                        }
+                    }
+                    if (rot) {
+                        const double xp = bx * L.costheta - by * L.sintheta;
+                        by = bx * L.sintheta + by * L.costheta;
+                        bx = xp;
+                    }
+                    ax = bx; ay = by;
+                } else {
+                    lens_deflection<true>(L, xi, yi, ax, ay);
+                }
+                dsx[p] += ax; dsy[p] += ay;
+            }
+            dsx[p] *= lm.zfac[p];
+            dsy[p] *= lm.zfac[p];
+            defx += dsx[p];
+            defy += dsy[p];
         }
-        dsx[p] *= lm.zfac[p];
-        dsy[p] *= lm.zfac[p];
-        defx += dsx[p];
-        defy += dsy[p];
-    }
-    if (valid) {
-        spx[t] = px - defx;
-        spy[t] = py - defy;
+        if (valid) {
+            spx[t] = px - defx;
+            spy[t] = py - defy;
+        }
     }
     if (fb) atomicAdd(&n_fb, fb);
-    sur_cta_end(S);
+    sur_cta_end(S, tmem_slot);
     if (threadIdx.x == 0) {
         if (n_fb) atomicAdd(&out->pad, n_fb);
         if (!ok) atomicExch(&gs->status, QLP_ERR_TIMEOUT);
@@ -713,34 +767,37 @@ __global__ void k_nfw_fallback(const EvalParams* __restrict__ ep, int lens, cons
 // ---------------------------------------------------------------------------
 // host side: one trained network per device, shared by every context
 // ---------------------------------------------------------------------------
-typedef CUresult (*EncodeTiledFnS)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
 struct SurState {
     bool ready = false;
-    float* params = nullptr;   // training layout
-    float* wt = nullptr;       // [3 layers][hi, lo][128 out][128 in]
-    float* small = nullptr;    // SUR_SMALL
-    float* bound = nullptr;    // SUR_NBINS
-    SurMaps maps;
+    float* params = nullptr;          // training layout
+    unsigned char* wimg = nullptr;    // SUR_WIMG: layers 1-3 as the MMA's shared-memory image (k_sur_prep)
+    float* small = nullptr;           // SUR_SMALL
+    float* bound = nullptr;           // SUR_NBINS
     qlp_surrogate_report rep{};
 };
 static std::mutex g_sur_mu;
 static SurState g_sur[64];
 
-// [l][out][in] hi/lo copies of layers 1-3 and the small parameters for
-// inference, with the target normalisation folded into the output layer
-__global__ void k_sur_prep(const float* __restrict__ p, float* __restrict__ wt, float* __restrict__ small, float mu0,
-                           float mu1, float sg0, float sg1)
+// The inference copies: layers 1-3 as the F16 hi/lo image the MMAs read from
+// shared memory -- byte offset of weight (out n, in k) of layer l, part h:
+// (2 l + h) SUR_OPB + (k / 64) (SUR_OPB / 2) + 128 n + 16 ((k % 64) / 8 XOR n % 8)
+// + 2 (k % 8), the 128-byte swizzled K-major layout -- each layer scaled by
+// 2^sexp[l]; and the small parameters, with the target normalisation folded
+// into the output layer and the unscale factors 2^-(SUR_ACT_EXP + sexp[l]).
+__global__ void k_sur_prep(const float* __restrict__ p, unsigned char* __restrict__ wimg, float* __restrict__ small,
+                           float mu0, float mu1, float sg0, float sg1, int3 sexp)
 {
     const int n = 3 * SUR_H * SUR_H;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const int l = e / (SUR_H * SUR_H), r = e % (SUR_H * SUR_H), o = r / SUR_H, i = r % SUR_H;
-        const float w = p[SUR_W1 + l * (SUR_H * SUR_H + SUR_H) + i * SUR_H + o];
-        const float h = tf32_round(w);
-        wt[(size_t)(2 * l) * SUR_H * SUR_H + o * SUR_H + i] = h;
-        wt[(size_t)(2 * l + 1) * SUR_H * SUR_H + o * SUR_H + i] = tf32_round(w - h);
+        const int se = (l == 0) ? sexp.x : (l == 1) ? sexp.y : sexp.z;
+        const float w = ldexpf(p[SUR_W1 + l * (SUR_H * SUR_H + SUR_H) + i * SUR_H + o], se);
+        const __half h = __float2half_rn(w);
+        const __half lo = __float2half_rn(w - __half2float(h));
+        const size_t off = (size_t)(i / 64) * (SUR_OPB / 2) + (size_t)o * 128 +
+                           (size_t)((((i % 64) / 8) ^ (o % 8)) * 16) + (size_t)(i % 8) * 2;
+        *reinterpret_cast<__half*>(wimg + (size_t)(2 * l) * SUR_OPB + off) = h;
+        *reinterpret_cast<__half*>(wimg + (size_t)(2 * l + 1) * SUR_OPB + off) = lo;
     }
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < SUR_SMALL; e += gridDim.x * blockDim.x) {
         float v;
@@ -749,7 +806,12 @@ __global__ void k_sur_prep(const float* __restrict__ p, float* __restrict__ wt, 
             const int l = (e - 3 * SUR_H) / SUR_H, u = (e - 3 * SUR_H) % SUR_H;
             v = p[SUR_B0 + l * (SUR_H * SUR_H + SUR_H) + u];
         } else if (e < 9 * SUR_H) v = p[SUR_W4 + (e - 7 * SUR_H)] * (((e - 7 * SUR_H) & 1) ? sg1 : sg0);
-        else v = p[SUR_B4 + (e - 9 * SUR_H)] * ((e & 1) ? sg1 : sg0) + ((e & 1) ? mu1 : mu0);   // un-normalised s
+        else if (e < 9 * SUR_H + 2)
+            v = p[SUR_B4 + (e - 9 * SUR_H)] * ((e & 1) ? sg1 : sg0) + ((e & 1) ? mu1 : mu0);   // un-normalised s
+        else {
+            const int l = e - (9 * SUR_H + 2);
+            v = ldexpf(1.0f, -(SUR_ACT_EXP + ((l == 0) ? sexp.x : (l == 1) ? sexp.y : sexp.z)));
+        }
         small[e] = v;
     }
 }
@@ -774,29 +836,18 @@ __global__ void k_sur_bound(int nbins, const float* __restrict__ Tnet, const dou
     }
 }
 
-static int sur_maps(SurState& st)
+// Persistent MLP kernels: one CTA per SM at most, two 128-point groups per CTA at a time.
+static int sur_grid(int n)
 {
-    static EncodeTiledFnS enc = nullptr;
-    if (!enc) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            return QLP_ERR_CUDA;
-        enc = (EncodeTiledFnS)p;
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
     }
-    for (int k = 0; k < 6; k++) {
-        cuuint64_t dims[2] = {SUR_H, SUR_H};
-        cuuint64_t strides[1] = {SUR_H * sizeof(float)};
-        cuuint32_t box[2] = {32, SUR_H};
-        cuuint32_t estr[2] = {1, 1};
-        if (enc(&st.maps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, st.wt + (size_t)k * SUR_H * SUR_H, dims, strides,
-                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return QLP_ERR_CUDA;
-    }
-    return QLP_OK;
+    const int pairs = (n + 255) / 256;
+    return std::max(1, std::min(pairs, sms));
 }
 
 #define SCK(x)                                                                    \
@@ -887,7 +938,7 @@ int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_repor
     SCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     if (!st.params) {
         SCK(cudaMalloc(&st.params, sizeof(float) * SUR_NP));
-        SCK(cudaMalloc(&st.wt, sizeof(float) * 6 * SUR_H * SUR_H));
+        SCK(cudaMalloc(&st.wimg, SUR_WIMG));
         SCK(cudaMalloc(&st.small, sizeof(float) * SUR_SMALL));
         SCK(cudaMalloc(&st.bound, sizeof(float) * SUR_NBINS));
     }
@@ -974,16 +1025,25 @@ int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_repor
     }
     SCK(cudaGetLastError());
     // inference copies, then the error-bound table from the tensor-core path
-    k_sur_prep<<<64, 256, 0, s>>>(st.params, st.wt, st.small, mu[0], mu[1], sg[0], sg[1]);
-    SCK(cudaStreamSynchronize(s));
-    if (sur_maps(st) != QLP_OK) {
-        set_error("%s (%d)", "surrogate: tensor map encoding failed", 0);
-        rc = QLP_ERR_CUDA;
-        goto done;
+    {   // per-layer power-of-two scale: the largest weight of layers 1-3 near 2^14 in F16
+        std::vector<float> hp(SUR_NP);
+        SCK(cudaMemcpyAsync(hp.data(), st.params, sizeof(float) * SUR_NP, cudaMemcpyDeviceToHost, s));
+        SCK(cudaStreamSynchronize(s));
+        int se[3];
+        for (int l = 0; l < 3; l++) {
+            float mx = 0.f;
+            for (int e = 0; e < SUR_H * SUR_H; e++) mx = std::max(mx, std::fabs(hp[SUR_W1 + l * (SUR_H * SUR_H + SUR_H) + e]));
+            int ex = 0;
+            std::frexp(std::max(mx, 1e-30f), &ex);       // mx < 2^ex
+            se[l] = 14 - ex;
+        }
+        k_sur_prep<<<64, 256, 0, s>>>(st.params, st.wimg, st.small, mu[0], mu[1], sg[0], sg[1],
+                                      make_int3(se[0], se[1], se[2]));
     }
+    SCK(cudaStreamSynchronize(s));
     SCK(cudaFuncSetAttribute(k_sur_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
     SCK(cudaFuncSetAttribute(k_raytrace_sur, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
-    k_sur_infer<<<(nval + 127) / 128, 128, SUR_SMEM, s>>>(nval, Xv, Tnet, st.maps, st.small, dstatus);
+    k_sur_infer<<<sur_grid(nval), SUR_THREADS, SUR_SMEM, s>>>(nval, Xv, Tnet, st.wimg, st.small, dstatus);
     k_sur_bound<<<(SUR_NBINS + 255) / 256, 256, 0, s>>>(SUR_NBINS, Tnet, Gv, Bv, Qv, st.bound, stats);
     SCK(cudaGetLastError());
     {
@@ -1093,7 +1153,7 @@ int surrogate_eval(int device, const double* rpq, int n, double* t_net, double* 
     SCK(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
     SCK(cudaMemcpyAsync(P, rpq, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, s));
     k_sur_points<<<(n + 127) / 128, 128, 0, s>>>(n, P, X, G, Bd);
-    k_sur_infer<<<(n + 127) / 128, 128, SUR_SMEM, s>>>(n, X, T, st.maps, st.small, dstatus);
+    k_sur_infer<<<sur_grid(n), SUR_THREADS, SUR_SMEM, s>>>(n, X, T, st.wimg, st.small, dstatus);
     SCK(cudaGetLastError());
     SCK(cudaMemcpyAsync(ht.data(), T, sizeof(float) * 2 * (size_t)n, cudaMemcpyDeviceToHost, s));
     SCK(cudaMemcpyAsync(hb.data(), st.bound, sizeof(float) * SUR_NBINS, cudaMemcpyDeviceToHost, s));
@@ -1136,7 +1196,8 @@ int launch_raytrace_sur(const StaticData& sd, Work& w, double thresh, int defer_
     }
     SurState& S = g_sur[dev];
     cudaMemsetAsync(w.fb_count, 0, sizeof(int), st);
-    k_raytrace_sur<<<(sd.n_sub + 127) / 128, 128, SUR_SMEM, st>>>(sd, w.ep, w.spx, w.spy, S.maps, S.small, S.bound,
+    k_raytrace_sur<<<sur_grid(sd.n_sub), SUR_THREADS, SUR_SMEM, st>>>(sd, w.ep, w.spx, w.spy, S.wimg, S.small,
+                                                                       S.bound,
                                                                    thresh, defer_lens, w.fb_count, w.fb_ray,
                                                                    w.fb_xy, w.gs, w.out);
     int n = 1;

@@ -77,6 +77,7 @@ def load_library(build_if_missing=False):
     L.qlp_surrogate_defaults.argtypes = [P(abi.qlp_surrogate_opts)]
     L.qlp_nfw_surrogate_train.argtypes = [C.c_int, P(abi.qlp_surrogate_opts), P(abi.qlp_surrogate_report)]
     L.qlp_set_nfw_mode.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.qlp_set_nfw_tolerance.argtypes = [C.c_void_p, C.c_double]
     L.qlp_surrogate_grad_check.argtypes = [C.c_int, P(C.c_float), P(C.c_float), P(C.c_float), C.c_int,
                                            P(C.c_double), P(C.c_float)]
     L.qlp_surrogate_eval.argtypes = [C.c_int, P(C.c_double), C.c_int, P(C.c_double), P(C.c_double),
@@ -89,6 +90,10 @@ def load_library(build_if_missing=False):
     L.qlp_load_mask_fits.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, P(C.c_ubyte), P(C.c_int)]
     L.qlp_load_noise_map_fits.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
     L.qlp_load_psf_fits.argtypes = [C.c_char_p, C.c_double, P(C.c_double), C.c_long, P(C.c_int), P(C.c_int)]
+    L.qlp_set_fit_params.argtypes = [C.c_void_p, P(abi.qlp_fit_param), C.c_int]
+    L.qlp_fit_loglike_batch.argtypes = [C.c_void_p, P(C.c_double), C.c_int, P(C.c_double), P(abi.qlp_result)]
+    L.qlp_fit_terms.argtypes = [P(abi.qlp_fit_param), C.c_int, P(C.c_double), P(C.c_double), P(C.c_int),
+                                P(C.c_double)]
     L.qlp_last_error.restype = C.c_char_p
     L.qlp_destroy.argtypes = [C.c_void_p]
     _lib = L
@@ -196,6 +201,10 @@ class PixelLikelihood:
         """abi.QLP_NFW_QUADRATURE or abi.QLP_NFW_SURROGATE (after train_nfw_surrogate);
         threshold_arcsec <= 0 keeps the default gate (2e-5 arcsec)."""
         self._check(self.lib.qlp_set_nfw_mode(self.ctx, int(mode), float(threshold_arcsec)))
+
+    def set_nfw_tolerance(self, tol):
+        """QLens's 'integral_tolerance' for the NFW quadrature (default 1e-3)."""
+        self._check(self.lib.qlp_set_nfw_tolerance(self.ctx, float(tol)))
 
     def schedule(self):
         s = abi.qlp_schedule()
@@ -306,6 +315,23 @@ class PixelLikelihood:
             self._check(code)
         return [out[i].as_dict() for i in range(n)]
 
+    def set_fit_params(self, spec):
+        """QLens's fit parameters over the lens parameters (qlp_set_fit_params):
+        spec is a list of dicts of qlp_fit_param fields."""
+        self._fit = abi.make_fit_params(spec)
+        self._nfit = len(spec)
+        self._check(self.lib.qlp_set_fit_params(self.ctx, self._fit, len(spec)))
+
+    def fit_loglike_batch(self, fit_params):
+        """-log L of each fit vector (QLens::fitmodel_loglike_extended_source)
+        and its evaluation's result dict."""
+        x = np.ascontiguousarray(fit_params, dtype=np.float64).reshape(-1, self._nfit)
+        n = x.shape[0]
+        ll = np.zeros(n)
+        out = (abi.qlp_result * n)()
+        self._check(self.lib.qlp_fit_loglike_batch(self.ctx, _dp(x), n, _dp(ll), out))
+        return ll, [out[i].as_dict() for i in range(n)]
+
     def dump(self, n_sub, res):
         """Intermediates of the last single evaluation (parity hooks)."""
         N, M, nnz = res["n_active_pixels"], res["n_active_src"], res["L_nnz"]
@@ -409,6 +435,21 @@ def surrogate_eval(rho_phi_q, device=0):
     if code != abi.QLP_OK:
         raise QLPixError(code, L.qlp_last_error().decode())
     return t, G, B, bound
+
+
+def fit_terms(spec, fit_params):
+    """Host side of one fit vector (qlp_fit_terms): (transformed values,
+    penalised, prior + Jacobian terms).  No device needed."""
+    L = load_library()
+    fp = abi.make_fit_params(spec)
+    x = np.ascontiguousarray(fit_params, dtype=np.float64)
+    t = np.zeros(len(spec))
+    pen = C.c_int()
+    terms = C.c_double()
+    code = L.qlp_fit_terms(fp, len(spec), _dp(x), _dp(t), C.byref(pen), C.byref(terms))
+    if code != abi.QLP_OK:
+        raise QLPixError(code, L.qlp_last_error().decode())
+    return t, bool(pen.value), terms.value
 
 
 def brent_min(f, ax, bx, tol, max_iter):

@@ -249,3 +249,281 @@ class NestedSampler:
         w_live = [math.exp(-logL[i] - count / N - lnZ) / N for i in range(N)]
         return dict(lnZ=lnZ, count=count, tries=trystot, dead=dead[:count], live=(pts.copy(), logL.copy()),
                     w_dead=np.array(w_dead), w_live=np.array(w_live), best=best, search=self.state.as_dict())
+
+
+class TWalk:
+    """QLens's T-Walk MCMC (UCMC::TWalk, mcmchdr.cpp:820-1210; Christen & Fox
+    2010) over a box prior, with its proposals batched.
+
+    n_chains chains in the unit cube of the fit parameters (at least ma + 2
+    and 5).  Every iteration picks a chain t and another tt, draws u and moves
+    t by a walk (u < div/2; Z = (1/sqrt(alim) + U (sqrt(alim) - 1/sqrt(alim)))^2
+    along (a_t - a_tt) projected on a fresh random `proj`-plane, log-ratio
+    (proj - 1) log Z), a traverse (u < div; Z = -U^(1/(alimt+1)) or
+    -U^(1/(1-alimt)), log-ratio (proj - 2) log(-Z)), or a multivariate jump of
+    t (u < (1+div)/2) or of tt (otherwise) of size din x dist along the
+    Cholesky factor of the chains' covariance (AdvanceDevs::MultiDev,
+    random.h:493-522; RandomPlane::Mult / RandRot, random.h:779-840); a
+    proposal inside the cube is accepted if ans = L_new - L_t - log-ratio <= 0
+    or an exponential variate is >= ans (-log L throughout).  Every n_chains
+    iterations the Gelman-Rubin R of every parameter is updated; the run ends
+    by the reference's rule (mcmchdr.cpp:1131-1185: once every R < tol, with
+    one reset of the statistics after the first unconverged check).  The
+    defaults are QLens's call (lens.cpp:9316: div 0.9836, proj 4, din 2.4,
+    alim 2.5, alimt 6).  Random numbers come from numpy, not from QLens's
+    generator, and calcCov uses the actual number of points (the reference
+    fixes it at its first call through a static).
+
+    While a chain's proposal is rejected nothing but the bookkeeping changes,
+    so candidates are proposed K at a time, each assuming the ones before it
+    were rejected, evaluated in one batch and examined in order
+    (qlp_speculative_search); the draws after the first accepted one (or the
+    one after which the run ends) are discarded and the generator is wound
+    back to the point the one-at-a-time run reaches.  The acceptance variate
+    is drawn with the proposal; a candidate accepted with ans <= 0, whose
+    variate the reference never draws, winds the generator back to just
+    before it.  The run -- every chain state, -log L, count, R -- is the
+    one-candidate-at-a-time run's (batch=(1, 1)), which the tests check."""
+
+    def __init__(self, target, lower, upper, n_chains=0, seed=0, log_prior=None, batch=(1, 32),
+                 div=0.9836, proj=4, din=2.4, alim=2.5, alimt=6.0, tol=1.01):
+        self.t = target
+        self.lo = np.asarray(lower, dtype=np.float64)
+        self.hi = np.asarray(upper, dtype=np.float64)
+        self.ma = len(self.lo)
+        nt = max(int(n_chains), self.ma + 2, 5 + 1)
+        if nt <= proj:
+            nt = proj + 1
+        self.NT = nt
+        self.rng = np.random.default_rng(seed)
+        self.log_prior = log_prior or (lambda x: 0.0)
+        self.k_min, self.k_max = batch
+        self.div, self.proj, self.din, self.alim, self.alimt, self.tol = div, min(proj, self.ma), din, alim, alimt, tol
+        self.state = qlp_search_state()
+        self.L = load_library()
+        _bind(self.L)
+
+    # ---- -log L (+ prior term) of points of the unit cube, in a batch
+    def _x(self, u):
+        return self.lo + np.asarray(u) * (self.hi - self.lo)
+
+    def _eval_units(self, U):
+        X = np.stack([self._x(u) for u in U])
+        if isinstance(self.t, FunctionTarget):
+            nll = np.asarray(self.t.f(X), dtype=np.float64)
+        else:
+            nll = np.array([self.t.neg_loglike(r) for r in self.t.pl.eval_batch(np.stack([self.t.full(x) for x in X]))])
+        return nll + np.array([float(self.log_prior(x)) for x in X])
+
+    # ---- the move generators (draw order as the reference's)
+    def _plane(self, rng):
+        """RandRot(0, proj): proj orthonormal vectors by Gram-Schmidt of Gaussian draws."""
+        V = np.zeros((self.proj, self.ma))
+        for i in range(self.proj):
+            v = rng.standard_normal(self.ma)
+            for j in range(i):
+                v = v - np.dot(v, V[j]) * V[j]
+            V[i] = v / math.sqrt(np.dot(v, v))
+        return V
+
+    def _mult(self, rng, a, a0, Z):
+        V = self._plane(rng)
+        z = np.array([np.sum((Z - 1.0) * (a - a0) * V[i]) for i in range(self.proj)])
+        return a + z @ V
+
+    @staticmethod
+    def _cov(pts):
+        P = np.asarray(pts)
+        n = len(P)
+        return (P.T @ P) / n - np.outer(P.sum(0), P.sum(0)) / n / n
+
+    @staticmethod
+    def _indent(pts):
+        P = np.asarray(pts)
+        hi = np.maximum(1.0, P.max(0))
+        lo = np.minimum(0.0, P.min(0))
+        return np.diag((hi - lo) ** 2 / 12.0)
+
+    @staticmethod
+    def _chol(C):
+        n = len(C)
+        L = np.zeros((n, n))
+        for i in range(n):
+            for j in range(i, n):
+                s = C[i, j] - sum(L[i, k] * L[j, k] for k in range(i - 1, -1, -1))
+                if i == j:
+                    if s <= 0.0:
+                        return None
+                    L[i, i] = math.sqrt(s)
+                else:
+                    L[j, i] = s / L[i, i]
+        return L
+
+    def _multi(self, rng, a0, pts):
+        L = self._chol(self._cov(pts))
+        if L is None:
+            L = self._chol(self._indent(pts))
+        vec = rng.standard_normal(self.ma)
+        norm = math.sqrt(np.dot(vec, vec))
+        if rng.random() < 0.33:
+            dist = rng.standard_exponential()
+        else:
+            d = 0.0
+            for _ in range(2):
+                g = rng.standard_normal()
+                d += g * g
+            dist = math.sqrt(d / 2.0)
+        return self.din * dist * (L @ vec) / norm + a0
+
+    def _propose(self, rng, A):
+        """One iteration's draws: (t, proposal, log-ratio)."""
+        NT = self.NT
+        t = int(NT * rng.random())
+        tt = int((NT - 1) * rng.random())
+        if tt >= t:
+            tt += 1
+        ran = rng.random()
+        b0, b1, b2 = self.div / 2.0, self.div, (1.0 + self.div) / 2.0
+        if ran < b0:
+            sa = math.sqrt(self.alim)
+            Z = (1.0 / sa + rng.random() * (sa - 1.0 / sa)) ** 2
+            return t, self._mult(rng, A[t], A[tt], Z), (self.proj - 1.0) * math.log(Z)
+        if ran < b1:
+            if rng.random() < (self.alimt - 1.0) / (2.0 * self.alimt):
+                Z = -rng.random() ** (1.0 / (self.alimt + 1.0))
+            else:
+                Z = -rng.random() ** (1.0 / (1.0 - self.alimt))
+            return t, self._mult(rng, A[t], A[tt], Z), (self.proj - 2.0) * math.log(-Z)
+        others = [A[i] for i in range(NT) if i != tt]
+        if ran < b2:
+            return t, self._multi(rng, A[t], list(A) + others), 0.0
+        return t, self._multi(rng, A[tt], others), 0.0
+
+    @staticmethod
+    def _outside(u):
+        return bool(np.any((u < 0.0) | (u > 1.0)))
+
+    def run(self, max_iter=100000):
+        NT, ma = self.NT, self.ma
+        rng = self.rng
+        A = [rng.random(ma) for _ in range(NT)]
+        ll = list(self._eval_units(A))
+        mult, count = [1] * NT, [1] * NT
+        total, ttotal, nlength = 1, 0, 1
+        covT = np.zeros((NT, ma)); avgT = np.zeros((NT, ma))
+        W = np.zeros(ma); avgTot = np.zeros(ma)
+        best = (min(ll), A[int(np.argmin(ll))].copy())
+        chain = []                                 # accepted points: (chain t, multiplicity, x, -log L)
+        R_hist = []
+        run = {"stop": False}
+
+        def bookkeeping():
+            """After each iteration: the multiplicities, the counter and, every
+            NT iterations, the R statistics and the stopping rule."""
+            nonlocal total, ttotal, nlength, covT, avgT, W, avgTot, best
+            for i in range(NT):
+                mult[i] += 1
+            total += 1
+            for i in range(NT):
+                if ll[i] < best[0]:
+                    best = (ll[i], A[i].copy())
+            if total % NT != 0:
+                return False
+            for k in range(NT):
+                for i in range(ma):
+                    davg = (A[k][i] - avgT[k][i]) / (ttotal + 1.0)
+                    dcov = ttotal * davg * davg - covT[k][i] / (ttotal + 1.0)
+                    avgTot[i] += davg / NT
+                    covT[k][i] += dcov
+                    avgT[k][i] += davg
+                    W[i] += dcov / NT
+            ttotal += 1
+            cont = False
+            Rmax = -1e30
+            for i in range(ma):
+                Bn = sum((avgT[s][i] - avgTot[i]) ** 2 for s in range(NT)) / (NT - 1.0)
+                R = 1.0 + (NT + 1.0) * Bn / W[i] / NT if W[i] != 0 else float("inf")
+                Rmax = max(Rmax, R)
+                if W[i] <= 0.0 or R >= self.tol or R <= 0.0:
+                    if nlength == 0:
+                        cont = True
+                    else:
+                        cont = False
+                        nlength -= 1
+                        covT = np.zeros((NT, ma)); avgT = np.zeros((NT, ma))
+                        W = np.zeros(ma); avgTot = np.zeros(ma)
+                        ttotal += 1
+            R_hist.append(Rmax)
+            return not cont
+
+        it = 0
+        while not run["stop"] and it < max_iter:
+            cand, before, after = {}, {}, {}
+
+            def propose(_u, i, lens_params, regparam):
+                t, u, logZ = self._propose(rng, A)
+                before[i] = rng.bit_generator.state
+                inside = not self._outside(u)
+                e = rng.standard_exponential() if inside else None     # the acceptance variate
+                after[i] = rng.bit_generator.state
+                cand[i] = (t, u, logZ, inside, e)
+                x = self._x(u if inside else A[t])
+                full = self.t.full(x)
+                C.memmove(lens_params, full.ctypes.data, full.nbytes)
+                regparam[0] = 0.0
+                return 0
+
+            def accept(_u, i, res):
+                nonlocal it
+                t, u, logZ, inside, e = cand[i]
+                took = False
+                used_e = False
+                if inside:
+                    r = res.contents.as_dict()
+                    nll = self.t.neg_loglike(r) + float(self.log_prior(self._x(u)))
+                    ans = nll - ll[t] - logZ
+                    used_e = ans > 0.0
+                    if ans <= 0.0 or e >= ans:
+                        chain.append((t, mult[t], self._x(u), nll))
+                        A[t] = u
+                        ll[t] = nll
+                        mult[t] = 0
+                        count[t] += 1
+                        took = True
+                cand["used_e"] = used_e
+                it += 1
+                stop = bookkeeping() or it >= max_iter
+                if stop:
+                    run["stop"] = True
+                cand["last"] = i
+                return 1 if (took or stop) else 0
+
+            def rewind(_u, nxt):
+                rng.bit_generator.state = after[nxt - 1] if cand["used_e"] else before[nxt - 1]
+
+            keep = (PROPOSE_FN(propose), ACCEPT_FN(accept), REWIND_FN(rewind))
+            idx = C.c_long(-1)
+            if isinstance(self.t, FunctionTarget):
+                def ev(_u, params, lam, n, out):
+                    X = np.ctypeslib.as_array(params, shape=(n, self.t.dim)).copy()
+                    vals = self.t.f(X)
+                    for k in range(n):
+                        out[k] = abi.qlp_result()
+                        out[k].m2logev = 2.0 * float(vals[k])
+                        out[k].status = 0
+                    return 0
+                evf = BATCH_EVAL_FN(ev)
+                code = self.L.qlp_speculative_search_fn(evf, None, self.t.dim, *keep, None, self.k_min, self.k_max,
+                                                        max_iter + 1, C.byref(self.state), C.byref(idx))
+            else:
+                code = self.L.qlp_speculative_search(self.t.pl.ctx, *keep, None, self.k_min, self.k_max,
+                                                     max_iter + 1, C.byref(self.state), C.byref(idx))
+            if code != abi.QLP_OK:
+                raise QLPixError(code, self.L.qlp_last_error().decode())
+            if idx.value < 0:
+                break
+            # the generator where the one-at-a-time run has it (rewind is not
+            # called when the accepted candidate was the last one proposed)
+            rng.bit_generator.state = after[idx.value] if cand["used_e"] else before[idx.value]
+        return dict(chains=[a.copy() for a in A], loglike=list(ll), count=list(count), mult=list(mult),
+                    iterations=it, chain=chain, R=R_hist, best=best, search=self.state.as_dict(), n_chains=NT)

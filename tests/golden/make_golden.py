@@ -2,7 +2,7 @@
 
 Run in a container that has the reference sources (read-only) and g++:
 
-    make -f oracle/Makefile.ref -j8 REF=/root/reference
+    make -f oracle/Makefile.ref -j8          # REF=<reference sources> to override
     python tests/golden/make_golden.py
 
 For every case below this writes a QLens script, runs oracle/_ref/qlens_harness
@@ -277,7 +277,9 @@ assert all("emask_n_neighbors" in CASES[k]["script"] for k in ("osb_tiny_sie", "
 # the threshold).  hst_fits: the FITS files the reference ships with its pixel
 # fitting demo (81x81 at 0.049", 37x37 PSF, mask), in Cartesian mode.
 FITS_FIXTURES = os.path.join(HERE, "fits")
-REF_DIR = "/root/reference"
+# where oracle/Makefile.ref reads the reference sources (its REF)
+REF_DIR = subprocess.run(["make", "-s", "-f", os.path.join(REPO, "oracle", "Makefile.ref"), "ref-dir"],
+                         capture_output=True, text=True).stdout.strip()
 CASES["fits_synth"] = dict(
     script="""emode 1
 sbmap loadimg image.fits -hdu=2
@@ -325,11 +327,105 @@ inversion_method dense
     dense_rows=64, full_F=True, harness="fits",
     files=[os.path.join(REF_DIR, f) for f in ("sim_hst_image.fits", "mask.fits", "hst_psf.fits")])
 
-ARRAYS_F64 = ["zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
+# Cases at the sizes of the benchmarked workloads.  Their PSFs are Airy-like
+# kernels (the workloads' own), given to the reference as FITS files through
+# its loader ('sbmap loadpsf', run by the FITS harness) with a threshold low
+# enough to keep the whole kernel.  Their largest arrays are slimmed before
+# packing (see SLIM below).
+#
+# cfg2_draw: one draw from the 200x200 power-law workload's prior box (0.04"
+# pixels, annulus 0.5"-2.5", 4x4 split, 21x21 Airy-like PSF, 64x64 source,
+# sigma 0.01, lambda 10).
+CASES["cfg2_draw"] = dict(
+    script="""random_seed 21
+grid -4 4 -4 4
+img_npixels 200 200
+emode 1
+psf_threshold 1e-9
+sbmap loadpsf psf.fits
+lens sple 1.31 1.08 0 0.72 47 0 0 shear=0.06 112
+source sersic 1 0.2 1.5 0.75 20 0.04 -0.02
+bg_pixel_noise 0.01
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0.5 2.5
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 64 64
+fit regularization curvature
+regparam 10
+imgpixel_nsplit 4
+split_imgpixels on
+inversion_method dense
+""",
+    lenses=[dict(type="sple", params=[1.31, 1.08, 0.0, 0.72, 47.0, 0.0, 0.0]),
+            dict(type="shear", params=[0.06, 112.0, 0.0, 0.0])],
+    dense_rows=16, full_F=False, harness="fits", psf_airy=(21, 0.04, 0.1), slim=True)
+# cfg5_m200: the two-plane workload at its sampling (0.03" pixels, 4x4 split,
+# 31x31 Airy-like PSF) on a smaller 160x160 image (annulus 0.3"-2.3"), with the
+# z = 0.8 subhalo given by its mass and concentration (QLens 'pmode=1':
+# NFW::set_ks_rs_from_m200_c200, models.cpp:968-976) -- the library's
+# QLP_LENS_NFW_M200_C with the cosmology the reference used for that lens.
+CASES["cfg5_m200"] = dict(
+    script="""random_seed 23
+zsrc 2
+zlens 0.5
+grid -2.4 2.4 -2.4 2.4
+img_npixels 160 160
+emode 1
+psf_threshold 1e-9
+sbmap loadpsf psf.fits
+lens sple 1.2 1 0 0.8 30 0 0 shear=0.05 10
+lens nfw 5e9 12 0.7 -50 0.85 0.8 z=0.8 pmode=1
+source sersic 1 0.2 1.5 0.75 20 0.04 -0.02
+bg_pixel_noise 0.01
+sbmap plotimg -pnoise -mkdata -nocc
+source clear
+sbmap generate_uniform_noisemap
+sbmap unset_all_pixels
+sbmap set_data_annulus 0 0 0.3 2.3
+fit source_mode cartesian
+auto_srcgrid on
+auto_src_npixels off
+src_npixels 40 40
+fit regularization curvature
+regparam 10
+imgpixel_nsplit 4
+split_imgpixels on
+inversion_method dense
+""",
+    lenses=[dict(type="sple", params=[1.2, 1.0, 0.0, 0.8, 30.0, 0.0, 0.0], plane=0),
+            dict(type="shear", params=[0.05, 10.0, 0.0, 0.0], plane=0),
+            dict(type="nfw_m200_c", params=[5e9, 12.0, 0.7, -50.0, 0.85, 0.8], plane=1)],
+    dense_rows=16, full_F=False, harness="fits", psf_airy=(31, 0.03, 0.08), slim=True)
+
+# Slimmed cases keep every input, the active set, the CSR row pointers, the L
+# column indices (as int16: M <= 4096), the source-grid corners and the
+# M- and N-sized vectors in full.  The sub-pixel source points and the L values
+# (about 3 and 5 MB at cfg2's size) are replaced by their SHA-256 digests (exact
+# comparisons) plus every SLIM_STRIDE-th element (tolerance comparisons).
+SLIM_STRIDE = 61
+SLIM_HASHED = ["srcpt_x", "srcpt_y", "L_value"]
+
+ARRAYS_F64 = ["lens_cosmo", "zfactors", "betafactors", "xvals", "yvals", "data", "covinv", "psf", "srcpt_x", "srcpt_y", "src_corner_x",
               "src_corner_y", "L_value", "R_value", "Lpsf_rows", "Lpsf_colsum", "Lpsf_rowsum", "D",
               "F_diag", "F_packed_upper", "s", "model", "osb_sb"]
 ARRAYS_I32 = ["lens_plane", "masked_pixels", "active_index", "active_pixels", "L_rowptr", "L_index", "R_index"]
 ARRAYS_U8 = ["mask", "emask", "osb_maps"]
+
+
+def write_airy_psf(path, n, pixel, fwhm):
+    """The workloads' Airy-like PSF (qlens_gb300.synthetic.airy_psf) as a
+    64-bit FITS image, for the reference's own PSF loader."""
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, HERE)
+    from make_fits import hdu_bytes
+    from qlens_gb300.synthetic import airy_psf
+    with open(path, "wb") as f:
+        f.write(hdu_bytes(airy_psf(n, pixel, fwhm), -64, True))
 
 
 def run_case(name, case, outdir):
@@ -340,6 +436,8 @@ def run_case(name, case, outdir):
             f.write(case["script"])
         for src in case.get("files", []):
             shutil.copy(src, os.path.join(tmp, os.path.basename(src)))
+        if case.get("psf_airy"):
+            write_airy_psf(os.path.join(tmp, "psf.fits"), *case["psf_airy"])
         dump = os.path.join(tmp, "dump")
         os.makedirs(dump)
         env = dict(os.environ, OMP_NUM_THREADS="4")
@@ -360,7 +458,24 @@ def run_case(name, case, outdir):
             for line in f:
                 k, v = line.split()
                 scalars[k] = float(v)
-        meta = dict(name=name, lenses=case["lenses"], script=case["script"], scalars=scalars)
+        lenses = [dict(l) for l in case["lenses"]]
+        if "lens_cosmo" in out:
+            lc = out["lens_cosmo"].reshape(len(lenses), 5)
+            for k, l in enumerate(lenses):
+                if l["type"] in ("nfw_m200_c", "nfw_m200_rs"):
+                    l["cosmo"] = [float(v) for v in lc[k, :3]]
+        meta = dict(name=name, lenses=lenses, script=case["script"], scalars=scalars)
+        if case.get("slim"):
+            import hashlib
+            slim = {"stride": SLIM_STRIDE, "sha256": {}}
+            for k in SLIM_HASHED:
+                a = np.ascontiguousarray(out.pop(k))
+                slim["sha256"][k] = hashlib.sha256(a.tobytes()).hexdigest()
+                out[k + "_sub"] = a[::SLIM_STRIDE].copy()
+            out.pop("F_packed_upper", None)
+            assert int(out["L_index"].max()) < 32768
+            out["L_index"] = out["L_index"].astype(np.int16)
+            meta["slim"] = slim
         out["meta_json"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
         np.savez_compressed(os.path.join(outdir, name + ".npz"), **out)
         print("%-10s -2logev=%.10f chi2=%.6f logdetF=%.6f logdetR=%.6f npix=%d nsrc=%d" % (
@@ -372,7 +487,7 @@ def run_case(name, case, outdir):
 
 def main(argv):
     if not os.path.exists(HARNESS):
-        sys.exit("build the harness first: make -f oracle/Makefile.ref -j8 REF=/root/reference")
+        sys.exit("build the harness first: make -f oracle/Makefile.ref -j8")
     names = argv[1:] or list(CASES)
     for n in names:
         run_case(n, CASES[n], HERE)

@@ -7,7 +7,10 @@ import numpy as np
 from qlens_gb300 import abi
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["tiny_sie", "fixed_grid", "powerlaw", "nfw", "twoplane", "cfg1", "fits_synth", "hst_fits"]
+CASES = ["tiny_sie", "fixed_grid", "powerlaw", "nfw", "twoplane", "cfg1", "fits_synth", "hst_fits",
+         "cfg2_draw", "cfg5_m200"]
+# cases at the benchmarked workloads' sizes (slimmed fixtures, see Golden.exact)
+LARGE_CASES = ["cfg2_draw", "cfg5_m200"]
 REGOPT_CASES = ["regopt_tiny_sie", "regopt_powerlaw"]
 
 
@@ -19,6 +22,9 @@ class Golden:
         self.meta = json.loads(bytes(self.arr.pop("meta_json")).decode())
         self.sc = self.meta["scalars"]
         self.lenses = self.meta["lenses"]
+        self.slim = self.meta.get("slim")
+        if "L_index" in self.arr:
+            self.arr["L_index"] = self.arr["L_index"].astype(np.int32)
         nx, ny = int(self.sc["nx"]), int(self.sc["ny"])
         self.nx, self.ny = nx, ny
         covinv = self.arr["covinv"] if int(self.sc["use_noise_map"]) else None
@@ -39,6 +45,29 @@ class Golden:
                 o.auto_sourcegrid = 0
                 o.xmin, o.xmax, o.ymin, o.ymax = map(float, w[1:])
         self.opts = o
+
+    @property
+    def n_sub(self):
+        """Sub-pixels (ray-traced points) of the masked pixels."""
+        return int(self.arr["masked_pixels"].size) * int(self.sc["nsplit"]) ** 2
+
+    def exact(self, name, a):
+        """Bit-for-bit equality of an array with the reference's: by value, or
+        for the slimmed arrays of the large cases by SHA-256 of the bytes."""
+        if self.slim and name in self.slim["sha256"]:
+            import hashlib
+            ref_dtype = np.float64
+            b = np.ascontiguousarray(np.asarray(a, dtype=ref_dtype)).tobytes()
+            return hashlib.sha256(b).hexdigest() == self.slim["sha256"][name]
+        return np.array_equal(a, self.arr[name])
+
+    def sample(self, name, a=None):
+        """(reference values, the same elements of a): everything, or every
+        stride-th element for the slimmed arrays of the large cases."""
+        if self.slim and name in self.slim["sha256"]:
+            ref = self.arr[name + "_sub"]
+            return ref, (None if a is None else np.asarray(a)[::self.slim["stride"]])
+        return self.arr[name], a
 
     @property
     def regopt(self):

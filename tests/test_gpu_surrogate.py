@@ -106,13 +106,13 @@ def test_gated_error_within_threshold(trained):
 def _nfw_q_index(lenses):
     o = 0
     for l in lenses:
-        if l["type"] == "nfw":
+        if l["type"].startswith("nfw"):
             return o + 2
         o += len(l["params"])
     raise ValueError("no NFW lens")
 
 
-@pytest.mark.parametrize("name", ["nfw", "twoplane"])
+@pytest.mark.parametrize("name", ["nfw", "twoplane", "cfg5_m200"])
 def test_likelihood_with_surrogate(trained, name):
     from qlens_gb300 import PixelLikelihood, abi
     g = Golden(name)
@@ -149,7 +149,7 @@ def test_surrogate_gain(trained):
     without it, single evaluations launched kernel by kernel with CUDA events
     around the stage, at the same source points to within the gate."""
     from qlens_gb300 import PixelLikelihood, abi, synthetic
-    wl = synthetic.cfg5()
+    wl = synthetic.cfg5_fixed()
     kw = dict(covinv=None, bg_noise=wl.noise, nsplit=wl.nsplit, src_npixels=wl.src_npixels, regparam=wl.regparam)
     pl = PixelLikelihood(wl.xvals, wl.yvals, wl.data, wl.mask, wl.psf, precision=abi.QLP_MIXED, **kw)
     pl.set_lens_model(wl.lenses, wl.zfac, wl.beta)
