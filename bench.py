@@ -261,6 +261,18 @@ def run_reference(args, rank, world):
     return 0
 
 
+def accuracy_of(fast, plain, has_nfw):
+    """|delta log L| = |delta(-2 log evidence)| / 2 of the timed path against
+    the plain FP64 path on the same vectors."""
+    d = sorted(abs(a["m2logev"] - b["m2logev"]) / 2.0 for a, b in zip(fast, plain)
+               if a["status"] == 0 and b["status"] == 0)
+    if not d:
+        return None
+    return {"max_abs_dlogL": d[-1], "median_abs_dlogL": float(np.median(d)),
+            "p90_abs_dlogL": float(np.quantile(d, 0.9)), "frac_within_bound": float(np.mean(np.array(d) < 0.1)),
+            "n_draws": len(d), "vs": "plain FP64 path" + (" with NFW quadrature" if has_nfw else ""), "bound": 0.1}
+
+
 def plain_fp64_arm(wl, params, inst, n, slots):
     """The plain FP64 path (FP64 SYRK, Cholesky and solves; the NFW deflection
     by quadrature) on the first n vectors of a timed batch: one warm-up batch
@@ -449,22 +461,33 @@ def main():
         write_trace(pl, run_step, args.warmup, args.trace)
 
     # the plain FP64 path on the first vectors of the first timed batch: its
-    # throughput and the largest |delta log L| of the timed path against it
+    # throughput, the ratio, and |delta log L| of the timed path against it
     plain = None
     accuracy = None
     if args.plain_sample > 0 and precision == "mixed":
         kfirst = args.warmup
         n = min(args.plain_sample, B)
-        ids, sizes, lam = insts[kfirst]
         pv, pres = plain_fp64_arm(wl, batches[kfirst], insts[kfirst], n, slots=min(n, 8))
-        ok = [(a, b) for a, b in zip(results[:n], pres) if a["status"] == 0 and b["status"] == 0]
-        d = [abs(a["m2logev"] - b["m2logev"]) / 2.0 for a, b in ok]
         plain = {"value": pv, "unit": UNIT, "sample": "the first %d vectors of the first timed batch" % n,
                  "path": "FP64 SYRK, Cholesky and solves" + ("; NFW deflection by quadrature" if has_nfw else ""),
                  "slots": min(n, 8)}
-        accuracy = {"max_abs_dlogL": max(d) if d else None, "mean_abs_dlogL": float(np.mean(d)) if d else None,
-                    "n_draws": len(d), "vs": "plain FP64 path" + (" with NFW quadrature" if has_nfw else ""),
-                    "bound": 0.1}
+        accuracy = accuracy_of(results[:n], pres, has_nfw)
+
+    # a second batch from the whole prior box (where the vectors above come
+    # from a narrower region): its throughput and accuracy, untimed for the headline
+    prior = None
+    if wl.draw_prior is not None and precision == "mixed" and args.plain_sample > 0:
+        rngp = np.random.default_rng(4242 + rank)
+        Pp = wl.draw_prior(rngp, B)
+        ip = wl.draw_instances(rngp, B) if uneven else (None, None, None)
+        pl.eval_batch(Pp, regparams=ip[2], mask_ids=ip[0], src_sizes=ip[1])        # graphs already captured
+        rp = pl.eval_batch(Pp, regparams=ip[2], mask_ids=ip[0], src_sizes=ip[1])
+        pv_ms = pl.last_device_ms()
+        n = min(args.plain_sample, B)
+        _pv, pres = plain_fp64_arm(wl, Pp, ip, n, slots=min(n, 8))
+        prior = {"value": B / (pv_ms / 1e3), "unit": UNIT, "batch": B,
+                 "accuracy": accuracy_of(rp[:n], pres, has_nfw),
+                 "median_chi2_per_pixel": float(np.median([r["chisq0"] / r["n_active_pixels"] for r in pres]))}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -495,6 +518,8 @@ def main():
             "vs_plain_fp64": (value / plain["value"]) if plain else None,
             "plain_fp64": plain,
             "accuracy": accuracy,
+            "draws": wl.draws_note,
+            "prior_draws": prior,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),

@@ -138,6 +138,8 @@ typedef struct {
     int regopt_evals;     /* -2 log(evidence) evaluations of the lambda optimisation (0 = off) */
     double outside_sb_penalty;  /* the outside-surface-brightness prior's penalty, included in
                                    m2logev (0 when the prior is off or not triggered) */
+    int nfw_exact_rays;   /* surrogate rays traced again by the quadrature because their error bound
+                             reached a cell edge, a cell's centre line or the grid's extremes */
 } qlp_result;
 
 /* Training of the NFW deflection surrogate (qlp_nfw_surrogate_train). */

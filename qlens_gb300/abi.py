@@ -72,7 +72,8 @@ class qlp_result(C.Structure):
                 ("logdet_R", C.c_double), ("Es_times_two", C.c_double), ("regterms", C.c_double),
                 ("n_active_pixels", C.c_int), ("n_active_src", C.c_int), ("L_nnz", C.c_longlong),
                 ("status", C.c_int), ("refine_iters", C.c_int), ("nfw_fallbacks", C.c_int),
-                ("regparam", C.c_double), ("regopt_evals", C.c_int), ("outside_sb_penalty", C.c_double)]
+                ("regparam", C.c_double), ("regopt_evals", C.c_int), ("outside_sb_penalty", C.c_double),
+                ("nfw_exact_rays", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

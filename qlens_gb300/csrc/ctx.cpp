@@ -47,7 +47,7 @@ static void free_work(Work& w)
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
                     w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep,
-                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart, w.lnz};
+                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart, w.lnz, w.sur_eps};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
@@ -109,6 +109,7 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     CK(dalloc(&w.linv, (size_t)Mc * 64), "alloc");
     CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc"); CK(dalloc(&w.ep, 1), "alloc");
     CK(dalloc(&w.fb_ray, n_sub), "alloc"); CK(dalloc(&w.fb_xy, 2 * n_sub), "alloc"); CK(dalloc(&w.fb_count, 1), "alloc");
+    CK(dalloc(&w.sur_eps, n_sub), "alloc");
     s.M_cap = Mc;
     s.N_cap = n_mask;
     s.npix_pad = (c->nx + 2 * (c->sd.pnx / 2)) * (c->ny + 2 * (c->sd.pny / 2));
@@ -328,6 +329,17 @@ static int run_pipeline(qlp_ctx* c, Slot& slot, const StaticData& sd_in, const S
     }
     if (ev) cudaEventRecord(ev[1], st);
     launch_grid(sd, so, w, st);
+    if (c->nfw_mode == QLP_NFW_SURROGATE && model_has_nfw(c)) {
+        // rays whose surrogate error could flip a grid decision are traced
+        // again exactly: first those that could set the grid's extremes (and
+        // the grid is laid out again), then those near a cell's lines
+        double zmax = 0;
+        for (int p = 0; p < c->planes.n_planes; p++) zmax = std::max(zmax, std::fabs(c->planes.zfac[p]));
+        const double eps_g = 2.0 * c->nfw_threshold * zmax + 1e-12;
+        launch_surrogate_exact(sd, so, w, eps_g, 0, st);
+        launch_grid(sd, so, w, st);
+        launch_surrogate_exact(sd, so, w, eps_g, 1, st);
+    }
     launch_locate(sd, so, w, st);
     launch_compact(sd, so, w, st);
     launch_build_L(sd, so, w, st);
@@ -483,6 +495,7 @@ static void fill_result(const EvalOut& o, qlp_result* out)
     out->status = o.status;
     out->refine_iters = o.refine_iters;
     out->nfw_fallbacks = o.pad;
+    out->nfw_exact_rays = o.n_exact;
     out->outside_sb_penalty = o.osb_penalty;
 }
 

@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(1024) k_grid(StaticData sd_, SrcOpts so_, int 
             ymn = fmin(ymn, red[2][k]); ymx = fmax(ymx, red[3][k]);
         }
         double gxmin, gxmax, gymin, gymax;
+        gs->ext[0] = xmn; gs->ext[1] = xmx; gs->ext[2] = ymn; gs->ext[3] = ymx;
         if (so.auto_grid) {
             gxmin = 1e30; gxmax = -1e30; gymin = 1e30; gymax = -1e30;
             if (xmn != DBL_MAX) gxmin = (xmn > so.lxmin) ? xmn : so.lxmin;
@@ -389,6 +390,8 @@ void launch_compact(const StaticData& sd, const SrcOpts& so, Work& w, cudaStream
 // i.e. exactly the row of convert_Lmatrix_to_dense, pixelgrid.cpp:13734-13739),
 // which the PSF kernel gathers from.
 // ---------------------------------------------------------------------------
+#define BUILD_L_MAXD 192      // entries of one row merged in local arrays (3 per sub-pixel, up to 8x8 split)
+
 __global__ void __launch_bounds__(128) k_build_L(StaticData sd_, const int* __restrict__ rowidx,
                                                  const int* __restrict__ rowptr, const int* __restrict__ cell3,
                                                  const double* __restrict__ w3, const int* __restrict__ active_index,
@@ -398,6 +401,44 @@ __global__ void __launch_bounds__(128) k_build_L(StaticData sd_, const int* __re
 {
     const StaticData sd = eval_shape(sd_);
     const int nsub = sd.nsub;
+    if (3 * nsub <= BUILD_L_MAXD) {
+        // one pass: each entry is written to the CSR row and merged at once
+        // into the row's distinct cells, kept in this thread's local arrays
+        // (a search over the distinct cells so far, not over all entries);
+        // a cell's sum starts from 0.0 and adds its entries in CSR order, and
+        // the distinct cells keep their first-occurrence order
+        int di[BUILD_L_MAXD];
+        double dv[BUILD_L_MAXD];
+        for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
+            const int r = rowidx[m];
+            if (r < 0) continue;
+            const int e0 = rowptr[r];
+            int e = e0, nc = 0;
+            for (int k = 0; k < nsub; k++) {
+                const int t = m * nsub + k;
+                const int c0 = cell3[3 * t];
+                if (c0 < 0) continue;
+                #pragma unroll
+                for (int u = 0; u < 3; u++) {
+                    const int idx = active_index[u == 0 ? c0 : cell3[3 * t + u]];
+                    const double val = w3[3 * t + u];
+                    Lidx[e] = idx;
+                    Lval[e] = val;
+                    e++;
+                    int j = 0;
+                    while (j < nc && di[j] != idx) j++;
+                    if (j == nc) { di[nc] = idx; dv[nc] = 0.0 + val; nc++; }
+                    else dv[j] += val;
+                }
+            }
+            for (int j = 0; j < nc; j++) {
+                cidx[e0 + j] = di[j];
+                cval[e0 + j] = dv[j];
+            }
+            ccnt[r] = nc;
+        }
+        return;
+    }
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
         const int r = rowidx[m];
         if (r < 0) continue;

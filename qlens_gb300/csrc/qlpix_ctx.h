@@ -166,4 +166,6 @@ int surrogate_grad_check(int device, const float* params, const float* x, const 
                          float* grad);
 int surrogate_eval(int device, const double* rpq, int n, double* t_net, double* G_quad, double* B, double* bound);
 int launch_raytrace_sur(const StaticData& sd, Work& w, double thresh, int defer_lens, cudaStream_t st);
+int launch_surrogate_exact(const StaticData& sd, const SrcOpts& so, Work& w, double eps_g, int step,
+                           cudaStream_t st);
 }  // namespace qlpix

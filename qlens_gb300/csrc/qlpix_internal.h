@@ -55,6 +55,8 @@ struct EvalParams {
 // Source-grid state computed on the device each evaluation.
 struct GridState {
     double xmin, xmax, ymin, ymax;    // bounds after auto-sizing
+    double ext[4];                    // the extremes of the per-pixel mean source points they came from
+                                      // (x min, x max, y min, y max; before the clamp and widening)
     int snx, sny;                     // cells
     int M;                            // active source cells
     int N;                            // active image pixels
@@ -70,6 +72,7 @@ struct EvalOut {
                                        // pixels + regularisation terms + log det F
     int n_active_pixels, n_active_src, L_nnz, status, refine_iters;
     int pad;                           // rays that took the NFW quadrature instead of the surrogate
+    int n_exact;                       // surrogate rays traced again exactly near a grid decision
     double osb_penalty;                // the outside-surface-brightness prior's penalty (0 when off)
 };
 
@@ -183,6 +186,7 @@ struct Work {
     EvalParams* ep;                    // this slot's per-evaluation parameters
     // rays whose NFW deflection the surrogate hands to the quadrature (n_sub capacity)
     int* fb_ray;  double* fb_xy;  int* fb_count;
+    float* sur_eps;                    // n_sub: bound on each ray's source-point error on the surrogate path
     double* F0;                        // plain path, lambda optimisation: L'^T C^-1 L' before lambda R
 };
 

@@ -122,6 +122,26 @@ __device__ __forceinline__ SurIn sur_inputs(double X, double Y, double q)
     return s;
 }
 
+// The same inputs for the ray shooting, with the network's features (log R,
+// the polar angle) in FP32 -- the network reads them in FP32 anyway -- and
+// the baseline B in FP64 (its small-radius form cancels).
+__device__ __forceinline__ SurIn sur_inputs_ray(double X, double Y, double q)
+{
+    SurIn s;
+    const double ax = fabs(X), ay = fabs(Y);
+    const float axf = (float)ax, ayf = (float)ay;
+    const float rho = 0.5f * __logf(__fmaf_rn(axf, axf, ayf * ayf));
+    const float phi = atan2f(ayf, axf);
+    const float hr = (float)(0.5 * (SUR_RHO_HI - SUR_RHO_LO)), mr = (float)(0.5 * (SUR_RHO_HI + SUR_RHO_LO));
+    const double hq = 0.5 * (1.0 - SUR_Q_LO), mq = 0.5 * (1.0 + SUR_Q_LO);
+    s.f0 = fminf(fmaxf((rho - mr) / hr, -2.0f), 2.0f);
+    s.f1 = phi * (float)(4.0 / M_PI) - 1.0f;
+    s.f2 = (float)fmin(fmax((q - mq) / hq, -2.0), 2.0);
+    s.bin = sur_cell((double)rho, (double)phi, q);
+    s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, q * ax * ax + ay * ay / q);
+    return s;
+}
+
 __device__ __forceinline__ uint64_t sur_hash(uint64_t x)
 {
     x += 0x9E3779B97F4A7C15ull;
@@ -622,7 +642,8 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
                                                                  const float* __restrict__ bound, double thresh,
                                                                  int defer_lens, int* __restrict__ fb_count,
                                                                  int* __restrict__ fb_ray, double* __restrict__ fb_xy,
-                                                                 GridState* gs, EvalOut* out)
+                                                                 float* __restrict__ sur_eps, GridState* gs,
+                                                                 EvalOut* out)
 {
     const StaticData sd = eval_shape(sd_);
     extern __shared__ unsigned char smem_raw[];
@@ -660,6 +681,10 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
         }
         double defx = 0, defy = 0;
         double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
+        // bound on this ray's source-point error against the plain path:
+        // rounding (a deferred fallback is subtracted in another order) plus,
+        // per surrogate deflection, twice its plane factor times its bound
+        double eps = 1e-12;
         for (int p = 0; p < lm.n_planes; p++) {
             dsx[p] = 0; dsy[p] = 0;
             if (lm.zfac[p] == 0.0) continue;
@@ -681,7 +706,7 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
                         y = -x * L.sintheta + y * L.costheta;
                         x = xp;
                     }
-                    const SurIn in = sur_inputs(x / L.rs, y / L.rs, L.q);
+                    const SurIn in = sur_inputs_ray(x / L.rs, y / L.rs, L.q);
                     const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
                     // before the network: |alpha| ~ ks B |(x, y)| (G is within a few
                     // tens of percent of B), so a group none of whose rays can pass
@@ -693,11 +718,13 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
                     if (wg_any(S.wg, maybe)) {
                         float t0, t1;
                         sur_mlp_wg(S, in.f0, in.f1, in.f2, t0, t1, ok);
-                        const double G0 = in.B * exp((1.0 - L.q) * t0), G1 = in.B * exp((1.0 - L.q) * t1);
+                        const float oq = (float)(1.0 - L.q);
+                        const double G0 = in.B * (double)expf(oq * t0), G1 = in.B * (double)expf(oq * t1);
                         bx = x * L.ks * G0;
                         by = y * L.ks * G1;
                         const double mag = sqrt(bx * bx + by * by);
                         use = ok && !centre && in.bin >= 0 && mag * (double)bound[in.bin] <= thresh;
+                        if (use) eps += 2.0 * fabs(lm.zfac[p]) * mag * (double)bound[in.bin];
                     }
                     if (!use && valid) {
                         fb++;
@@ -730,6 +757,7 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
         if (valid) {
             spx[t] = px - defx;
             spy[t] = py - defy;
+            sur_eps[t] = (float)eps;
         }
     }
     if (fb) atomicAdd(&n_fb, fb);
@@ -738,6 +766,165 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
         if (n_fb) atomicAdd(&out->pad, n_fb);
         if (!ok) atomicExch(&gs->status, QLP_ERR_TIMEOUT);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Exact rays where the grid decides.  QLens's likelihood is not continuous in
+// the source points: which cells a sub-pixel maps to changes at cell edges
+// and at the lines through cell centres (SourcePixelGrid::
+// assign_source_mapping_flags_interpolate, pixelgrid.cpp:2343-2432), and
+// the grid itself is laid out from the extremes of the per-pixel mean source
+// points (find_optimal_sourcegrid, pixelgrid.cpp:10998-11080).  A ray moved
+// by the surrogate's error across such a line changes L by a finite step.
+// So every ray whose error bound (sur_eps) reaches a decision is traced again
+// with the plain path's own code (find_sourcept with the quadrature,
+// lens_device.cuh; this file is compiled with --fmad=false like
+// raytrace.cu), which gives the plain path's bits:
+//   k_sur_exact_extremes  after a first grid: the rays of every pixel whose
+//                         mean could be an extreme (within twice the largest
+//                         bound); the grid is then laid out again and its
+//                         extremes are the plain path's;
+//   k_sur_exact_cells     after the final grid: every ray within its bound of
+//                         a cell edge, a centre line or the grid's border.
+// Afterwards the cells of every sub-pixel, the active set and L's sparsity
+// are the plain path's; only the weights move, continuously.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sur_exact_ray(const StaticData& sd, const LensModel& lm, const double* rho_tab,
+                                              int t, double* spx, double* spy)
+{
+    const int ns = sd.nsplit, nsub = sd.nsub;
+    const int m = t / nsub, k = t - m * nsub;
+    const int pix = sd.mpix[m];
+    const int i = pix / sd.ny, j = pix - i * sd.ny;
+    const int ii = k / ns, jj = k - ii * ns;
+    const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
+    const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
+    const double px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
+    const double py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
+    double bx, by;
+    find_sourcept<true>(lm, px, py, bx, by, rho_tab);
+    spx[t] = bx;
+    spy[t] = by;
+}
+
+// the lens model and the power-law coefficients in shared memory, as k_raytrace stages them
+__device__ __forceinline__ void sur_stage_model(const EvalParams* __restrict__ ep, LensModel& lm, double* rho_tab)
+{
+    {
+        const double* src = reinterpret_cast<const double*>(&ep->lm);
+        double* dst = reinterpret_cast<double*>(&lm);
+        for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < lm.nlens * SPLE_RHO_TAB; e += blockDim.x) {
+        const LensRec& L = lm.lens[e / SPLE_RHO_TAB];
+        rho_tab[e] = (L.type == QLP_LENS_SPLE && L.kind == 2) ? sple_rho(L, e % SPLE_RHO_TAB + 1) : 0.0;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_sur_exact_extremes(StaticData sd_, SrcOpts so, const EvalParams* __restrict__ ep,
+                                                            double* __restrict__ spx, double* __restrict__ spy,
+                                                            float* __restrict__ sur_eps, const GridState* gs,
+                                                            double eps_g, int* __restrict__ n_exact)
+{
+    const StaticData sd = eval_shape(sd_);
+    __shared__ __align__(16) LensModel lm;
+    __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
+    sur_stage_model(ep, lm, rho_tab);
+    const int nsub = sd.nsub;
+    const bool use_nt = so.noise_threshold > 0;
+    const double e0 = gs->ext[0], e1 = gs->ext[1], e2 = gs->ext[2], e3 = gs->ext[3];
+    int cnt = 0;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
+        if (use_nt) {
+            const int pix = sd.mpix[m];
+            if (sd.data[pix] <= so.noise_threshold * sqrt(1.0 / sd.covinv[pix])) continue;
+        }
+        double xs = 0, ys = 0;
+        float emax = 0.f;
+        for (int k = 0; k < nsub; k++) {
+            xs += spx[m * nsub + k];
+            ys += spy[m * nsub + k];
+            emax = fmaxf(emax, sur_eps[m * nsub + k]);
+        }
+        if (emax == 0.f) continue;
+        xs /= nsub; ys /= nsub;
+        const double tol = 2.0 * eps_g;
+        const bool near = fabs(xs - e0) <= tol || fabs(xs - e1) <= tol || fabs(ys - e2) <= tol || fabs(ys - e3) <= tol;
+        if (!near) continue;
+        for (int k = 0; k < nsub; k++) {
+            sur_exact_ray(sd, lm, rho_tab, m * nsub + k, spx, spy);
+            sur_eps[m * nsub + k] = 0.f;
+        }
+        cnt += nsub;
+    }
+    if (cnt) atomicAdd(n_exact, cnt);
+}
+
+// distance from v to the decision lines of one axis: the grid's border when
+// outside it, else the edges of its cell and the line through its centre
+__device__ __forceinline__ double sur_axis_margin(double v, const double* c, const double* cc, int n)
+{
+    if (!(v >= c[0] && v < c[n])) return fmin(fabs(v - c[0]), fabs(v - c[n]));
+    int lo = 0, hi = n - 1;
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (c[mid] <= v) lo = mid; else hi = mid - 1; }
+    return fmin(fmin(v - c[lo], c[lo + 1] - v), fabs(v - cc[lo]));
+}
+
+__global__ void __launch_bounds__(256) k_sur_exact_cells(StaticData sd_, SrcOpts so_, const EvalParams* __restrict__ ep,
+                                                         double* __restrict__ spx, double* __restrict__ spy,
+                                                         float* __restrict__ sur_eps, const double* __restrict__ cx_g,
+                                                         const double* __restrict__ cy_g,
+                                                         const double* __restrict__ ccx_g,
+                                                         const double* __restrict__ ccy_g, int* __restrict__ n_exact)
+{
+    extern __shared__ double sm[];
+    const StaticData sd = eval_shape(sd_);
+    const SrcOpts so = eval_grid(so_, sd_);
+    __shared__ __align__(16) LensModel lm;
+    __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
+    const int snx = so.snx, sny = so.sny;
+    double* cx = sm;
+    double* cy = cx + snx + 1;
+    double* ccx = cy + sny + 1;
+    double* ccy = ccx + snx;
+    for (int i = threadIdx.x; i <= snx; i += blockDim.x) cx[i] = cx_g[i];
+    for (int j = threadIdx.x; j <= sny; j += blockDim.x) cy[j] = cy_g[j];
+    for (int i = threadIdx.x; i < snx; i += blockDim.x) ccx[i] = ccx_g[i];
+    for (int j = threadIdx.x; j < sny; j += blockDim.x) ccy[j] = ccy_g[j];
+    sur_stage_model(ep, lm, rho_tab);
+    int cnt = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < sd.n_sub; t += gridDim.x * blockDim.x) {
+        const double e = sur_eps[t];
+        if (e == 0.0) continue;
+        const double dx = sur_axis_margin(spx[t], cx, ccx, snx), dy = sur_axis_margin(spy[t], cy, ccy, sny);
+        if (dx <= e || dy <= e || dx != dx || dy != dy) {
+            sur_exact_ray(sd, lm, rho_tab, t, spx, spy);
+            sur_eps[t] = 0.f;
+            cnt++;
+        }
+    }
+    if (cnt) atomicAdd(n_exact, cnt);
+}
+
+int launch_surrogate_exact(const StaticData& sd, const SrcOpts& so, Work& w, double eps_g, int step,
+                           cudaStream_t st)
+{
+    if (sd.n_sub == 0) return QLP_OK;
+    if (step == 0) {
+        if (!so.auto_grid) return QLP_OK;
+        const int blocks = std::max(1, std::min((sd.n_mask + 255) / 256, 152 * 8));
+        k_sur_exact_extremes<<<blocks, 256, 0, st>>>(sd, so, w.ep, w.spx, w.spy, w.sur_eps, w.gs, eps_g,
+                                                      &w.out->n_exact);
+    } else {
+        const size_t smem = sizeof(double) * (2 * (so.snx + so.sny) + 2);
+        const int blocks = std::max(1, std::min((sd.n_sub + 255) / 256, 152 * 16));
+        k_sur_exact_cells<<<blocks, 256, smem, st>>>(sd, so, w.ep, w.spx, w.spy, w.sur_eps, w.cx, w.cy, w.ccx,
+                                                     w.ccy, &w.out->n_exact);
+    }
+    count_launches(1);
+    return QLP_OK;
 }
 
 // The queued fallbacks of k_raytrace_sur: quadrature deflection of lens
@@ -1199,7 +1386,7 @@ int launch_raytrace_sur(const StaticData& sd, Work& w, double thresh, int defer_
     k_raytrace_sur<<<sur_grid(sd.n_sub), SUR_THREADS, SUR_SMEM, st>>>(sd, w.ep, w.spx, w.spy, S.wimg, S.small,
                                                                        S.bound,
                                                                    thresh, defer_lens, w.fb_count, w.fb_ray,
-                                                                   w.fb_xy, w.gs, w.out);
+                                                                   w.fb_xy, w.sur_eps, w.gs, w.out);
     int n = 1;
     if (defer_lens >= 0) {
         const int blocks = std::min((sd.n_sub + 255) / 256, 152 * 8);
