@@ -4,8 +4,10 @@
                     [--config cfg5] [--batch B] [--precision mixed|fp64]
 
 A step is one batch of B likelihood evaluations: B lens-parameter vectors are
-drawn from the configuration's prior box and evaluated through the public C
-ABI (qlp_eval_batch).  The default workload is the metric's own: the two-plane
+drawn from the configuration's sampling region (for the default workload the
+posterior region around the mock's parameters, where a sampler spends its
+evaluations; the line's `draws` says which) and evaluated through the public
+C ABI (qlp_eval_batch).  The default workload is the metric's own: the two-plane
 subhalo configuration (300x300 pixels at 0.03", annulus 0.3"-3.5", 4x4 split,
 31x31 Airy-like PSF; SIE + shear at z = 0.5, an elliptical NFW subhalo at
 z = 0.8 given by its mass, 1e8-1e10 M_sun; source at z = 2), 1024 vectors per
@@ -44,6 +46,14 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import numpy as np  # noqa: E402
 
 METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 at |ΔlogL|<0.1"
+
+# Useful FLOP of the surrogate network per ray on the tensor cores: its three
+# 128 x 128 layers, each product counted once (the hi/lo split is not work).
+MLP_FLOP_PER_RAY = 2 * 3 * 128 * 128
+# DRAM bytes (read + written) of one launch, from one ncu capture of that
+# kernel on the workload (dram__bytes_read.sum + dram__bytes_write.sum)
+RAYSUR_TRAFFIC = {"cfg5": 589824 + 512}
+SYRK_TRAFFIC = {}
 UNIT = "evals/s"
 
 
@@ -315,6 +325,12 @@ def main():
                     help="keep the default launch schedule instead of tuning it on a sample batch first")
     ap.add_argument("--nfw", default="surrogate", choices=["surrogate", "quadrature"],
                     help="NFW deflection: trained MLP surrogate (quadrature fallback) or quadrature only")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="after the measurement, run one more step between cudaProfilerStart and cudaProfilerStop "
+                         "(for ncu --profile-from-start off); untimed")
+    ap.add_argument("--train-steps", type=int, default=0,
+                    help="Adam steps of the surrogate's training (default: the library's; fewer only to shorten "
+                         "profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -350,7 +366,8 @@ def main():
         nfw = {"mode": "quadrature"}
         if args.nfw == "surrogate":
             from qlens_gb300 import pixlike
-            rep = pixlike.train_nfw_surrogate(device=local_rank)
+            rep = pixlike.train_nfw_surrogate(device=local_rank,
+                                              **({"steps": args.train_steps} if args.train_steps > 0 else {}))
             pl.set_nfw_mode(abi.QLP_NFW_SURROGATE)
             nfw = {"mode": "surrogate", "threshold_arcsec": 2e-5, "train_ms": rep["train_ms"],
                    "val_mean_rel": rep["val_mean_rel"], "n_params": rep["n_params"]}
@@ -452,13 +469,47 @@ def main():
         peak = 1.25
         peak_note = "nominal GB300 FP64 (no FP64 figure in MEASURED_PEAKS.json)"
         bound = "fp64"
-    roofline = {"bound": bound, "kernel": "F = L'^T C^-1 L' (SYRK)", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
-                "peak_source": peak_note, "algorithmic_flops_per_launch": flops,
-                "timing": "CUDA events around the SYRK launch of single evaluations after the timed region"}
+    roofline_syrk = {"bound": bound, "kernel": "F = L'^T C^-1 L' (SYRK)", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": SYRK_TRAFFIC.get(args.config) if precision == "mixed" else None,
+                     "peak_source": peak_note, "algorithmic_flops_per_launch": flops,
+                     "timing": "CUDA events around the SYRK launch of single evaluations after the timed region"}
+    # the dominant kernel of the batch: the ray shooting on the NFW surrogate
+    # workloads (k_raytrace_sur), else the factorisation of F
+    roofline = roofline_syrk
+    if precision == "mixed" and nfw and nfw["mode"] == "surrogate":
+        ray_ms = stage[0]
+        n_rays = wl.n_mask * wl.nsplit ** 2
+        mlp = n_rays * MLP_FLOP_PER_RAY
+        ach = mlp / (ray_ms / 1e3) / 1e12 if ray_ms > 0 else None
+        roofline = {"bound": "tensor", "kernel": "k_raytrace_sur (ray shooting with the NFW surrogate)",
+                    "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if ach else None,
+                    "traffic": RAYSUR_TRAFFIC.get(args.config), "peak_source": peak_note,
+                    "algorithmic_flops_per_launch": mlp,
+                    "work": "the network's three 128x128 layers per ray (2 x 3 x 128^2 FLOP), %d rays" % n_rays,
+                    "limiter": "the FP64 pipe (SIE deflection, lens equation and the NFW baseline per ray in FP64): "
+                               "34% active, tensor pipe 6%, 8 warps per SM (one ncu capture)",
+                    "timing": "CUDA events around the ray-shooting stage of single evaluations after the timed "
+                              "region"}
+    elif precision == "mixed":
+        ch_flop = float(np.mean([r["n_active_src"] ** 3 / 3.0 for r in iso_res]))
+        ach = ch_flop / (stage[4] / 1e3) / 1e12 if stage[4] > 0 else None
+        roofline = {"bound": "tensor", "kernel": "Cholesky of F (k_potrf128, k_chol_tile128, k_chol_upd16)",
+                    "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if ach else None,
+                    "traffic": None, "peak_source": peak_note, "algorithmic_flops_per_launch": ch_flop,
+                    "work": "M^3/3 FLOP per factorisation",
+                    "limiter": "the single-CTA pivot chain of M/128 steps per evaluation",
+                    "timing": "CUDA events around the factorisation stage of single evaluations after the timed "
+                              "region"}
 
     if args.trace and rank == 0:
         write_trace(pl, run_step, args.warmup, args.trace)
+    if args.profile_step:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        run_step(args.warmup)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
 
     # the plain FP64 path on the first vectors of the first timed batch: its
     # throughput, the ratio, and |delta log L| of the timed path against it
@@ -504,7 +555,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-tensor+f64" if precision == "mixed" else "f64",
-            "data": "synthetic (seeded mock image; parameters drawn from the prior box)",
+            "data": "synthetic (seeded mock image; parameter vectors drawn as `draws` states)",
             "config": {**wl.describe(), "batch_per_step": B, "precision": precision,
                        "nfw": nfw["mode"] if nfw else None,
                        "schedule": pl.schedule(),
@@ -518,9 +569,10 @@ def main():
             "vs_plain_fp64": (value / plain["value"]) if plain else None,
             "plain_fp64": plain,
             "accuracy": accuracy,
-            "draws": wl.draws_note,
+            "draws": wl.draws_note or "uniform over the configuration's prior box",
             "prior_draws": prior,
             "roofline": roofline,
+            "roofline_syrk": roofline_syrk,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "launches_per_eval": launches / float(B * args.steps),

@@ -1,8 +1,9 @@
 """Build libqlpix.so in-tree (qlens_gb300/_lib/) with nvcc for sm_103a.
 
 Every translation unit is compiled separately so that the ray-shooting and
-mapping kernels can be built with --fmad=false (QLens's operation order, no
-contracted multiply-adds) while the dense algebra keeps FMA.  Compiles run in
+mapping kernels that reproduce QLens's bits can be built with --fmad=false
+(QLens's operation order, no contracted multiply-adds) while the dense algebra
+and the surrogate ray shooting keep FMA.  Compiles run in
 parallel and only when a source is newer than its object.
 """
 import concurrent.futures as cf
@@ -30,7 +31,8 @@ UNITS = [
     ("sparseops.cu", []),
     ("noalloc.cu", []),
     ("mixed.cu", []),
-    ("surrogate.cu", ["--fmad=false"]),
+    ("surrogate.cu", []),
+    ("sur_exact.cu", ["--fmad=false"]),
     ("outside.cu", ["--fmad=false"]),
     ("ctx.cpp", []),
     ("autotune.cpp", []),

@@ -14,6 +14,7 @@ namespace qlpix {
 void psf_init_attributes();
 void linalg_init_attributes();
 void sparseops_init_attributes();
+void sur_exact_init_attributes();
 
 static int cuda_fail(cudaError_t e, const char* where)
 {
@@ -47,7 +48,7 @@ static void free_work(Work& w)
     void* ptrs[] = {w.spx, w.spy, w.cx, w.cy, w.ccx, w.ccy, w.cell3, w.w3, w.mapped, w.active_index, w.pixmaps,
                     w.rowidx, w.pixindex, w.rowpix, w.rowptr, w.Lidx, w.Lval, w.cidx, w.cval, w.ccnt, w.Lpsf,
                     w.dvec, w.cvec, w.D, w.F, w.R, w.s, w.tmp, w.model, w.partial, w.linv, w.gs, w.out, w.ep,
-                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart, w.lnz, w.sur_eps};
+                    w.fb_ray, w.fb_xy, w.fb_count, w.F0, w.gpart, w.gpart_cnt, w.cpart, w.lnz, w.sur_eps, w.xlist, w.xcount, w.nfw_xy};
     for (void* p : ptrs) if (p) cudaFree(p);
     memset(&w, 0, sizeof(w));
 }
@@ -110,6 +111,8 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     CK(dalloc(&w.gs, 1), "alloc"); CK(dalloc(&w.out, 1), "alloc"); CK(dalloc(&w.ep, 1), "alloc");
     CK(dalloc(&w.fb_ray, n_sub), "alloc"); CK(dalloc(&w.fb_xy, 2 * n_sub), "alloc"); CK(dalloc(&w.fb_count, 1), "alloc");
     CK(dalloc(&w.sur_eps, n_sub), "alloc");
+    CK(dalloc(&w.xlist, n_sub), "alloc"); CK(dalloc(&w.xcount, 1), "alloc");
+    CK(dalloc(&w.nfw_xy, 2 * n_sub), "alloc");
     s.M_cap = Mc;
     s.N_cap = n_mask;
     s.npix_pad = (c->nx + 2 * (c->sd.pnx / 2)) * (c->ny + 2 * (c->sd.pny / 2));
@@ -204,6 +207,14 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
         const double xmax = 4.0 * std::max(psum, 1e-30) * std::max(sqrt(cmax), 1e-30);
         sd.x_exp = std::max(-60, std::min(60, (int)floor(log2(16384.0 / xmax))));
         sd.fix_exp_x = std::max(0, std::min(100, 61 - (int)ceil(log2(4.0 * std::max(psum, 1e-30)))));
+        const int pnx = psf->nx, pny = psf->ny;
+        std::vector<float> pf((size_t)pnx * pny);
+        for (int pl = 0; pl < pny; pl++)
+            for (int pk = 0; pk < pnx; pk++)
+                pf[(size_t)pl * pnx + pk] = (float)psf->matrix[(size_t)pk * pny + pl] * ldexpf(1.0f, sd.fix_exp_x);
+        CK(dalloc(&c->d_psf_fix, pf.size()), "alloc");
+        CK(cudaMemcpy(c->d_psf_fix, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice), "h2d");
+        sd.psf_fix = c->d_psf_fix;
     }
 
     SrcOpts& so = c->so;
@@ -219,6 +230,7 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
     psf_init_attributes();
     linalg_init_attributes();
     sparseops_init_attributes();
+    sur_exact_init_attributes();
     int snx = std::max(so.snx, 2), sny = std::max(so.sny, 2);
     return ensure_slot(c, 0, sd.n_mask, snx * sny, snx, sny);
 }
@@ -234,7 +246,7 @@ void ctx_free(qlp_ctx* c)
         if (s.side_join) cudaEventDestroy(s.side_join);
     }
     c->slots.clear();
-    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_mpix, c->d_inst_mpix,
+    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_psf_fix, c->d_mpix, c->d_inst_mpix,
                     c->d_emask, c->d_inmask, c->d_epix, c->d_eoff};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);

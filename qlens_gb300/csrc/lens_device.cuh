@@ -1,5 +1,7 @@
 // lens_device.cuh -- FP64 deflection of the lens models on the device.
-// Included by translation units built with --fmad=false.
+// The units that must reproduce QLens's bits (raytrace.cu, sur_exact.cu,
+// outside.cu) include it built with --fmad=false;
+// surrogate.cu includes it with contraction (its rays carry an error bound).
 #pragma once
 #include "qlpix_internal.h"
 
@@ -96,9 +98,10 @@ namespace qlpix {
 
 // LensProfile::deflection (profile.cpp:1782-1805); Shear::deflection (models.cpp:2266-2272).
 // NFW = false compiles the kernel without the quadrature (no NFW lens in the model).
+// wbuf: see nfw_deflection (null: one ray per thread).
 template <bool NFW>
 __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, double y, double& dx, double& dy,
-                                                const double* rho_tab = nullptr)
+                                                const double* rho_tab = nullptr, double* wbuf = nullptr)
 {
     if (L.type == QLP_LENS_SHEAR) {
         x -= L.xc; y -= L.yc;
@@ -116,7 +119,7 @@ __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, doub
     }
     double ax, ay;
     if (!NFW || L.type == QLP_LENS_SPLE) sple_deflection(L, x, y, ax, ay, rho_tab);
-    else nfw_deflection(L, x, y, ax, ay);
+    else nfw_deflection(L, x, y, ax, ay, wbuf);
     if (rot) {
         double xp = ax * L.costheta - ay * L.sintheta;
         ay = ax * L.sintheta + ay * L.costheta;
@@ -125,12 +128,42 @@ __device__ __forceinline__ void lens_deflection(const LensRec& L, double x, doub
     dx = ax; dy = ay;
 }
 
+// Sub-pixel centres (set_nsplits, pixelgrid.cpp:10898-10938): sub-pixel
+// (ii, jj) of pixel (i, j) sits at (1-u0) x_i + u0 x_{i+1} with
+// u0 = (1 + 2 ii) / (2 ns), likewise in y.  subpix_table forms u0 and 1 - u0
+// once per CTA (any threads; a barrier before use); subpix_centre uses the
+// table when ns fits it and the same expressions otherwise -- the same bits
+// either way, with no FP64 divide per ray.
+#define SUBPIX_TAB 32
+__device__ __forceinline__ void subpix_table(int ns, double* fu, double* f1mu)
+{
+    for (int e = threadIdx.x; e < ns && e < SUBPIX_TAB; e += blockDim.x) {
+        const double u0 = ((double)(1 + 2 * e)) / (2 * ns);
+        fu[e] = u0;
+        f1mu[e] = 1 - u0;
+    }
+}
+
+__device__ __forceinline__ void subpix_centre(const StaticData& sd, int ns, int ii, int jj, int i, int j,
+                                              const double* fu, const double* f1mu, double& px, double& py)
+{
+    if (ns <= SUBPIX_TAB) {
+        px = f1mu[ii] * sd.xvals[i] + fu[ii] * sd.xvals[i + 1];
+        py = f1mu[jj] * sd.yvals[j] + fu[jj] * sd.yvals[j + 1];
+    } else {
+        const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
+        const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
+        px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
+        py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
+    }
+}
+
 // QLens::deflection + QLens::find_sourcept (lenscalc.cpp:81-113, 325-330).
 // rho_tab: SPLE_RHO_TAB series coefficients per lens (lens k at k *
 // SPLE_RHO_TAB), or null.
 template <bool NFW>
 __device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, double y, double& bx, double& by,
-                                              const double* rho_tab = nullptr)
+                                              const double* rho_tab = nullptr, double* wbuf = nullptr)
 {
     double defx = 0, defy = 0;
     double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
@@ -148,7 +181,8 @@ __device__ __forceinline__ void find_sourcept(const LensModel& lm, double x, dou
             for (int k = 0; k < lm.nlens; k++) {
                 if (lm.lens[k].plane != i) continue;
                 double ax, ay;
-                lens_deflection<NFW>(lm.lens[k], xi, yi, ax, ay, rho_tab ? rho_tab + k * SPLE_RHO_TAB : nullptr);
+                lens_deflection<NFW>(lm.lens[k], xi, yi, ax, ay, rho_tab ? rho_tab + k * SPLE_RHO_TAB : nullptr,
+                                     wbuf);
                 dsx[i] += ax; dsy[i] += ay;
             }
             dsx[i] *= lm.zfac[i];

@@ -217,17 +217,54 @@ __global__ void k_csc_fill(const GridState* __restrict__ gs, const int* __restri
 }
 
 // Each column's entries in increasing row order, so that every sum over a
-// column runs in a fixed order (k_csc_fill places them in atomic order): the
-// rank of an entry is the number of entries of its column with a smaller row
-// (rows are distinct within a column of the merged L).  One CTA per column.
-__global__ void __launch_bounds__(128) k_csc_sort(const GridState* __restrict__ gs, const int* __restrict__ colptr,
+// column runs in a fixed order (k_csc_fill places them in atomic order).
+// Rows are distinct within a column of the merged L, so the order is a
+// permutation: a bitonic sort of the (row, source position) pairs in shared
+// memory for columns of up to CSC_SORT_MAX entries, else each entry's rank
+// counted directly.  One CTA per column.
+#define CSC_SORT_MAX 4096
+__global__ void __launch_bounds__(256) k_csc_sort(const GridState* __restrict__ gs, const int* __restrict__ colptr,
                                                   const int* __restrict__ col_u, const int* __restrict__ src_u,
                                                   const double* __restrict__ cval, int* __restrict__ colrow,
                                                   float* __restrict__ colval, double* __restrict__ colval64)
 {
+    __shared__ int key[CSC_SORT_MAX];
+    __shared__ int pos[CSC_SORT_MAX];
     const int s = blockIdx.x;
     if (s >= gs->M) return;
     const int b = colptr[s], n = colptr[s + 1] - b;
+    if (n <= CSC_SORT_MAX) {
+        int p2 = 1;
+        while (p2 < n) p2 <<= 1;
+        for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+            key[i] = (i < n) ? col_u[b + i] : INT_MAX;
+            pos[i] = (i < n) ? src_u[b + i] : 0;
+        }
+        __syncthreads();
+        for (int k = 2; k <= p2; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const bool up = (i & k) == 0;
+                        const int ki = key[i], kl = key[l];
+                        if ((ki > kl) == up) {
+                            key[i] = kl; key[l] = ki;
+                            const int t = pos[i]; pos[i] = pos[l]; pos[l] = t;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double v = cval[pos[i]];
+            colrow[b + i] = key[i];
+            colval[b + i] = (float)v;
+            colval64[b + i] = v;
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int ri = col_u[b + i];
         int rank = 0;
@@ -271,6 +308,23 @@ __global__ void __launch_bounds__(256) k_LTw_csc(const GridState* __restrict__ g
 // band's active rows; for each entry only the PSF rows that land in the band
 // are visited, lanes along x (consecutive accumulators: the 64-bit shared
 // atomics of one instruction do not collide).
+// float -> int64, rounded to nearest even, without the 64-bit conversion
+// instruction (on GB300 it issues to the FP64 pipe, 1/64 of the FP32 rate,
+// and the PSF-to-X kernels convert one product per tap).  A float of
+// magnitude >= 2^23 is an integer: its value is the 24-bit significand
+// shifted left by the exponent.  Smaller ones (products below 2^-36 of the
+// grid's range) round through the 32-bit conversion.  Same result as
+// __float2ll_rn for |x| < 2^63, which the fixed-point scale guarantees
+// (4 sum|psf| 2^fix_exp_x <= 2^61, |L| <= 1).
+__device__ __forceinline__ long long f2ll_rn_int(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    const int e = (int)((u >> 23) & 0xffu) - 150;
+    if (e < 0) return (long long)__float2int_rn(x);
+    const long long m = (long long)((u & 0x7fffffu) | 0x800000u) << e;
+    return (u >> 31) ? -m : m;
+}
+
 __device__ __forceinline__ int lower_bound_row(const int* __restrict__ rowpix, const int* __restrict__ idx, int n,
                                                int ny, int jmin)
 {
@@ -284,6 +338,105 @@ __device__ __forceinline__ int lower_bound_row(const int* __restrict__ rowpix, c
     return lo;
 }
 
+// The same search by a whole warp (all lanes, converged): 32 probes per
+// round narrow the range 32-fold, so a few rounds of dependent loads instead
+// of log2(n).
+__device__ __forceinline__ int warp_lower_bound_row(const int* __restrict__ rowpix, const int* __restrict__ idx,
+                                                    int n, int ny, int jmin)
+{
+    const int lane = threadIdx.x & 31;
+    int lo = 0, hi = n;                       // the answer lies in [lo, hi]
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) / 32;
+        const int p = lo + lane * step;
+        bool ge = true;
+        if (p < hi) {
+            const int pix = rowpix[idx ? idx[p] : p];
+            ge = pix - (pix / ny) * ny >= jmin;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, ge);
+        if (b == 0) {
+            lo = lo + 31 * step + 1;
+        } else {
+            const int f = __ffs(b) - 1;
+            const int pf = lo + f * step;
+            if (f > 0) lo = lo + (f - 1) * step + 1;
+            hi = min(hi, pf);
+        }
+    }
+    const int p = lo + lane;
+    bool ge = true;
+    if (p < hi) {
+        const int pix = rowpix[idx ? idx[p] : p];
+        ge = pix - (pix / ny) * ny >= jmin;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, ge);
+    return b ? lo + __ffs(b) - 1 : hi;
+}
+
+// int64 -> float, rounded to nearest even, in integer arithmetic (the same
+// result as the conversion instruction, which GB300 issues to its FP64 pipe):
+// the top 24 significant bits, rounded on the bits below them.
+__device__ __forceinline__ float ll2f_rn_int(long long v)
+{
+    if (v == 0) return 0.0f;
+    const unsigned sign = v < 0 ? 0x80000000u : 0u;
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    int e = 63 - __clzll((long long)a);          // index of the top bit
+    unsigned m;
+    if (e <= 23) {
+        m = (unsigned)(a << (23 - e));
+    } else {
+        const int sh = e - 23;
+        m = (unsigned)(a >> sh);
+        const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (m & 1u))) {
+            if (++m == (1u << 24)) { m >>= 1; e++; }
+        }
+    }
+    return __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (m & 0x7fffffu));
+}
+
+// Eight consecutive entries of X (idx a multiple of 8): the F16 hi + lo
+// parts as 16-byte stores (or the TF32 parts as 32-byte pairs).  Returns
+// whether any part is nonzero.
+__device__ __forceinline__ bool store_x8(void* Xh, void* Xl, size_t idx, const float* v, float xs, bool half)
+{
+    bool any = false;
+    if (half) {
+        __align__(16) __half h[8], l[8];
+        #pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const float vs = v[u] * xs;
+            h[u] = __float2half_rn(vs);
+            l[u] = __float2half_rn(vs - __half2float(h[u]));
+            any |= __half2float(h[u]) != 0.0f || __half2float(l[u]) != 0.0f;
+        }
+        *reinterpret_cast<uint4*>(reinterpret_cast<__half*>(Xh) + idx) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(reinterpret_cast<__half*>(Xl) + idx) = *reinterpret_cast<const uint4*>(l);
+        return any;
+    }
+    __align__(16) float h[8], l[8];
+    #pragma unroll
+    for (int u = 0; u < 8; u++) {
+        h[u] = to_tf32(v[u]);
+        l[u] = to_tf32(v[u] - h[u]);
+        any |= h[u] != 0.0f || l[u] != 0.0f;
+    }
+    float4* ph = reinterpret_cast<float4*>(reinterpret_cast<float*>(Xh) + idx);
+    float4* pl = reinterpret_cast<float4*>(reinterpret_cast<float*>(Xl) + idx);
+    ph[0] = *reinterpret_cast<const float4*>(h);
+    ph[1] = *reinterpret_cast<const float4*>(h + 4);
+    pl[0] = *reinterpret_cast<const float4*>(l);
+    pl[1] = *reinterpret_cast<const float4*>(l + 4);
+    return any;
+}
+
+// REGPSF (PSFs of at most 32 x 32 taps): lane pk holds PSF column pk in
+// registers and an entry's footprint is visited row by row, fully unrolled
+// -- no shared-memory loads of taps or offsets per tap, independent atomics
+// back to back.  The integer sums are the same either way.
+template <bool REGPSF>
 __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
@@ -305,16 +458,21 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     const int s = blockIdx.x;
     const int j0 = blockIdx.y * H, j1 = min(j0 + H, sd.ny);
     if (s >= Mp || j0 >= sd.ny) return;
-    const float scale = ldexpf(1.0f, sd.fix_exp_x), inv = ldexpf(1.0f, -sd.fix_exp_x);
+    const float inv = ldexpf(1.0f, -sd.fix_exp_x);
     const int b = (s < M) ? colptr[s] : 0, n = (s < M) ? colptr[s + 1] - b : 0;
-    // four binary searches, one thread each: the entries whose footprint
-    // (rows jq - nyh .. jq - nyh + pny - 1) can reach rows [j0, j1), i.e. jq in
+    // four searches, a warp each: the entries whose footprint (rows
+    // jq - nyh .. jq - nyh + pny - 1) can reach rows [j0, j1), i.e. jq in
     // [j0 - nyh, j1 + nyh), and the band's active rows
-    if (threadIdx.x == 0) sh[0] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
-    if (threadIdx.x == 32) sh[1] = lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
-    if (threadIdx.x == 64) sh[2] = lower_bound_row(rowpix, nullptr, N, sd.ny, j0);
-    if (threadIdx.x == 96) sh[3] = lower_bound_row(rowpix, nullptr, N, sd.ny, j1);
-    if (threadIdx.x == 1) { sh[4] = INT_MAX; sh[5] = INT_MIN; sh[6] = INT_MAX; sh[7] = INT_MIN; }
+    {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        int r = 0;
+        if (warp == 0) r = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
+        if (warp == 1) r = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
+        if (warp == 2) r = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, j0);
+        if (warp == 3) r = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, j1);
+        if (warp < 4 && lane == 0) sh[warp] = r;
+    }
+    if (threadIdx.x == 0) { sh[4] = INT_MAX; sh[5] = INT_MIN; sh[6] = INT_MAX; sh[7] = INT_MIN; }
     __syncthreads();
     const int e0 = sh[0], e1 = sh[1];
     // bounding box of the entries (x and y image indices)
@@ -343,16 +501,38 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     const int wr1 = any ? min(j1, sh[7] - nyh + pny) : j0;
     const int Wb = any ? sh[5] - imin + pnx : 0;
     for (int i = threadIdx.x; i < (wr1 - wr0) * Wb; i += blockDim.x) acc[i] = 0;
-    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] scaled to the
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on the
     // fixed-point grid, and the tap's offset in the window from the
-    // footprint's corner
-    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
-        const int pl = t / pnx, pk = t - pl * pnx;
-        tpsf[t] = (float)sd.psf[pk * pny + pl] * scale;
-        toff[t] = pl * Wb + pk;
+    // footprint's corner (the register path reads the taps directly)
+    if (!REGPSF && any) {
+        for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+            const int pl = t / pnx, pk = t - pl * pnx;
+            tpsf[t] = sd.psf_fix[t];
+            toff[t] = pl * Wb + pk;
+        }
     }
     __syncthreads();
-    {
+    if (REGPSF) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        float col[32];
+        #pragma unroll
+        for (int pl = 0; pl < 32; pl++) col[pl] = (e1 > e0 && lane < pnx && pl < pny) ? sd.psf_fix[pl * pnx + lane] : 0.0f;
+        for (int e = e0 + warp; e < e1; e += nw) {
+            const int q = colrow[b + e];
+            const float v = colval[b + e];
+            const int pix = rowpix[q];
+            const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
+            const int pl0 = max(0, wr0 - (jq - nyh)), pl1 = min(pny, wr1 - (jq - nyh));
+            unsigned long long* cl = reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb +
+                                     (iq - imin) + lane;
+            if (lane < pnx) {
+                #pragma unroll
+                for (int pl = 0; pl < 32; pl++)
+                    if (pl >= pl0 && pl < pl1)
+                        atomicAdd(cl + pl * Wb, (unsigned long long)f2ll_rn_int(col[pl] * v));
+            }
+        }
+    } else {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         for (int e = e0 + warp; e < e1; e += nw) {
             const int q = colrow[b + e];
@@ -365,21 +545,38 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
             unsigned long long* corner = reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb + (iq - imin);
             const int t1 = pl1 * pnx;
             for (int t = pl0 * pnx + lane; t < t1; t += 32)
-                atomicAdd(corner + toff[t], (unsigned long long)__float2ll_rn(tpsf[t] * v));
+                atomicAdd(corner + toff[t], (unsigned long long)f2ll_rn_int(tpsf[t] * v));
         }
     }
     __syncthreads();
     // X[s][r] for the band's active rows r: v = sqrt(C^-1)_r * sum (0 outside
     // the window) split into hi + lo; the first band also clears X[s][N .. N
     // rounded up to 64) (the SYRK reads whole stages)
-    for (int r = sh[2] + threadIdx.x; r < sh[3]; r += blockDim.x) {
-        const int pix = rowpix[r];
-        const int i = pix / sd.ny, j = pix - i * sd.ny;
-        const int wc = i - imin + nxh;
-        float v = 0.0f;
-        if (j >= wr0 && j < wr1 && wc >= 0 && wc < Wb) v = ((float)acc[(j - wr0) * Wb + wc] * inv) * sqc[r];
-        if (store_x(Xh, Xl, (size_t)s * K_cap + r, v, xs, half))
-            nz[(size_t)(s / TC_TILE) * nkb_cap + r / TC_KB] = 1;
+    // (eight rows per thread where the band's range is aligned to eight,
+    // single rows at its two ends)
+    {
+        const int ra = sh[2], rb = sh[3];
+        const int ha = min(rb, (ra + 7) & ~7), tb = max(ha, rb & ~7);
+        auto xval = [&](int r) -> float {
+            const int pix = rowpix[r];
+            const int i = pix / sd.ny, j = pix - i * sd.ny;
+            const int wc = i - imin + nxh;
+            float v = 0.0f;
+            if (j >= wr0 && j < wr1 && wc >= 0 && wc < Wb) v = (ll2f_rn_int(acc[(j - wr0) * Wb + wc]) * inv) * sqc[r];
+            return v;
+        };
+        for (int r = threadIdx.x; r < (ha - ra) + (rb - tb); r += blockDim.x) {
+            const int rr = (r < ha - ra) ? ra + r : tb + (r - (ha - ra));
+            if (store_x(Xh, Xl, (size_t)s * K_cap + rr, xval(rr), xs, half))
+                nz[(size_t)(s / TC_TILE) * nkb_cap + rr / TC_KB] = 1;
+        }
+        for (int g = ha + 8 * threadIdx.x; g < tb; g += 8 * blockDim.x) {
+            float v[8];
+            #pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = xval(g + u);
+            if (store_x8(Xh, Xl, (size_t)s * K_cap + g, v, xs, half))
+                nz[(size_t)(s / TC_TILE) * nkb_cap + g / TC_KB] = 1;
+        }
     }
     if (blockIdx.y == 0) {
         const int Np = (N + 63) & ~63;
@@ -411,17 +608,17 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
     const int r0 = blockIdx.y * chunk, r1 = min(r0 + chunk, Np);
     if (s >= Mp || r0 >= Np) return;
     const int nT = sd.pnx * sd.pny;
-    const float scale = ldexpf(1.0f, sd.fix_exp_x), inv = ldexpf(1.0f, -sd.fix_exp_x);
+    const float inv = ldexpf(1.0f, -sd.fix_exp_x);
     const int pnx = sd.pnx, pny = sd.pny;
     const int nxp = sd.nx + 2 * (pnx / 2);                    // padded width of pixT
     int* toff = reinterpret_cast<int*>(tpsf + nT);
     for (int i = threadIdx.x; i < r1 - r0; i += blockDim.x) acc[i] = 0;
-    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] scaled to the
-    // fixed-point grid (a power of two: exact, so x * scale keeps its bits), and
-    // the tap's offset in pixT from the footprint's corner
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on the
+    // fixed-point grid (StaticData::psf_fix), and the tap's offset in pixT
+    // from the footprint's corner
     for (int t = threadIdx.x; t < nT; t += blockDim.x) {
         const int pl = t / pnx, pk = t - pl * pnx;
-        tpsf[t] = (float)sd.psf[pk * pny + pl] * scale;
+        tpsf[t] = sd.psf_fix[t];
         toff[t] = pl * nxp + pk;
     }
     __syncthreads();
@@ -456,7 +653,7 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
                 for (int u = 0; u < 4; u++) {
                     if (P[u].x >= r0 && P[u].x < r1)                // inactive (-1) or another chunk
                         atomicAdd(reinterpret_cast<unsigned long long*>(&acc[P[u].x - r0]),
-                                  (unsigned long long)__float2ll_rn(w[u] * v));
+                                  (unsigned long long)f2ll_rn_int(w[u] * v));
                 }
             }
         }
@@ -469,7 +666,7 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
         const int i = i0 + threadIdx.x;
         bool nonzero = false;
         if (i < span) {
-            const float v = (r0 + i < N) ? ((float)acc[i] * inv) * sqc[r0 + i] : 0.0f;
+            const float v = (r0 + i < N) ? (ll2f_rn_int(acc[i]) * inv) * sqc[r0 + i] : 0.0f;
             nonzero = store_x(Xh, Xl, (size_t)s * K_cap + r0 + i, v, xs, half);
         }
         const unsigned any = __ballot_sync(0xffffffffu, nonzero);
@@ -660,7 +857,8 @@ int mixed_init(Slot& c)
         return QLP_ERR_CUDA;
     }
     cudaFuncSetAttribute(k_psf_x_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_psf_x_band, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_psf_x_band<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_psf_x_band<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
     cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
     cudaFuncSetAttribute(k_chol_upd16, cudaFuncAttributeMaxDynamicSharedMemorySize, U16_SMEM);
@@ -753,12 +951,12 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
                                                      m->sqc, m->pixT);
         k_csc_scan<<<1, 1024, 0, st>>>(w.gs, m->colcnt, m->cursor);
         k_csc_fill<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, m->cursor, m->col_u, m->src_u);
-        k_csc_sort<<<m->M_cap, 128, 0, st>>>(w.gs, m->colcnt, m->col_u, m->src_u, w.cval, m->colrow, m->colval,
+        k_csc_sort<<<m->M_cap, 256, 0, st>>>(w.gs, m->colcnt, m->col_u, m->src_u, w.cval, m->colrow, m->colval,
                                             m->colval64);
         n += 4;
     }
     // D = L^T P^T (C^-1 d), FP64
-    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, m->img, st);
+    op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, m->img, m->pixT, st);
     k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, w.D);
     n++;
     // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
@@ -777,7 +975,12 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
             const int H = std::max(1, std::min(sd.ny, fit) / split);
             const int nband = (sd.ny + H - 1) / H;
             const size_t smem = sizeof(long long) * (size_t)H * W + tap_bytes;
-            k_psf_x_band<<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
+            if (sd.pnx <= 32 && sd.pny <= 32)
+                k_psf_x_band<true><<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
+                                                                   w.rowpix, m->sqc, H, m->X_hi, m->X_lo, xs,
+                                                                   m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
+            else
+                k_psf_x_band<false><<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
                                                                    w.rowpix, m->sqc, H, m->X_hi, m->X_lo, xs,
                                                                    m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
         } else {
@@ -850,8 +1053,8 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         n += 3;
         if (it == refine) break;
         op_Ls(w, N_cap, w.s, m->t, st);
-        op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, m->img, st);
-        op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, m->img, st);
+        op_conv(sd, w, N_cap, false, m->t, nullptr, m->u, m->img, m->pixT, st);
+        op_conv(sd, w, N_cap, true, m->u, w.cvec, m->t, m->img, m->pixT, st);
         k_LTw_csc<<<ltw_blocks, 256, 0, st>>>(w.gs, m->colcnt, m->colrow, m->colval64, m->t, m->v);
         n++;
         k_residual<<<(so.snx * so.sny + 255) / 256, 256, 0, st>>>(w.gs, w.D, m->v, w.active_index, regp,
@@ -860,7 +1063,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     }
     // model image P L s in FP64 for chi^2
     op_Ls(w, N_cap, w.s, m->t, st);
-    op_conv(sd, w, N_cap, false, m->t, nullptr, w.model, m->img, st);
+    op_conv(sd, w, N_cap, false, m->t, nullptr, w.model, m->img, m->pixT, st);
     count_launches(n);
     return QLP_OK;
 }

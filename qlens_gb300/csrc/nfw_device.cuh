@@ -18,7 +18,7 @@
 // ascending order, as in the reference.  Node values of levels <= 5 (63
 // nodes) are kept per thread; the rare rays that need levels 6-8 recompute
 // the older values they lack, which gives the same bits (same code, no
-// contraction: this header is compiled with --fmad=false).
+// contraction in the units built with --fmad=false).
 //
 // (1-eps u)^(1/2) and ^(3/2) use sqrt (correctly rounded) rather than pow;
 // kappa's atan / atanh / log are CUDA's, within a few ulp of the host libm.
@@ -114,7 +114,61 @@ static __device__ void nfw_integrals(const LensRec& L, double xsq, double ysq, d
     I1 = 0.5 * r1;
 }
 
-static __device__ void nfw_deflection(const LensRec& L, double x, double y, double& dx, double& dy)
+// The same two integrals for one ray per warp (all 32 lanes call it with the
+// same arguments, converged): the lanes evaluate a level's new nodes in
+// parallel into the warp's buffers v0, v1 (QLP_PAT_N doubles each, by node
+// index), then every lane forms the level sums from the buffers in
+// nfw_integrals' order.  The node values come from the same function and
+// are added in the same order, so the result has nfw_integrals' bits, after
+// about one node's latency per level instead of 2^level of them.
+static __device__ void nfw_integrals_warp(const LensRec& L, double xsq, double ysq, double tol, double& I0,
+                                          double& I1, double* v0, double* v1)
+{
+    const int lane = threadIdx.x & 31;
+    double r0 = 0, r1 = 0, old0, old1;
+    bool done0 = false, done1 = false;
+    int level = 0;
+    do {
+        const double* wt = c_pat_weights + ((2 << level) - level - 2);
+        const int order = (2 << level) - 1;
+        const int istep0 = (QLP_PAT_N + 1) / (order + 1);
+        const int istep = 2 * istep0;
+        old0 = r0; old1 = r1;
+        for (int q = lane; 2 * q < order; q += 32) {
+            const int i = istep0 - 1 + q * istep;
+            double f0, f1;
+            nfw_node(L, xsq, ysq, i, f0, f1);
+            v0[i] = f0;
+            v1[i] = f1;
+        }
+        __syncwarp();
+        double s0 = 0, s1 = 0;
+        for (int j = 0, i = istep0 - 1; j < order; j += 2, i += istep) {
+            s0 += wt[j] * v0[i];
+            s1 += wt[j] * v1[i];
+        }
+        for (int j = 1, i = istep - 1; j < order; j += 2, i += istep) {
+            s0 += wt[j] * v0[i];
+            s1 += wt[j] * v1[i];
+        }
+        if (!done0) {
+            r0 = s0;
+            if ((level > 1) && (fabs(r0 - old0) < tol * fabs(r0))) done0 = true;
+        }
+        if (!done1) {
+            r1 = s1;
+            if ((level > 1) && (fabs(r1 - old1) < tol * fabs(r1))) done1 = true;
+        }
+        __syncwarp();
+    } while (++level < QLP_PAT_LEVELS && !(done0 && done1));
+    I0 = 0.5 * r0;
+    I1 = 0.5 * r1;
+}
+
+// wbuf: null, or the calling warp's 2 QLP_PAT_N doubles for
+// nfw_integrals_warp (then all 32 lanes call with the same arguments)
+static __device__ void nfw_deflection(const LensRec& L, double x, double y, double& dx, double& dy,
+                                      double* wbuf = nullptr)
 {
     if (L.q == 1.0) {
         double kapavg = nfw_kapavg_spherical_rsq(L.ks, L.rs, x * x + y * y);
@@ -128,7 +182,8 @@ static __device__ void nfw_deflection(const LensRec& L, double x, double y, doub
         return;
     }
     double I0, I1;
-    nfw_integrals(L, x * x, y * y, L.tol, I0, I1);
+    if (wbuf) nfw_integrals_warp(L, x * x, y * y, L.tol, I0, I1, wbuf, wbuf + QLP_PAT_N);
+    else nfw_integrals(L, x * x, y * y, L.tol, I0, I1);
     const double sqe = sqrt(1 - L.epsilon);
     dx = x * (sqe * I0);
     dy = y * (sqe * I1);

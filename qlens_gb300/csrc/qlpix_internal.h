@@ -112,6 +112,9 @@ struct StaticData {            // per-context, uploaded once
     // (sqrt(C^-1) is applied to the sum): 2^fix_exp_x keeps 4 sum|psf| below
     // 2^61 (|L entries| <= 4)
     int fix_exp_x;
+    // the PSF as floats scaled by 2^fix_exp_x, x fastest: psf_fix[pl * pnx + pk]
+    // = (float)psf[pk * pny + pl] * 2^fix_exp_x (a power of two: exact)
+    const float* psf_fix;
     // F16 operands of the mixed path's SYRK: X scaled by 2^x_exp puts its
     // largest possible entry (4 sum|psf| max sqrt(C^-1)) at or below 2^14
     int x_exp;
@@ -186,7 +189,9 @@ struct Work {
     EvalParams* ep;                    // this slot's per-evaluation parameters
     // rays whose NFW deflection the surrogate hands to the quadrature (n_sub capacity)
     int* fb_ray;  double* fb_xy;  int* fb_count;
+    double* nfw_xy;                    // 2 n_sub: rays' positions on the NFW lens's plane (k_ray_pre)
     float* sur_eps;                    // n_sub: bound on each ray's source-point error on the surrogate path
+    int* xlist;  int* xcount;          // n_sub, 1: rays the surrogate path traces again exactly
     double* F0;                        // plain path, lambda optimisation: L'^T C^-1 L' before lambda R
 };
 
@@ -206,7 +211,7 @@ void launch_rowpix(const StaticData& sd, Work& w, cudaStream_t st);
 void launch_psf(const StaticData& sd, const SrcOpts& so, Work& w, int M_max, cudaStream_t st);
 void op_Ls(Work& w, int N_cap, const double* s, double* t, cudaStream_t st);
 void op_conv(const StaticData& sd, Work& w, int N_cap, bool transpose, const double* in, const double* scale_in,
-             double* out, double* img, cudaStream_t st);
+             double* out, double* img, const int2* pixT, cudaStream_t st);
 void launch_dvec(const StaticData& sd, Work& w, int N_max, cudaStream_t st);
 void launch_D(Work& w, int N_max, int M_max, cudaStream_t st);
 void launch_syrk_fp64(const StaticData& sd, Work& w, int N_max, int M_max, cudaStream_t st);

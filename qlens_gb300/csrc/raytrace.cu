@@ -23,6 +23,9 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd_, const EvalPara
     // loop would compute; used only by core-free power laws)
     __shared__ __align__(16) LensModel lm;
     __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
+    // the sub-pixel fractions u0 = (1 + 2 ii) / (2 ns) and 1 - u0, formed once
+    // per CTA by the same expressions (the same bits): no FP64 divide per ray
+    __shared__ double frac_u[SUBPIX_TAB], frac_1mu[SUBPIX_TAB];
     {
         const double* src = reinterpret_cast<const double*>(&ep->lm);
         double* dst = reinterpret_cast<double*>(&lm);
@@ -33,17 +36,16 @@ __global__ void __launch_bounds__(256) k_raytrace(StaticData sd_, const EvalPara
         const LensRec& L = lm.lens[e / SPLE_RHO_TAB];
         rho_tab[e] = (L.type == QLP_LENS_SPLE && L.kind == 2) ? sple_rho(L, e % SPLE_RHO_TAB + 1) : 0.0;
     }
-    __syncthreads();
     const int ns = sd.nsplit, nsub = sd.nsub;
+    subpix_table(ns, frac_u, frac_1mu);
+    __syncthreads();
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < sd.n_sub; t += gridDim.x * blockDim.x) {
         int m = t / nsub, k = t - m * nsub;
         int pix = sd.mpix[m];
         int i = pix / sd.ny, j = pix - i * sd.ny;
         int ii = k / ns, jj = k - ii * ns;
-        double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
-        double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
-        double px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
-        double py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
+        double px, py;
+        subpix_centre(sd, ns, ii, jj, i, j, frac_u, frac_1mu, px, py);
         double bx, by;
         find_sourcept<NFW>(lm, px, py, bx, by, rho_tab);
         spx[t] = bx;

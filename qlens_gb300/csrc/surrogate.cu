@@ -79,16 +79,43 @@ namespace qlpix {
 // ---------------------------------------------------------------------------
 // shared pieces: inputs, baseline, activation
 // ---------------------------------------------------------------------------
+// tanh(x) = 1 - 2 / (1 + e^2x), the quotient by the SFU reciprocal (within
+// 2 ulp; e^2x beyond 2^126 gives 1 exactly).  Training and inference share it.
 __device__ __forceinline__ float sur_tanh(float x)
 {
-    return 1.0f - 2.0f / (1.0f + __expf(2.0f * x));
+    return 1.0f - __fdividef(2.0f, 1.0f + __expf(2.0f * x));
 }
 
 struct SurIn {
     float f0, f1, f2;   // normalised inputs
     int bin;            // error-bound cell, -1 outside the domain
     double B;           // baseline
+    double B_rel;       // bound on B's relative error (0: FP64)
 };
+
+// The baseline B = kapavg_hat(xi^2) (ks = rs = 1) in FP32 where xi^2 >= 0.5:
+// there 2 F + log(xi^2 / 4) cancels by at most a factor 6, and FP32 sqrt,
+// atan / atanh and log (within a few ulp) keep B within SUR_B32_REL of the
+// FP64 value (measured on CPU over xi^2 in [0.5, 1e6]: 9e-7 at most).  The
+// ray adds SUR_B32_REL to its cell's error bound.  Smaller xi^2 (rays within
+// about one scale radius) keep the FP64 form, whose small-radius branch
+// cancels.
+#define SUR_B32_MIN 0.5
+#define SUR_B32_REL 5e-6
+__device__ __forceinline__ float sur_B32(float x)
+{
+    float F;
+    if (x > 1.0f) {
+        const float s = sqrtf(x - 1.0f);
+        F = atanf(s) / s;
+    } else if (x < 1.0f) {
+        const float s = sqrtf(1.0f - x);
+        F = atanhf(s) / s;
+    } else {
+        F = 1.0f;
+    }
+    return 2.0f * (2.0f * F + logf(0.25f * x)) / x;
+}
 
 __host__ __device__ __forceinline__ int sur_cell(double rho, double phi, double q)
 {
@@ -119,13 +146,15 @@ __device__ __forceinline__ SurIn sur_inputs(double X, double Y, double q)
     s.f2 = (float)fmin(fmax((q - mq) / hq, -2.0), 2.0);
     s.bin = sur_cell(rho, phi, q);
     s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, q * ax * ax + ay * ay / q);
+    s.B_rel = 0.0;
     return s;
 }
 
 // The same inputs for the ray shooting, with the network's features (log R,
 // the polar angle) in FP32 -- the network reads them in FP32 anyway -- and
-// the baseline B in FP64 (its small-radius form cancels).
-__device__ __forceinline__ SurIn sur_inputs_ray(double X, double Y, double q)
+// the baseline B in FP32 where that is accurate (sur_B32), else FP64.
+// inv_q = 1 / q.
+__device__ __forceinline__ SurIn sur_inputs_ray(double X, double Y, double q, double inv_q)
 {
     SurIn s;
     const double ax = fabs(X), ay = fabs(Y);
@@ -138,7 +167,14 @@ __device__ __forceinline__ SurIn sur_inputs_ray(double X, double Y, double q)
     s.f1 = phi * (float)(4.0 / M_PI) - 1.0f;
     s.f2 = (float)fmin(fmax((q - mq) / hq, -2.0), 2.0);
     s.bin = sur_cell((double)rho, (double)phi, q);
-    s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, q * ax * ax + ay * ay / q);
+    const double xi2 = q * ax * ax + ay * ay * inv_q;
+    if (xi2 >= SUR_B32_MIN) {
+        s.B = (double)sur_B32((float)xi2);
+        s.B_rel = SUR_B32_REL;
+    } else {
+        s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, xi2);
+        s.B_rel = 0.0;
+    }
     return s;
 }
 
@@ -419,10 +455,11 @@ __device__ __forceinline__ void tmem_st_32cols_u(uint32_t taddr, const uint32_t*
 // (a, b) -> packed F16 high parts and packed F16 remainders, a in the low half
 __device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint32_t& lo)
 {
-    const __half ah = __float2half_rn(a), bh = __float2half_rn(b);
-    const __half al = __float2half_rn(a - __half2float(ah)), bl = __float2half_rn(b - __half2float(bh));
-    hi = (uint32_t)__half_as_ushort(ah) | ((uint32_t)__half_as_ushort(bh) << 16);
-    lo = (uint32_t)__half_as_ushort(al) | ((uint32_t)__half_as_ushort(bl) << 16);
+    const __half2 h = __floats2half2_rn(a, b);              // a in the low half
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // named barrier of one warpgroup (ids 1, 2; 0 is __syncthreads)
@@ -635,13 +672,142 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_sur_infer(int n, const float
 // plane), later in k_nfw_fallback at full occupancy (its lens-frame position
 // is queued and its contribution left out here).  out->pad counts the
 // fallbacks.
+// Per-CTA tables of the ray shooting: per-lens reciprocals (a multiply per
+// ray instead of an FP64 divide), the constants of a core-free SIE, and the
+// sub-pixel fractions.  Any threads fill them; a barrier precedes their use.
+struct SurTabs {
+    double inv_rs[QLP_MAX_LENSES], inv_q[QLP_MAX_LENSES];
+    double sie_u[QLP_MAX_LENSES], sie_pre[QLP_MAX_LENSES];
+    double frac_u[SUBPIX_TAB], frac_1mu[SUBPIX_TAB];
+};
+
+__device__ __forceinline__ void sur_tabs_fill(const EvalParams* __restrict__ ep, int nsplit, SurTabs& T)
+{
+    if (threadIdx.x < QLP_MAX_LENSES && threadIdx.x < ep->lm.nlens) {
+        const LensRec& L = ep->lm.lens[threadIdx.x];
+        T.inv_rs[threadIdx.x] = (L.type == QLP_LENS_NFW) ? 1.0 / L.rs : 0.0;
+        T.inv_q[threadIdx.x] = (L.type == QLP_LENS_NFW) ? 1.0 / L.q : 0.0;
+        // SIE without core (sple_deflection kind 1, s = 0)
+        const bool sie0 = L.type == QLP_LENS_SPLE && L.kind == 1 && L.sprime == 0.0 && L.ssq == 0.0;
+        T.sie_u[threadIdx.x] = sie0 ? sqrt(1 - L.qsq) : 0.0;
+        T.sie_pre[threadIdx.x] = sie0 ? L.bprime * L.q / sqrt(1 - L.qsq) : 0.0;
+    }
+    subpix_table(nsplit, T.frac_u, T.frac_1mu);
+}
+
+// sub-pixel t's centre
+__device__ __forceinline__ void sur_ray_pos(const StaticData& sd, const SurTabs& T, int t, double& px, double& py)
+{
+    const int ns = sd.nsplit, nsub = sd.nsub;
+    const int m = t / nsub, k = t - m * nsub;
+    const int pix = sd.mpix[m];
+    const int i = pix / sd.ny, j = pix - i * sd.ny;
+    const int ii = k / ns, jj = k - ii * ns;
+    subpix_centre(sd, ns, ii, jj, i, j, T.frac_u, T.frac_1mu, px, py);
+}
+
+// SPLE_Lens::deflection_elliptical_iso with s = 0 (T.sie_u[k] != 0): both
+// components share the reciprocal u / psi
+__device__ __forceinline__ void sur_sie0(const LensRec& L, const SurTabs& T, int k, double xi, double yi,
+                                         double& ax, double& ay)
+{
+    double x = xi - L.xc, y = yi - L.yc;
+    const bool rot = (L.sintheta != 0);
+    if (rot) {
+        const double xp = x * L.costheta + y * L.sintheta;
+        y = -x * L.sintheta + y * L.costheta;
+        x = xp;
+    }
+    const double r = T.sie_u[k] / sqrt(L.qsq * x * x + y * y);
+    double bx = T.sie_pre[k] * atan(x * r), by = T.sie_pre[k] * atanh(y * r);
+    if (rot) {
+        const double xp = bx * L.costheta - by * L.sintheta;
+        by = bx * L.sintheta + by * L.costheta;
+        bx = xp;
+    }
+    ax = bx; ay = by;
+}
+
+// The deflection of NFW lens k at (xi, yi) on its plane through the
+// surrogate, for the 128 rays of a warpgroup (every thread calls, converged;
+// `valid` false for padding rays).  LensProfile::deflection's shift, rotate,
+// deflect, rotate back.  A ray that fails the gate takes the quadrature
+// inline, or, for the deferred lens, is queued for k_nfw_fallback (deflection
+// 0 here).  Adds the ray's error bound to eps (twice the plane factor times
+// |alpha| times the relative bound) and counts fallbacks in fb.
+struct SurRayOut {
+    int* fb_count; int* fb_ray; double* fb_xy;
+};
+
+__device__ __forceinline__ void sur_nfw(SurWG& S, bool& ok, const LensRec& L, int k, const SurTabs& T,
+                                        const float* __restrict__ bound, double thresh, double zabs, bool valid,
+                                        int t, int defer_lens, const SurRayOut& q, int& fb, double& eps,
+                                        double xi, double yi, double& ax, double& ay)
+{
+    double x = xi - L.xc, y = yi - L.yc;
+    const bool rot = (L.sintheta != 0);
+    if (rot) {
+        const double xp = x * L.costheta + y * L.sintheta;
+        y = -x * L.sintheta + y * L.costheta;
+        x = xp;
+    }
+    const SurIn in = sur_inputs_ray(x * T.inv_rs[k], y * T.inv_rs[k], L.q, T.inv_q[k]);
+    const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
+    // the cell's bound on the relative error of G, plus B's
+    const double bnd = (in.bin >= 0) ? (double)bound[in.bin] + in.B_rel : 0.0;
+    // before the network: |alpha| ~ ks B |(x, y)| (G is within a few tens of
+    // percent of B), so a group none of whose rays can pass the gate skips
+    // the network and sends every ray to the quadrature (the gates compare
+    // squares: no FP64 square root)
+    const double gb = L.ks * in.B * bnd;
+    const bool maybe = valid && !centre && in.bin >= 0 && gb * gb * (x * x + y * y) <= 2.25 * thresh * thresh;
+    double bx = 0, by = 0;
+    bool use = false;
+    if (wg_any(S.wg, maybe)) {
+        float t0, t1;
+        sur_mlp_wg(S, in.f0, in.f1, in.f2, t0, t1, ok);
+        const float oq = (float)(1.0 - L.q);
+        const double G0 = in.B * (double)expf(oq * t0), G1 = in.B * (double)expf(oq * t1);
+        bx = x * L.ks * G0;
+        by = y * L.ks * G1;
+        const double m2 = bx * bx + by * by;
+        use = ok && !centre && in.bin >= 0 && m2 * bnd * bnd <= thresh * thresh;
+        // |alpha| in FP32, rounded up by far more than its error
+        if (use) eps += 2.0 * zabs * (double)(sqrtf((float)m2) * 1.000001f) * bnd;
+    }
+    if (!use && valid) {
+        fb++;
+        if (k == defer_lens) {
+            const int e = atomicAdd(q.fb_count, 1);
+            q.fb_ray[e] = t;
+            q.fb_xy[2 * (size_t)e] = x;
+            q.fb_xy[2 * (size_t)e + 1] = y;
+            bx = 0; by = 0;
+        } else {
+            nfw_deflection(L, x, y, bx, by);
+        }
+    }
+    if (rot) {
+        const double xp = bx * L.costheta - by * L.sintheta;
+        by = bx * L.sintheta + by * L.costheta;
+        bx = xp;
+    }
+    ax = bx; ay = by;
+}
+
+// PRE = false: the whole lens equation per ray (any model).  PRE = true: the
+// model has one NFW lens (defer_lens) on the last plane and k_ray_pre has
+// already traced every other lens: spx/spy hold the source points without
+// that lens's deflection and nfw_xy the rays' positions on its plane, so
+// this kernel runs only the surrogate and subtracts its deflection.
+template <bool PRE>
 __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_, const EvalParams* __restrict__ ep,
                                                                  double* __restrict__ spx, double* __restrict__ spy,
+                                                                 const double* __restrict__ nfw_xy,
                                                                  const unsigned char* __restrict__ wimg,
                                                                  const float* __restrict__ small_g,
                                                                  const float* __restrict__ bound, double thresh,
-                                                                 int defer_lens, int* __restrict__ fb_count,
-                                                                 int* __restrict__ fb_ray, double* __restrict__ fb_xy,
+                                                                 int defer_lens, SurRayOut q,
                                                                  float* __restrict__ sur_eps, GridState* gs,
                                                                  EvalOut* out)
 {
@@ -651,6 +817,7 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
     __shared__ __align__(16) LensModel lm;
+    __shared__ SurTabs T;
     __shared__ int n_fb;
     if ((int)blockIdx.x * 2 * 128 >= sd.n_sub) return;     // launched for the slot's capacity
     {
@@ -658,6 +825,7 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
         double* dst = reinterpret_cast<double*>(&lm);
         for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
         if (threadIdx.x == 0) n_fb = 0;
+        sur_tabs_fill(ep, sd.nsplit, T);     // (sur_cta_begin's barrier orders these with their readers)
     }
     SurWG S;
     bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag);
@@ -667,24 +835,35 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
         if (wg_any(S.wg, !ok || abort_flag)) { ok = false; break; }
         const int t = grp * 128 + tid;
         const bool valid = t < sd.n_sub;
-        double px = 0, py = 0;
-        if (valid) {
-            const int ns = sd.nsplit, nsub = sd.nsub;
-            const int m = t / nsub, k = t - m * nsub;
-            const int pix = sd.mpix[m];
-            const int i = pix / sd.ny, j = pix - i * sd.ny;
-            const int ii = k / ns, jj = k - ii * ns;
-            const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
-            const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
-            px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
-            py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
+        // bound on this ray's source-point error against the plain path:
+        // rounding (this unit contracts multiply-adds, and deflections are
+        // summed in another order) plus, per surrogate deflection, twice its
+        // plane factor times its bound
+        double eps = 1e-12;
+        if (PRE) {
+            const LensRec& L = lm.lens[defer_lens];
+            const double z = lm.zfac[L.plane];
+            double xi = 0, yi = 0, sx = 0, sy = 0;
+            if (valid) {
+                xi = nfw_xy[2 * (size_t)t];
+                yi = nfw_xy[2 * (size_t)t + 1];
+                sx = spx[t];
+                sy = spy[t];
+            }
+            double ax, ay;
+            sur_nfw(S, ok, L, defer_lens, T, bound, thresh, fabs(z), valid, t, defer_lens, q, fb, eps, xi, yi,
+                    ax, ay);
+            if (valid) {
+                spx[t] = sx - z * ax;
+                spy[t] = sy - z * ay;
+                sur_eps[t] = (float)eps;
+            }
+            continue;
         }
+        double px = 0, py = 0;
+        if (valid) sur_ray_pos(sd, T, t, px, py);
         double defx = 0, defy = 0;
         double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
-        // bound on this ray's source-point error against the plain path:
-        // rounding (a deferred fallback is subtracted in another order) plus,
-        // per surrogate deflection, twice its plane factor times its bound
-        double eps = 1e-12;
         for (int p = 0; p < lm.n_planes; p++) {
             dsx[p] = 0; dsy[p] = 0;
             if (lm.zfac[p] == 0.0) continue;
@@ -697,56 +876,13 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
                 const LensRec& L = lm.lens[k];
                 if (L.plane != p) continue;
                 double ax, ay;
-                if (L.type == QLP_LENS_NFW && L.q != 1.0) {
-                    // LensProfile::deflection: shift, rotate, deflect, rotate back
-                    double x = xi - L.xc, y = yi - L.yc;
-                    const bool rot = (L.sintheta != 0);
-                    if (rot) {
-                        const double xp = x * L.costheta + y * L.sintheta;
-                        y = -x * L.sintheta + y * L.costheta;
-                        x = xp;
-                    }
-                    const SurIn in = sur_inputs_ray(x / L.rs, y / L.rs, L.q);
-                    const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
-                    // before the network: |alpha| ~ ks B |(x, y)| (G is within a few
-                    // tens of percent of B), so a group none of whose rays can pass
-                    // the gate skips the network and sends every ray to the quadrature
-                    const bool maybe = valid && !centre && in.bin >= 0 &&
-                                       L.ks * in.B * sqrt(x * x + y * y) * (double)bound[in.bin] <= 1.5 * thresh;
-                    double bx = 0, by = 0;
-                    bool use = false;
-                    if (wg_any(S.wg, maybe)) {
-                        float t0, t1;
-                        sur_mlp_wg(S, in.f0, in.f1, in.f2, t0, t1, ok);
-                        const float oq = (float)(1.0 - L.q);
-                        const double G0 = in.B * (double)expf(oq * t0), G1 = in.B * (double)expf(oq * t1);
-                        bx = x * L.ks * G0;
-                        by = y * L.ks * G1;
-                        const double mag = sqrt(bx * bx + by * by);
-                        use = ok && !centre && in.bin >= 0 && mag * (double)bound[in.bin] <= thresh;
-                        if (use) eps += 2.0 * fabs(lm.zfac[p]) * mag * (double)bound[in.bin];
-                    }
-                    if (!use && valid) {
-                        fb++;
-                        if (k == defer_lens) {
-                            const int e = atomicAdd(fb_count, 1);
-                            fb_ray[e] = t;
-                            fb_xy[2 * (size_t)e] = x;
-                            fb_xy[2 * (size_t)e + 1] = y;
-                            bx = 0; by = 0;
-                        } else {
-                            nfw_deflection(L, x, y, bx, by);
-                        }
-                    }
-                    if (rot) {
-                        const double xp = bx * L.costheta - by * L.sintheta;
-                        by = bx * L.sintheta + by * L.costheta;
-                        bx = xp;
-                    }
-                    ax = bx; ay = by;
-                } else {
+                if (L.type == QLP_LENS_NFW && L.q != 1.0)
+                    sur_nfw(S, ok, L, k, T, bound, thresh, fabs(lm.zfac[p]), valid, t, defer_lens, q, fb, eps, xi,
+                            yi, ax, ay);
+                else if (T.sie_u[k] != 0.0)
+                    sur_sie0(L, T, k, xi, yi, ax, ay);
+                else
                     lens_deflection<true>(L, xi, yi, ax, ay);
-                }
                 dsx[p] += ax; dsy[p] += ay;
             }
             dsx[p] *= lm.zfac[p];
@@ -768,52 +904,25 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
     }
 }
 
-// ---------------------------------------------------------------------------
-// Exact rays where the grid decides.  QLens's likelihood is not continuous in
-// the source points: which cells a sub-pixel maps to changes at cell edges
-// and at the lines through cell centres (SourcePixelGrid::
-// assign_source_mapping_flags_interpolate, pixelgrid.cpp:2343-2432), and
-// the grid itself is laid out from the extremes of the per-pixel mean source
-// points (find_optimal_sourcegrid, pixelgrid.cpp:10998-11080).  A ray moved
-// by the surrogate's error across such a line changes L by a finite step.
-// So every ray whose error bound (sur_eps) reaches a decision is traced again
-// with the plain path's own code (find_sourcept with the quadrature,
-// lens_device.cuh; this file is compiled with --fmad=false like
-// raytrace.cu), which gives the plain path's bits:
-//   k_sur_exact_extremes  after a first grid: the rays of every pixel whose
-//                         mean could be an extreme (within twice the largest
-//                         bound); the grid is then laid out again and its
-//                         extremes are the plain path's;
-//   k_sur_exact_cells     after the final grid: every ray within its bound of
-//                         a cell edge, a centre line or the grid's border.
-// Afterwards the cells of every sub-pixel, the active set and L's sparsity
-// are the plain path's; only the weights move, continuously.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void sur_exact_ray(const StaticData& sd, const LensModel& lm, const double* rho_tab,
-                                              int t, double* spx, double* spy)
+// The FP64 part of the rays of a model whose one NFW lens (nfw_lens) sits on
+// the last plane: every other lens of every plane, a thread per ray at full
+// occupancy (GB300's FP64 pipe needs many warps in flight; the fused kernel
+// holds eight per SM).  Writes the source points without the NFW lens's
+// deflection and the rays' positions on its plane (nfw_xy) for
+// k_raytrace_sur<true>.
+__global__ void __launch_bounds__(256) k_ray_pre(StaticData sd_, const EvalParams* __restrict__ ep, int nfw_lens,
+                                                 double* __restrict__ spx, double* __restrict__ spy,
+                                                 double* __restrict__ nfw_xy)
 {
-    const int ns = sd.nsplit, nsub = sd.nsub;
-    const int m = t / nsub, k = t - m * nsub;
-    const int pix = sd.mpix[m];
-    const int i = pix / sd.ny, j = pix - i * sd.ny;
-    const int ii = k / ns, jj = k - ii * ns;
-    const double u0 = ((double)(1 + 2 * ii)) / (2 * ns);
-    const double w0 = ((double)(1 + 2 * jj)) / (2 * ns);
-    const double px = (1 - u0) * sd.xvals[i] + u0 * sd.xvals[i + 1];
-    const double py = (1 - w0) * sd.yvals[j] + w0 * sd.yvals[j + 1];
-    double bx, by;
-    find_sourcept<true>(lm, px, py, bx, by, rho_tab);
-    spx[t] = bx;
-    spy[t] = by;
-}
-
-// the lens model and the power-law coefficients in shared memory, as k_raytrace stages them
-__device__ __forceinline__ void sur_stage_model(const EvalParams* __restrict__ ep, LensModel& lm, double* rho_tab)
-{
+    const StaticData sd = eval_shape(sd_);
+    __shared__ __align__(16) LensModel lm;
+    __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
+    __shared__ SurTabs T;
     {
         const double* src = reinterpret_cast<const double*>(&ep->lm);
         double* dst = reinterpret_cast<double*>(&lm);
         for (int k = threadIdx.x; k < (int)(sizeof(LensModel) / sizeof(double)); k += blockDim.x) dst[k] = src[k];
+        sur_tabs_fill(ep, sd.nsplit, T);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < lm.nlens * SPLE_RHO_TAB; e += blockDim.x) {
@@ -821,110 +930,39 @@ __device__ __forceinline__ void sur_stage_model(const EvalParams* __restrict__ e
         rho_tab[e] = (L.type == QLP_LENS_SPLE && L.kind == 2) ? sple_rho(L, e % SPLE_RHO_TAB + 1) : 0.0;
     }
     __syncthreads();
-}
-
-__global__ void __launch_bounds__(256) k_sur_exact_extremes(StaticData sd_, SrcOpts so, const EvalParams* __restrict__ ep,
-                                                            double* __restrict__ spx, double* __restrict__ spy,
-                                                            float* __restrict__ sur_eps, const GridState* gs,
-                                                            double eps_g, int* __restrict__ n_exact)
-{
-    const StaticData sd = eval_shape(sd_);
-    __shared__ __align__(16) LensModel lm;
-    __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
-    sur_stage_model(ep, lm, rho_tab);
-    const int nsub = sd.nsub;
-    const bool use_nt = so.noise_threshold > 0;
-    const double e0 = gs->ext[0], e1 = gs->ext[1], e2 = gs->ext[2], e3 = gs->ext[3];
-    int cnt = 0;
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
-        if (use_nt) {
-            const int pix = sd.mpix[m];
-            if (sd.data[pix] <= so.noise_threshold * sqrt(1.0 / sd.covinv[pix])) continue;
-        }
-        double xs = 0, ys = 0;
-        float emax = 0.f;
-        for (int k = 0; k < nsub; k++) {
-            xs += spx[m * nsub + k];
-            ys += spy[m * nsub + k];
-            emax = fmaxf(emax, sur_eps[m * nsub + k]);
-        }
-        if (emax == 0.f) continue;
-        xs /= nsub; ys /= nsub;
-        const double tol = 2.0 * eps_g;
-        const bool near = fabs(xs - e0) <= tol || fabs(xs - e1) <= tol || fabs(ys - e2) <= tol || fabs(ys - e3) <= tol;
-        if (!near) continue;
-        for (int k = 0; k < nsub; k++) {
-            sur_exact_ray(sd, lm, rho_tab, m * nsub + k, spx, spy);
-            sur_eps[m * nsub + k] = 0.f;
-        }
-        cnt += nsub;
-    }
-    if (cnt) atomicAdd(n_exact, cnt);
-}
-
-// distance from v to the decision lines of one axis: the grid's border when
-// outside it, else the edges of its cell and the line through its centre
-__device__ __forceinline__ double sur_axis_margin(double v, const double* c, const double* cc, int n)
-{
-    if (!(v >= c[0] && v < c[n])) return fmin(fabs(v - c[0]), fabs(v - c[n]));
-    int lo = 0, hi = n - 1;
-    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (c[mid] <= v) lo = mid; else hi = mid - 1; }
-    return fmin(fmin(v - c[lo], c[lo + 1] - v), fabs(v - cc[lo]));
-}
-
-__global__ void __launch_bounds__(256) k_sur_exact_cells(StaticData sd_, SrcOpts so_, const EvalParams* __restrict__ ep,
-                                                         double* __restrict__ spx, double* __restrict__ spy,
-                                                         float* __restrict__ sur_eps, const double* __restrict__ cx_g,
-                                                         const double* __restrict__ cy_g,
-                                                         const double* __restrict__ ccx_g,
-                                                         const double* __restrict__ ccy_g, int* __restrict__ n_exact)
-{
-    extern __shared__ double sm[];
-    const StaticData sd = eval_shape(sd_);
-    const SrcOpts so = eval_grid(so_, sd_);
-    __shared__ __align__(16) LensModel lm;
-    __shared__ double rho_tab[QLP_MAX_LENSES * SPLE_RHO_TAB];
-    const int snx = so.snx, sny = so.sny;
-    double* cx = sm;
-    double* cy = cx + snx + 1;
-    double* ccx = cy + sny + 1;
-    double* ccy = ccx + snx;
-    for (int i = threadIdx.x; i <= snx; i += blockDim.x) cx[i] = cx_g[i];
-    for (int j = threadIdx.x; j <= sny; j += blockDim.x) cy[j] = cy_g[j];
-    for (int i = threadIdx.x; i < snx; i += blockDim.x) ccx[i] = ccx_g[i];
-    for (int j = threadIdx.x; j < sny; j += blockDim.x) ccy[j] = ccy_g[j];
-    sur_stage_model(ep, lm, rho_tab);
-    int cnt = 0;
+    const int P = lm.lens[nfw_lens].plane;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < sd.n_sub; t += gridDim.x * blockDim.x) {
-        const double e = sur_eps[t];
-        if (e == 0.0) continue;
-        const double dx = sur_axis_margin(spx[t], cx, ccx, snx), dy = sur_axis_margin(spy[t], cy, ccy, sny);
-        if (dx <= e || dy <= e || dx != dx || dy != dy) {
-            sur_exact_ray(sd, lm, rho_tab, t, spx, spy);
-            sur_eps[t] = 0.f;
-            cnt++;
+        double px, py;
+        sur_ray_pos(sd, T, t, px, py);
+        double defx = 0, defy = 0, xP = px, yP = py;
+        double dsx[QLP_MAX_PLANES], dsy[QLP_MAX_PLANES];
+        for (int p = 0; p < lm.n_planes; p++) {
+            dsx[p] = 0; dsy[p] = 0;
+            if (lm.zfac[p] == 0.0) continue;
+            double xi = px, yi = py;
+            for (int jp = 0; jp < p; jp++) {
+                xi -= lm.beta[p - 1][jp] * dsx[jp];
+                yi -= lm.beta[p - 1][jp] * dsy[jp];
+            }
+            if (p == P) { xP = xi; yP = yi; }
+            for (int k = 0; k < lm.nlens; k++) {
+                const LensRec& L = lm.lens[k];
+                if (L.plane != p || k == nfw_lens) continue;
+                double ax, ay;
+                if (T.sie_u[k] != 0.0) sur_sie0(L, T, k, xi, yi, ax, ay);
+                else lens_deflection<false>(L, xi, yi, ax, ay, rho_tab + k * SPLE_RHO_TAB);
+                dsx[p] += ax; dsy[p] += ay;
+            }
+            dsx[p] *= lm.zfac[p];
+            dsy[p] *= lm.zfac[p];
+            defx += dsx[p];
+            defy += dsy[p];
         }
+        spx[t] = px - defx;
+        spy[t] = py - defy;
+        nfw_xy[2 * (size_t)t] = xP;
+        nfw_xy[2 * (size_t)t + 1] = yP;
     }
-    if (cnt) atomicAdd(n_exact, cnt);
-}
-
-int launch_surrogate_exact(const StaticData& sd, const SrcOpts& so, Work& w, double eps_g, int step,
-                           cudaStream_t st)
-{
-    if (sd.n_sub == 0) return QLP_OK;
-    if (step == 0) {
-        if (!so.auto_grid) return QLP_OK;
-        const int blocks = std::max(1, std::min((sd.n_mask + 255) / 256, 152 * 8));
-        k_sur_exact_extremes<<<blocks, 256, 0, st>>>(sd, so, w.ep, w.spx, w.spy, w.sur_eps, w.gs, eps_g,
-                                                      &w.out->n_exact);
-    } else {
-        const size_t smem = sizeof(double) * (2 * (so.snx + so.sny) + 2);
-        const int blocks = std::max(1, std::min((sd.n_sub + 255) / 256, 152 * 16));
-        k_sur_exact_cells<<<blocks, 256, smem, st>>>(sd, so, w.ep, w.spx, w.spy, w.sur_eps, w.cx, w.cy, w.ccx,
-                                                     w.ccy, &w.out->n_exact);
-    }
-    count_launches(1);
-    return QLP_OK;
 }
 
 // The queued fallbacks of k_raytrace_sur: quadrature deflection of lens
@@ -1229,7 +1267,8 @@ int surrogate_train(int device, const qlp_surrogate_opts* o, qlp_surrogate_repor
     }
     SCK(cudaStreamSynchronize(s));
     SCK(cudaFuncSetAttribute(k_sur_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
-    SCK(cudaFuncSetAttribute(k_raytrace_sur, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
+    SCK(cudaFuncSetAttribute(k_raytrace_sur<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
+    SCK(cudaFuncSetAttribute(k_raytrace_sur<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SUR_SMEM));
     k_sur_infer<<<sur_grid(nval), SUR_THREADS, SUR_SMEM, s>>>(nval, Xv, Tnet, st.wimg, st.small, dstatus);
     k_sur_bound<<<(SUR_NBINS + 255) / 256, 256, 0, s>>>(SUR_NBINS, Tnet, Gv, Bv, Qv, st.bound, stats);
     SCK(cudaGetLastError());
@@ -1383,11 +1422,20 @@ int launch_raytrace_sur(const StaticData& sd, Work& w, double thresh, int defer_
     }
     SurState& S = g_sur[dev];
     cudaMemsetAsync(w.fb_count, 0, sizeof(int), st);
-    k_raytrace_sur<<<sur_grid(sd.n_sub), SUR_THREADS, SUR_SMEM, st>>>(sd, w.ep, w.spx, w.spy, S.wimg, S.small,
-                                                                       S.bound,
-                                                                   thresh, defer_lens, w.fb_count, w.fb_ray,
-                                                                   w.fb_xy, w.sur_eps, w.gs, w.out);
+    const SurRayOut q{w.fb_count, w.fb_ray, w.fb_xy};
     int n = 1;
+    if (defer_lens >= 0) {
+        // one NFW lens, on the last plane: the other lenses first, at full occupancy
+        k_ray_pre<<<(sd.n_sub + 255) / 256, 256, 0, st>>>(sd, w.ep, defer_lens, w.spx, w.spy, w.nfw_xy);
+        k_raytrace_sur<true><<<sur_grid(sd.n_sub), SUR_THREADS, SUR_SMEM, st>>>(
+            sd, w.ep, w.spx, w.spy, w.nfw_xy, S.wimg, S.small, S.bound, thresh, defer_lens, q, w.sur_eps, w.gs,
+            w.out);
+        n++;
+    } else {
+        k_raytrace_sur<false><<<sur_grid(sd.n_sub), SUR_THREADS, SUR_SMEM, st>>>(
+            sd, w.ep, w.spx, w.spy, nullptr, S.wimg, S.small, S.bound, thresh, defer_lens, q, w.sur_eps, w.gs,
+            w.out);
+    }
     if (defer_lens >= 0) {
         const int blocks = std::min((sd.n_sub + 255) / 256, 152 * 8);
         k_nfw_fallback<<<blocks, 256, 0, st>>>(w.ep, defer_lens, w.fb_count, w.fb_ray, w.fb_xy, w.spx, w.spy);
