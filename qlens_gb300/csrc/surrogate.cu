@@ -418,15 +418,20 @@ __global__ void k_sur_adam(int n, float* __restrict__ p, const float* __restrict
 //   A (activations): in TMEM, two F16 per 32-bit column (even k in the low
 //     half), hi and lo 64 columns each;
 //   D: 128 FP32 columns of TMEM.
-// Persistent CTAs, one per SM, two warpgroups: each owns 256 TMEM columns
-// (D | A_hi | A_lo) and runs 128-ray groups of its own, so one warpgroup's
-// epilogue and FP64 lens work overlap the other's MMAs.
+// Persistent CTAs, one per SM, two ray groups of 256 threads (8 warps): each
+// owns 256 TMEM columns (D | A_hi | A_lo) and runs 128-ray groups of its
+// own, so one group's epilogues and FP64 lens work overlap the other's MMAs.
+// Two threads share a ray (warps w and w + 4 of a group read the same TMEM
+// lane quadrant): each runs the epilogues of half the hidden units, which
+// doubles the warps on the SIMT-bound epilogues (tanh, the F16 split, TMEM
+// loads and stores) for the same TMEM.
 #define SUR_SMALL (3 * SUR_H + 4 * SUR_H + 2 * SUR_H + 2 + 3)   // W0, b0..b3, W4, b4, unscale of layers 1..3
 #define SUR_OPB (SUR_H * SUR_H * 2)                              // one F16 part of one layer: 32 KB
 #define SUR_WIMG (3 * 2 * SUR_OPB)                               // 192 KB
 #define SUR_ACT_EXP 14
 #define SUR_SMEM (SUR_WIMG + 1024 + SUR_SMALL * 4)
-#define SUR_THREADS 256
+#define SUR_THREADS 512
+#define SUR_RG 256                                               // threads of a ray group
 
 __device__ __forceinline__ void mma_f16_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
                                            uint32_t acc)
@@ -436,6 +441,16 @@ __device__ __forceinline__ void mma_f16_ta(uint32_t tmem_d, uint32_t tmem_a, uin
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
         "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_16cols_u(uint32_t taddr, const uint32_t* v)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
         : "memory");
 }
 
@@ -462,17 +477,17 @@ __device__ __forceinline__ void f16_split2(float a, float b, uint32_t& hi, uint3
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-// named barrier of one warpgroup (ids 1, 2; 0 is __syncthreads)
-__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+// named barrier of one ray group (ids 1, 2; 0 is __syncthreads)
+__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 256;" ::"r"(1 + wg) : "memory"); }
 
-// true on every thread of the warpgroup if p holds on any of them
+// true on every thread of the ray group if p holds on any of them
 __device__ __forceinline__ bool wg_any(int wg, bool p)
 {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred pi, po;\n\t"
         "setp.ne.u32 pi, %1, 0;\n\t"
-        "bar.red.or.pred po, %2, 128, pi;\n\t"
+        "bar.red.or.pred po, %2, 256, pi;\n\t"
         "selp.u32 %0, 1, 0, po;\n\t}"
         : "=r"(r)
         : "r"((uint32_t)p), "r"(1 + wg)
@@ -480,24 +495,28 @@ __device__ __forceinline__ bool wg_any(int wg, bool p)
     return r != 0;
 }
 
-// Per-warpgroup state of the tensor-core MLP.
+// Per-ray-group state of the tensor-core MLP.
 struct SurWG {
     const unsigned char* w;   // weight image in shared memory (1024-aligned)
     const float* small;       // SUR_SMALL floats in shared memory
-    uint64_t* mma_bar;        // this warpgroup's MMA-completion barrier
+    uint64_t* mma_bar;        // this group's MMA-completion barrier
     volatile int* abort;
-    uint32_t tmem;            // this warpgroup's columns: D [0,128), A_hi [128,192), A_lo [192,256)
+    float2* xo;               // this group's [2 halves][128 rays] partial outputs
+    float4* xin;              // this group's [128 rays] network inputs (the first half's, for the second)
+    uint32_t tmem;            // this group's columns: D [0,128), A_hi [128,192), A_lo [192,256)
     uint32_t phase;           // completed layers (mbarrier parity)
-    int wg;
+    int wg;                   // ray group
+    int half;                 // hidden units [64 half, 64 half + 64) of the thread's ray
 };
 
-// The 128 threads of a warpgroup call this together, each with its ray's
-// inputs; returns the network's two outputs.  ok is cleared if a bounded wait
-// ran out.
+// The 256 threads of a ray group call this together, two per ray (row
+// threadIdx.x % 128), each with its ray's inputs; both return the network's
+// two outputs.  ok is cleared if a bounded wait ran out.
 __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, float& t1, bool& ok)
 {
     const int tid = threadIdx.x & 127, warp = tid >> 5;
     const uint32_t row = S.tmem + (((uint32_t)(warp * 32)) << 16);   // this warp's 32 lanes
+    const int u0 = 64 * S.half;                                        // this thread's hidden units
     const float* W0 = S.small;
     const float* bb = S.small + 3 * SUR_H;          // b0, b1, b2, b3
     const float* W4 = S.small + 7 * SUR_H;
@@ -506,10 +525,10 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
     const float ascale = (float)(1 << SUR_ACT_EXP);
     // layer 0 on the CUDA cores, straight into TMEM as the next A operand
     #pragma unroll 1
-    for (int c = 0; c < SUR_H; c += 64) {
-        uint32_t hi[32], lo[32];
+    for (int c = u0; c < u0 + 64; c += 32) {
+        uint32_t hi[16], lo[16];
         #pragma unroll
-        for (int j = 0; j < 32; j++) {
+        for (int j = 0; j < 16; j++) {
             const int u = c + 2 * j;
             const float h0 = sur_tanh(
                 __fmaf_rn(W0[2 * SUR_H + u], f2, __fmaf_rn(W0[SUR_H + u], f1, __fmaf_rn(W0[u], f0, bb[u]))));
@@ -517,8 +536,8 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
                                                 __fmaf_rn(W0[SUR_H + u + 1], f1, __fmaf_rn(W0[u + 1], f0, bb[u + 1]))));
             f16_split2(h0 * ascale, h1 * ascale, hi[j], lo[j]);
         }
-        tmem_st_32cols_u(row + 128 + c / 2, hi);
-        tmem_st_32cols_u(row + 192 + c / 2, lo);
+        tmem_st_16cols_u(row + 128 + c / 2, hi);
+        tmem_st_16cols_u(row + 192 + c / 2, lo);
     }
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     float o0 = 0.f, o1 = 0.f;
@@ -526,7 +545,7 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
         tc_fence_before();
         wg_sync(S.wg);
         tc_fence_after();
-        if (tid == 0) {
+        if ((threadIdx.x & (SUR_RG - 1)) == 0) {
             const uint32_t idesc = idesc_f16_128x128();
             const unsigned char* wl = S.w + (size_t)(l - 1) * 2 * SUR_OPB;
             #pragma unroll
@@ -554,21 +573,20 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
         const float us = unscale[l - 1];
         const float* bl = bb + l * SUR_H;
         #pragma unroll 1
-        for (int c = 0; c < SUR_H; c += 64) {
-            float v[64];
+        for (int c = u0; c < u0 + 64; c += 32) {
+            float v[32];
             tmem_ld_32cols(row + c, v);
-            tmem_ld_32cols(row + c + 32, v + 32);
             #pragma unroll
-            for (int j = 0; j < 64; j++) v[j] = sur_tanh(__fmaf_rn(v[j], us, bl[c + j]));
+            for (int j = 0; j < 32; j++) v[j] = sur_tanh(__fmaf_rn(v[j], us, bl[c + j]));
             if (l < 3) {
-                uint32_t hi[32], lo[32];
+                uint32_t hi[16], lo[16];
                 #pragma unroll
-                for (int j = 0; j < 32; j++) f16_split2(v[2 * j] * ascale, v[2 * j + 1] * ascale, hi[j], lo[j]);
-                tmem_st_32cols_u(row + 128 + c / 2, hi);
-                tmem_st_32cols_u(row + 192 + c / 2, lo);
+                for (int j = 0; j < 16; j++) f16_split2(v[2 * j] * ascale, v[2 * j + 1] * ascale, hi[j], lo[j]);
+                tmem_st_16cols_u(row + 128 + c / 2, hi);
+                tmem_st_16cols_u(row + 192 + c / 2, lo);
             } else {
                 #pragma unroll
-                for (int j = 0; j < 64; j++) {
+                for (int j = 0; j < 32; j++) {
                     o0 = __fmaf_rn(v[j], W4[2 * (c + j)], o0);
                     o1 = __fmaf_rn(v[j], W4[2 * (c + j) + 1], o1);
                 }
@@ -576,8 +594,12 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     }
-    t0 = o0 + b4[0];
-    t1 = o1 + b4[1];
+    // the two halves' output sums, added in the same order on both threads
+    S.xo[S.half * 128 + tid] = make_float2(o0, o1);
+    wg_sync(S.wg);
+    const float2 a = S.xo[tid], b = S.xo[128 + tid];
+    t0 = (a.x + b.x) + b4[0];
+    t1 = (a.y + b.y) + b4[1];
 }
 
 // CTA set-up of the persistent MLP kernels (all SUR_THREADS threads): the
@@ -586,11 +608,11 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
 // within the bounded wait.
 __device__ __forceinline__ bool sur_cta_begin(SurWG& S, unsigned char* smem_raw, const unsigned char* __restrict__ wimg,
                                               const float* __restrict__ small_g, uint64_t* w_bar, uint64_t* mma_bar,
-                                              uint32_t* tmem_slot, volatile int* abort)
+                                              uint32_t* tmem_slot, volatile int* abort, float2* xo)
 {
     unsigned char* w = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     float* small = reinterpret_cast<float*>(w + SUR_WIMG);
-    const int wg = threadIdx.x >> 7;
+    const int wg = threadIdx.x / SUR_RG;
     if (threadIdx.x == 0) {
         mbar_init(w_bar, 1);
         mbar_init(&mma_bar[0], 1);
@@ -622,6 +644,9 @@ __device__ __forceinline__ bool sur_cta_begin(SurWG& S, unsigned char* smem_raw,
     S.tmem = *tmem_slot + (uint32_t)(wg * 256);
     S.phase = 0;
     S.wg = wg;
+    S.half = (threadIdx.x >> 7) & 1;
+    S.xo = xo + wg * 256;
+    S.xin = reinterpret_cast<float4*>(xo + 2 * 256) + wg * 128;
     return mbar_wait_bounded(w_bar, 0, abort, false);
 }
 
@@ -646,8 +671,9 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_sur_infer(int n, const float
     __shared__ uint64_t w_bar, mma_bar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ volatile int abort_flag;
+    __shared__ float2 xo[2 * 256 + 2 * 2 * 128];   // partial outputs, then the inputs
     SurWG S;
-    bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag);
+    bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag, xo);
     const int tid = threadIdx.x & 127;
     for (int grp = blockIdx.x * 2 + S.wg; grp * 128 < n; grp += gridDim.x * 2) {
         if (wg_any(S.wg, !ok || abort_flag)) { ok = false; break; }
@@ -656,7 +682,7 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_sur_infer(int n, const float
         if (i < n) { f0 = X[3 * (size_t)i]; f1 = X[3 * (size_t)i + 1]; f2 = X[3 * (size_t)i + 2]; }
         float t0, t1;
         sur_mlp_wg(S, f0, f1, f2, t0, t1, ok);
-        if (i < n) { T[2 * (size_t)i] = t0; T[2 * (size_t)i + 1] = t1; }
+        if (i < n && S.half == 0) { T[2 * (size_t)i] = t0; T[2 * (size_t)i + 1] = t1; }
     }
     if (!ok && tid == 0) atomicExch(status, QLP_ERR_TIMEOUT);
     sur_cta_end(S, tmem_slot);
@@ -744,37 +770,57 @@ __device__ __forceinline__ void sur_nfw(SurWG& S, bool& ok, const LensRec& L, in
                                         int t, int defer_lens, const SurRayOut& q, int& fb, double& eps,
                                         double xi, double yi, double& ax, double& ay)
 {
-    double x = xi - L.xc, y = yi - L.yc;
-    const bool rot = (L.sintheta != 0);
-    if (rot) {
-        const double xp = x * L.costheta + y * L.sintheta;
-        y = -x * L.sintheta + y * L.costheta;
-        x = xp;
+    // the FP64 work is the first half's; the second half takes the network's
+    // inputs from shared memory (after the group's reduction below)
+    const int tid = threadIdx.x & 127;
+    const bool first = S.half == 0;
+    double x = 0, y = 0, bnd = 0, B = 0;
+    bool rot = false, centre = false, inb = false, maybe = false;
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+    if (first) {
+        x = xi - L.xc; y = yi - L.yc;
+        rot = (L.sintheta != 0);
+        if (rot) {
+            const double xp = x * L.costheta + y * L.sintheta;
+            y = -x * L.sintheta + y * L.costheta;
+            x = xp;
+        }
+        const SurIn in = sur_inputs_ray(x * T.inv_rs[k], y * T.inv_rs[k], L.q, T.inv_q[k]);
+        centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
+        inb = in.bin >= 0;
+        B = in.B;
+        // the cell's bound on the relative error of G, plus B's
+        bnd = inb ? (double)bound[in.bin] + in.B_rel : 0.0;
+        // before the network: |alpha| ~ ks B |(x, y)| (G is within a few tens of
+        // percent of B), so a group none of whose rays can pass the gate skips
+        // the network and sends every ray to the quadrature (the gates compare
+        // squares: no FP64 square root)
+        const double gb = L.ks * in.B * bnd;
+        maybe = valid && !centre && inb && gb * gb * (x * x + y * y) <= 2.25 * thresh * thresh;
+        f0 = in.f0; f1 = in.f1; f2 = in.f2;
+        S.xin[tid] = make_float4(f0, f1, f2, 0.f);
     }
-    const SurIn in = sur_inputs_ray(x * T.inv_rs[k], y * T.inv_rs[k], L.q, T.inv_q[k]);
-    const bool centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
-    // the cell's bound on the relative error of G, plus B's
-    const double bnd = (in.bin >= 0) ? (double)bound[in.bin] + in.B_rel : 0.0;
-    // before the network: |alpha| ~ ks B |(x, y)| (G is within a few tens of
-    // percent of B), so a group none of whose rays can pass the gate skips
-    // the network and sends every ray to the quadrature (the gates compare
-    // squares: no FP64 square root)
-    const double gb = L.ks * in.B * bnd;
-    const bool maybe = valid && !centre && in.bin >= 0 && gb * gb * (x * x + y * y) <= 2.25 * thresh * thresh;
     double bx = 0, by = 0;
     bool use = false;
     if (wg_any(S.wg, maybe)) {
+        if (!first) {
+            const float4 v = S.xin[tid];
+            f0 = v.x; f1 = v.y; f2 = v.z;
+        }
         float t0, t1;
-        sur_mlp_wg(S, in.f0, in.f1, in.f2, t0, t1, ok);
-        const float oq = (float)(1.0 - L.q);
-        const double G0 = in.B * (double)expf(oq * t0), G1 = in.B * (double)expf(oq * t1);
-        bx = x * L.ks * G0;
-        by = y * L.ks * G1;
-        const double m2 = bx * bx + by * by;
-        use = ok && !centre && in.bin >= 0 && m2 * bnd * bnd <= thresh * thresh;
-        // |alpha| in FP32, rounded up by far more than its error
-        if (use) eps += 2.0 * zabs * (double)(sqrtf((float)m2) * 1.000001f) * bnd;
+        sur_mlp_wg(S, f0, f1, f2, t0, t1, ok);
+        if (first) {
+            const float oq = (float)(1.0 - L.q);
+            const double G0 = B * (double)expf(oq * t0), G1 = B * (double)expf(oq * t1);
+            bx = x * L.ks * G0;
+            by = y * L.ks * G1;
+            const double m2 = bx * bx + by * by;
+            use = ok && !centre && inb && m2 * bnd * bnd <= thresh * thresh;
+            // |alpha| in FP32, rounded up by far more than its error
+            if (use) eps += 2.0 * zabs * (double)(sqrtf((float)m2) * 1.000001f) * bnd;
+        }
     }
+    if (!first) { ax = 0; ay = 0; return; }
     if (!use && valid) {
         fb++;
         if (k == defer_lens) {
@@ -819,6 +865,7 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
     __shared__ __align__(16) LensModel lm;
     __shared__ SurTabs T;
     __shared__ int n_fb;
+    __shared__ float2 xo[2 * 256 + 2 * 2 * 128];   // partial outputs, then the inputs
     if ((int)blockIdx.x * 2 * 128 >= sd.n_sub) return;     // launched for the slot's capacity
     {
         const double* src = reinterpret_cast<const double*>(&ep->lm);
@@ -828,13 +875,15 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
         sur_tabs_fill(ep, sd.nsplit, T);     // (sur_cta_begin's barrier orders these with their readers)
     }
     SurWG S;
-    bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag);
+    bool ok = sur_cta_begin(S, smem_raw, wimg, small_g, &w_bar, mma_bar, &tmem_slot, &abort_flag, xo);
     const int tid = threadIdx.x & 127;
     int fb = 0;
     for (int grp = blockIdx.x * 2 + S.wg; grp * 128 < sd.n_sub; grp += gridDim.x * 2) {
         if (wg_any(S.wg, !ok || abort_flag)) { ok = false; break; }
         const int t = grp * 128 + tid;
-        const bool valid = t < sd.n_sub;
+        // both threads of a ray trace it; the first half stores it, queues
+        // its fallback and counts it
+        const bool valid = t < sd.n_sub && S.half == 0;
         // bound on this ray's source-point error against the plain path:
         // rounding (this unit contracts multiply-adds, and deflections are
         // summed in another order) plus, per surrogate deflection, twice its
@@ -879,6 +928,8 @@ __global__ void __launch_bounds__(SUR_THREADS, 1) k_raytrace_sur(StaticData sd_,
                 if (L.type == QLP_LENS_NFW && L.q != 1.0)
                     sur_nfw(S, ok, L, k, T, bound, thresh, fabs(lm.zfac[p]), valid, t, defer_lens, q, fb, eps, xi,
                             yi, ax, ay);
+                else if (S.half != 0)
+                    ax = ay = 0;       // (the second half only joins the network's evaluations)
                 else if (T.sie_u[k] != 0.0)
                     sur_sie0(L, T, k, xi, yi, ax, ay);
                 else
