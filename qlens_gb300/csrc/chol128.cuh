@@ -76,8 +76,7 @@ __global__ void __launch_bounds__(256, 1) k_potrf128(float* __restrict__ A, int 
     extern __shared__ float p128_smem[];
     float (*S)[C2 + 1] = reinterpret_cast<float (*)[C2 + 1]>(p128_smem);
     float (*V)[C2 + 1] = reinterpret_cast<float (*)[C2 + 1]>(p128_smem + C2 * (C2 + 1));
-    float (*T)[33] = reinterpret_cast<float (*)[33]>(p128_smem + 2 * C2 * (C2 + 1));
-    float* rdiag = p128_smem + 2 * C2 * (C2 + 1) + 32 * 33;   // 1 / L_ii
+    float* rdiag = p128_smem + 2 * C2 * (C2 + 1) + 32 * 33;   // 1 / L_ii (after a 32 x 33 scratch)
     const int Mp = cpad128(gs->M);
     const int o = k * C2;
     if (o >= Mp) return;
@@ -185,27 +184,29 @@ __global__ void __launch_bounds__(256, 1) k_potrf128(float* __restrict__ A, int 
     }
     __syncthreads();
     // ---- off-diagonal blocks by distance d: V_ij = -V_ii (sum_{k=j}^{i-1} L_ik V_kj) ----
+    // The blocks of one distance depend only on nearer ones, so all of them
+    // are formed together: two barriers per distance instead of two per
+    // block, each sum in its old order.  The products sum_k L_ik V_kj go into
+    // the upper triangle of V (block (j, i)), which nothing reads as V.
     for (int d = 1; d < 4; d++) {
-        for (int jb = 0; jb + d < 4; jb++) {
-            const int ib = jb + d;
-            for (int e = tid; e < 32 * 32; e += blockDim.x) {
-                const int r = e >> 5, c = e & 31;
-                float acc = 0.f;
-                for (int kb = jb; kb < ib; kb++)
-                    #pragma unroll 8
-                    for (int m = 0; m < 32; m++) acc += S[ib * 32 + r][kb * 32 + m] * V[kb * 32 + m][jb * 32 + c];
-                T[r][c] = acc;
-            }
-            __syncthreads();
-            for (int e = tid; e < 32 * 32; e += blockDim.x) {
-                const int r = e >> 5, c = e & 31;
-                float acc = 0.f;
+        const int nbk = 4 - d;
+        for (int e = tid; e < nbk * 32 * 32; e += blockDim.x) {
+            const int jb = e >> 10, r = (e >> 5) & 31, c = e & 31, ib = jb + d;
+            float acc = 0.f;
+            for (int kb = jb; kb < ib; kb++)
                 #pragma unroll 8
-                for (int m = 0; m <= r; m++) acc += V[ib * 32 + r][ib * 32 + m] * T[m][c];
-                V[ib * 32 + r][jb * 32 + c] = -acc;
-            }
-            __syncthreads();
+                for (int m = 0; m < 32; m++) acc += S[ib * 32 + r][kb * 32 + m] * V[kb * 32 + m][jb * 32 + c];
+            V[jb * 32 + r][ib * 32 + c] = acc;
         }
+        __syncthreads();
+        for (int e = tid; e < nbk * 32 * 32; e += blockDim.x) {
+            const int jb = e >> 10, r = (e >> 5) & 31, c = e & 31, ib = jb + d;
+            float acc = 0.f;
+            #pragma unroll 8
+            for (int m = 0; m <= r; m++) acc += V[ib * 32 + r][ib * 32 + m] * V[jb * 32 + m][ib * 32 + c];
+            V[ib * 32 + r][jb * 32 + c] = -acc;
+        }
+        __syncthreads();
     }
     // Linv (row-major, upper part zero) and its transpose right after it
     #pragma unroll 4

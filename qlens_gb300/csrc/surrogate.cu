@@ -120,9 +120,10 @@ __device__ __forceinline__ float sur_B32(float x)
 __host__ __device__ __forceinline__ int sur_cell(double rho, double phi, double q)
 {
     if (!(rho >= SUR_RHO_LO && rho < SUR_RHO_HI && q >= SUR_Q_LO && q < 1.0)) return -1;
-    int ir = (int)((rho - SUR_RHO_LO) / (SUR_RHO_HI - SUR_RHO_LO) * SUR_NB_RHO);
-    int ip = (int)(phi / (0.5 * M_PI) * SUR_NB_PHI);
-    int iq = (int)((q - SUR_Q_LO) / (1.0 - SUR_Q_LO) * SUR_NB_Q);
+    // (multiplications by the cells per unit: no FP64 divide per ray)
+    int ir = (int)((rho - SUR_RHO_LO) * (SUR_NB_RHO / (SUR_RHO_HI - SUR_RHO_LO)));
+    int ip = (int)(phi * (SUR_NB_PHI / (0.5 * M_PI)));
+    int iq = (int)((q - SUR_Q_LO) * (SUR_NB_Q / (1.0 - SUR_Q_LO)));
     ir = ir < 0 ? 0 : (ir >= SUR_NB_RHO ? SUR_NB_RHO - 1 : ir);
     ip = ip < 0 ? 0 : (ip >= SUR_NB_PHI ? SUR_NB_PHI - 1 : ip);
     iq = iq < 0 ? 0 : (iq >= SUR_NB_Q ? SUR_NB_Q - 1 : iq);
@@ -143,7 +144,7 @@ __device__ __forceinline__ SurIn sur_inputs(double X, double Y, double q)
     // inputs, but the ray takes the quadrature
     s.f0 = (float)fmin(fmax((rho - mr) / hr, -2.0), 2.0);
     s.f1 = (float)(phi * (4.0 / M_PI) - 1.0);
-    s.f2 = (float)fmin(fmax((q - mq) / hq, -2.0), 2.0);
+    s.f2 = (float)fmin(fmax((q - mq) * (1.0 / hq), -2.0), 2.0);
     s.bin = sur_cell(rho, phi, q);
     s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, q * ax * ax + ay * ay / q);
     s.B_rel = 0.0;
@@ -165,7 +166,7 @@ __device__ __forceinline__ SurIn sur_inputs_ray(double X, double Y, double q, do
     const double hq = 0.5 * (1.0 - SUR_Q_LO), mq = 0.5 * (1.0 + SUR_Q_LO);
     s.f0 = fminf(fmaxf((rho - mr) / hr, -2.0f), 2.0f);
     s.f1 = phi * (float)(4.0 / M_PI) - 1.0f;
-    s.f2 = (float)fmin(fmax((q - mq) / hq, -2.0), 2.0);
+    s.f2 = (float)fmin(fmax((q - mq) * (1.0 / hq), -2.0), 2.0);
     s.bin = sur_cell((double)rho, (double)phi, q);
     const double xi2 = q * ax * ax + ay * ay * inv_q;
     if (xi2 >= SUR_B32_MIN) {
