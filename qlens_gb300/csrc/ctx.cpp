@@ -116,6 +116,8 @@ static int alloc_work(qlp_ctx* c, Slot& s, int n_mask, int nsub, int Mcells, int
     s.M_cap = Mc;
     s.N_cap = n_mask;
     s.npix_pad = (c->nx + 2 * (c->sd.pnx / 2)) * (c->ny + 2 * (c->sd.pny / 2));
+    s.img_nx = c->nx; s.img_ny = c->ny;
+    s.psf_nx = c->sd.pnx; s.psf_ny = c->sd.pny;
     s.nsub_cap = nsub;
     s.snx_cap = snx_max;
     s.sny_cap = sny_max;

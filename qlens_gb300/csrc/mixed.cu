@@ -47,6 +47,8 @@ struct MixedWork {
     int M_cap = 0;           // rows of X, multiple of 128
     unsigned char* nz = nullptr;
     int nkb_cap = 0;
+    int4* psfx_meta = nullptr; // band schedule: 2 int4 per (cell, band) item (k_psfx_meta)
+    int psfx_bands = 0;        // bands it has room for
     float* F32 = nullptr;
     float* R32 = nullptr;
     int ld32 = 0;
@@ -432,53 +434,32 @@ __device__ __forceinline__ bool store_x8(void* Xh, void* Xl, size_t idx, const f
     return any;
 }
 
-// REGPSF (PSFs of at most 32 x 32 taps): lane pk holds PSF column pk in
-// registers and an entry's footprint is visited row by row, fully unrolled
-// -- no shared-memory loads of taps or offsets per tap, independent atomics
-// back to back.  The integer sums are the same either way.
-template <bool REGPSF>
-__global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridState* __restrict__ gs,
-                                               const int* __restrict__ colptr, const int* __restrict__ colrow,
-                                               const float* __restrict__ colval, const int* __restrict__ rowpix,
-                                               const float* __restrict__ sqc, int H, void* __restrict__ Xh,
-                                               void* __restrict__ Xl, float xs, int half, int K_cap,
-                                               unsigned char* __restrict__ nz,
-                                               int nkb_cap)
+// The band schedule's per-item set-up, one warp per (source cell s, band):
+// the range [e0, e1) of s's entries whose footprints reach the band's image
+// rows [j0, j1), their bounding box, the window's image rows [wr0, wr1) and
+// the active rows [r0, r1) lying in them (active rows are ordered by image
+// row).  meta[2 i] = (e0, e1, imin, imax), meta[2 i + 1] = (wr0, wr1, r0, r1)
+// for item i = s * nband + band; an item without entries gets e0 = e1.
+__global__ void __launch_bounds__(256) k_psfx_meta(StaticData sd, const GridState* __restrict__ gs,
+                                                   const int* __restrict__ colptr, const int* __restrict__ colrow,
+                                                   const int* __restrict__ rowpix, int H, int nband,
+                                                   int4* __restrict__ meta)
 {
-    extern __shared__ __align__(16) unsigned char psfx_smem[];
-    const int pnx = sd.pnx, pny = sd.pny, nxh = pnx / 2, nyh = pny / 2;
-    const int nT = pnx * pny;
-    const int Wmax = sd.nx + pnx - 1;
-    long long* acc = reinterpret_cast<long long*>(psfx_smem);
-    float* tpsf = reinterpret_cast<float*>(acc + (size_t)H * Wmax);
-    int* toff = reinterpret_cast<int*>(tpsf + nT);
-    int* sh = toff + nT;          // [0..1] entry range, [2..3] band's active rows, [4..7] box
+    const int lane = threadIdx.x & 31;
+    const int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int N = gs->N, M = gs->M;
     const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
-    const int s = blockIdx.x;
-    const int j0 = blockIdx.y * H, j1 = min(j0 + H, sd.ny);
-    if (s >= Mp || j0 >= sd.ny) return;
-    const float inv = ldexpf(1.0f, -sd.fix_exp_x);
+    const int s = item / nband, band = item - s * nband;
+    if (s >= Mp) return;
+    const int nxh = sd.pnx / 2, nyh = sd.pny / 2;
+    const int j0 = band * H, j1 = min(j0 + H, sd.ny);
     const int b = (s < M) ? colptr[s] : 0, n = (s < M) ? colptr[s + 1] - b : 0;
-    // four searches, a warp each: the entries whose footprint (rows
-    // jq - nyh .. jq - nyh + pny - 1) can reach rows [j0, j1), i.e. jq in
-    // [j0 - nyh, j1 + nyh), and the band's active rows
-    {
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        int r = 0;
-        if (warp == 0) r = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
-        if (warp == 1) r = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
-        if (warp == 2) r = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, j0);
-        if (warp == 3) r = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, j1);
-        if (warp < 4 && lane == 0) sh[warp] = r;
-    }
-    if (threadIdx.x == 0) { sh[4] = INT_MAX; sh[5] = INT_MIN; sh[6] = INT_MAX; sh[7] = INT_MIN; }
-    __syncthreads();
-    const int e0 = sh[0], e1 = sh[1];
-    // bounding box of the entries (x and y image indices)
-    {
+    const int e0 = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
+    const int e1 = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j1 + nyh);
+    int4 m0 = make_int4(e0, e0, 0, 0), m1 = make_int4(j0, j0, 0, 0);
+    if (e1 > e0) {
         int imn = INT_MAX, imx = INT_MIN, jmn = INT_MAX, jmx = INT_MIN;
-        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        for (int e = e0 + lane; e < e1; e += 32) {
             const int pix = rowpix[colrow[b + e]];
             const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
             imn = min(imn, iq); imx = max(imx, iq); jmn = min(jmn, jq); jmx = max(jmx, jq);
@@ -489,22 +470,71 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
             jmn = min(jmn, __shfl_xor_sync(0xffffffffu, jmn, o));
             jmx = max(jmx, __shfl_xor_sync(0xffffffffu, jmx, o));
         }
-        if ((threadIdx.x & 31) == 0 && e1 > e0) {
-            atomicMin(&sh[4], imn); atomicMax(&sh[5], imx); atomicMin(&sh[6], jmn); atomicMax(&sh[7], jmx);
-        }
+        const int wr0 = max(j0, jmn - nyh), wr1 = min(j1, jmx - nyh + sd.pny);
+        const int r0 = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, wr0);
+        const int r1 = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, wr1);
+        m0 = make_int4(e0, e1, imn, imx);
+        m1 = make_int4(wr0, wr1, r0, r1);
+        (void)nxh;
     }
-    __syncthreads();
-    const bool any = e1 > e0;
-    const int imin = any ? sh[4] : 0;
-    // window: rows [wr0, wr1) of the image, columns imin - nxh .. imin - nxh + Wb - 1
-    const int wr0 = any ? max(j0, sh[6] - nyh) : j0;
-    const int wr1 = any ? min(j1, sh[7] - nyh + pny) : j0;
-    const int Wb = any ? sh[5] - imin + pnx : 0;
+    if (lane == 0) {
+        meta[2 * (size_t)item] = m0;
+        meta[2 * (size_t)item + 1] = m1;
+    }
+}
+
+// X's first Mp rows (cells) cleared before the band kernel, which then writes
+// only the active rows of its windows: 16-byte stores, every column of X
+// (K_cap, a multiple of 64) -- the tail beyond N included, which the SYRK
+// reads as whole 64-pixel stages.
+__global__ void k_zero_x(const GridState* __restrict__ gs, uint4* __restrict__ Xh, uint4* __restrict__ Xl,
+                         size_t row_vec)
+{
+    const int M = gs->M;
+    const size_t n = (size_t)((M + TC_TILE - 1) / TC_TILE * TC_TILE) * row_vec;
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        Xh[i] = z;
+        Xl[i] = z;
+    }
+}
+
+// REGPSF (PSFs of at most 32 x 32 taps): lane pk holds PSF column pk in
+// registers and an entry's footprint is visited row by row, fully unrolled
+// -- no shared-memory loads of taps or offsets per tap, independent atomics
+// back to back.  The integer sums are the same either way.
+template <bool REGPSF>
+__global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridState* __restrict__ gs,
+                                               const int* __restrict__ colptr, const int* __restrict__ colrow,
+                                               const float* __restrict__ colval, const int* __restrict__ rowpix,
+                                               const float* __restrict__ sqc, int nband,
+                                               const int4* __restrict__ meta, void* __restrict__ Xh,
+                                               void* __restrict__ Xl, float xs, int half, int K_cap,
+                                               unsigned char* __restrict__ nz, int nkb_cap)
+{
+    extern __shared__ __align__(16) unsigned char psfx_smem[];
+    const int pnx = sd.pnx, pny = sd.pny, nxh = pnx / 2, nyh = pny / 2;
+    const int nT = pnx * pny;
+    const int M = gs->M;
+    const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
+    const int s = blockIdx.x;
+    if (s >= Mp) return;
+    const size_t item = (size_t)s * nband + blockIdx.y;
+    const int4 m0 = meta[2 * item], m1 = meta[2 * item + 1];
+    const int e0 = m0.x, e1 = m0.y, imin = m0.z;
+    if (e1 <= e0) return;                                // nothing reaches the band: X stays zero
+    const int wr0 = m1.x, wr1 = m1.y, ra = m1.z, rb = m1.w;
+    const int Wb = m0.w - imin + pnx;                    // window columns imin - nxh .. imin - nxh + Wb - 1
+    long long* acc = reinterpret_cast<long long*>(psfx_smem);
+    float* tpsf = reinterpret_cast<float*>(acc + (size_t)(wr1 - wr0) * Wb);
+    int* toff = reinterpret_cast<int*>(tpsf + nT);
+    const float inv = ldexpf(1.0f, -sd.fix_exp_x);
+    const int b = colptr[s];
     for (int i = threadIdx.x; i < (wr1 - wr0) * Wb; i += blockDim.x) acc[i] = 0;
     // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on the
     // fixed-point grid, and the tap's offset in the window from the
     // footprint's corner (the register path reads the taps directly)
-    if (!REGPSF && any) {
+    if (!REGPSF) {
         for (int t = threadIdx.x; t < nT; t += blockDim.x) {
             const int pl = t / pnx, pk = t - pl * pnx;
             tpsf[t] = sd.psf_fix[t];
@@ -516,7 +546,7 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         float col[32];
         #pragma unroll
-        for (int pl = 0; pl < 32; pl++) col[pl] = (e1 > e0 && lane < pnx && pl < pny) ? sd.psf_fix[pl * pnx + lane] : 0.0f;
+        for (int pl = 0; pl < 32; pl++) col[pl] = (lane < pnx && pl < pny) ? sd.psf_fix[pl * pnx + lane] : 0.0f;
         for (int e = e0 + warp; e < e1; e += nw) {
             const int q = colrow[b + e];
             const float v = colval[b + e];
@@ -549,13 +579,11 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
         }
     }
     __syncthreads();
-    // X[s][r] for the band's active rows r: v = sqrt(C^-1)_r * sum (0 outside
-    // the window) split into hi + lo; the first band also clears X[s][N .. N
-    // rounded up to 64) (the SYRK reads whole stages)
-    // (eight rows per thread where the band's range is aligned to eight,
-    // single rows at its two ends)
+    // X[s][r] for the active rows r of the window's image rows: v =
+    // sqrt(C^-1)_r * sum (0 outside the window's columns) split into hi + lo;
+    // eight rows per thread where the range is aligned to eight, single rows
+    // at its two ends.  Every other entry of X's row s is zero (k_zero_x).
     {
-        const int ra = sh[2], rb = sh[3];
         const int ha = min(rb, (ra + 7) & ~7), tb = max(ha, rb & ~7);
         auto xval = [&](int r) -> float {
             const int pix = rowpix[r];
@@ -577,10 +605,6 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
             if (store_x8(Xh, Xl, (size_t)s * K_cap + g, v, xs, half))
                 nz[(size_t)(s / TC_TILE) * nkb_cap + g / TC_KB] = 1;
         }
-    }
-    if (blockIdx.y == 0) {
-        const int Np = (N + 63) & ~63;
-        for (int r = N + threadIdx.x; r < Np; r += blockDim.x) store_x(Xh, Xl, (size_t)s * K_cap + r, 0.0f, xs, half);
     }
 }
 
@@ -785,10 +809,26 @@ void mixed_free(Slot& c)
     void* ptrs[] = {m->t, m->X_hi, m->X_lo, m->nz, m->F32, m->R32, m->u, m->v, m->r, m->z, m->y, m->img,
                     m->linvF, m->linv128, m->yf, m->zf, m->flags, m->colcnt, m->cursor, m->colrow, m->colval,
                     m->sqc, m->col_u, m->src_u, m->colval64, m->pixT, m->F0, m->Pf_hi, m->Pf_lo, m->Pf_exp,
-                    m->Pr_hi, m->Pr_lo, m->Pr_exp};
+                    m->Pr_hi, m->Pr_lo, m->Pr_exp, m->psfx_meta};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete m;
     c.mixed = nullptr;
+}
+
+// The band schedule's geometry: image rows per band H -- as many as fit
+// beside the PSF tables in about half an SM's shared memory (two CTAs per
+// SM), divided by `split` -- the number of bands and the dynamic shared
+// memory of a CTA.
+static void psfx_band_geom(int nx, int ny, int pnx, int pny, int split, int& H, int& nband, size_t& smem)
+{
+    const int nT = pnx * pny;
+    const int W = nx + pnx - 1;
+    const size_t tap_bytes = (sizeof(float) + sizeof(int)) * (size_t)nT + 8 * sizeof(int);
+    const size_t avail = (110 * 1024 > tap_bytes) ? 110 * 1024 - tap_bytes : 0;
+    const int fit = std::max(1, (int)(avail / (sizeof(long long) * W)));
+    H = std::max(1, std::min(ny, fit) / split);
+    nband = (ny + H - 1) / H;
+    smem = sizeof(long long) * (size_t)H * W + tap_bytes;
 }
 
 int mixed_init(Slot& c)
@@ -810,6 +850,12 @@ int mixed_init(Slot& c)
     A((void**)&m->X_hi, xbytes);
     A((void**)&m->X_lo, xbytes);
     A((void**)&m->nz, (size_t)(M_cap / TC_TILE) * m->nkb_cap);
+    {
+        int H = 1;
+        size_t sm = 0;
+        psfx_band_geom(c.img_nx, c.img_ny, c.psf_nx, c.psf_ny, 4, H, m->psfx_bands, sm);   // the finest split
+        A((void**)&m->psfx_meta, sizeof(int4) * 2 * (size_t)M_cap * m->psfx_bands);
+    }
     A((void**)&m->F32, sizeof(float) * (size_t)M_cap * M_cap);
     A((void**)&m->R32, sizeof(float) * (size_t)M_cap * M_cap);
     m->nnz_cap = 3 * c.N_cap * c.nsub_cap;
@@ -966,23 +1012,24 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         const int split = std::max(1, std::min(c->psfx_split, 4));
         const int pt = (c->psfx_threads == 128 || c->psfx_threads == 512) ? c->psfx_threads : 256;
         if (c->psfx_mode == 1) {
-            // image rows per CTA: as many as fit beside the PSF tables in about
-            // half an SM's shared memory (two CTAs per SM), divided by psfx_split
-            const int W = sd.nx + sd.pnx - 1;
-            const size_t tap_bytes = (sizeof(float) + sizeof(int)) * (size_t)nT + 8 * sizeof(int);
-            const size_t avail = (110 * 1024 > tap_bytes) ? 110 * 1024 - tap_bytes : 0;
-            const int fit = std::max(1, (int)(avail / (sizeof(long long) * W)));
-            const int H = std::max(1, std::min(sd.ny, fit) / split);
-            const int nband = (sd.ny + H - 1) / H;
-            const size_t smem = sizeof(long long) * (size_t)H * W + tap_bytes;
+            int H = 1, nband = 1;
+            size_t smem = 0;
+            psfx_band_geom(sd.nx, sd.ny, sd.pnx, sd.pny, split, H, nband, smem);
+            // X's rows cleared, each item's set-up, then the windows
+            const size_t row_vec = (size_t)m->K_cap * (m->half ? 2 : 4) / 16;
+            k_zero_x<<<152 * 8, 256, 0, st>>>(w.gs, reinterpret_cast<uint4*>(m->X_hi),
+                                              reinterpret_cast<uint4*>(m->X_lo), row_vec);
+            k_psfx_meta<<<(m->M_cap * nband + 7) / 8, 256, 0, st>>>(sd, w.gs, m->colcnt, m->colrow, w.rowpix, H,
+                                                                  nband, m->psfx_meta);
             if (sd.pnx <= 32 && sd.pny <= 32)
-                k_psf_x_band<true><<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
-                                                                   w.rowpix, m->sqc, H, m->X_hi, m->X_lo, xs,
-                                                                   m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
+                k_psf_x_band<true><<<dim3(m->M_cap, nband), pt, smem, st>>>(
+                    sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->sqc, nband, m->psfx_meta, m->X_hi,
+                    m->X_lo, xs, m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
             else
-                k_psf_x_band<false><<<dim3(m->M_cap, nband), pt, smem, st>>>(sd, w.gs, m->colcnt, m->colrow, m->colval,
-                                                                   w.rowpix, m->sqc, H, m->X_hi, m->X_lo, xs,
-                                                                   m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
+                k_psf_x_band<false><<<dim3(m->M_cap, nband), pt, smem, st>>>(
+                    sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->sqc, nband, m->psfx_meta, m->X_hi,
+                    m->X_lo, xs, m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
+            n += 2;
         } else {
             // accumulator rows per CTA: the active rows split into psfx_split
             // chunks (or more, if a chunk does not fit beside the PSF in 227 KB)

@@ -23,6 +23,8 @@ struct Slot {
     int nsub_cap = 0;
     int snx_cap = 0, sny_cap = 0;
     int npix_pad = 0;               // image pixels with a PSF-half-width border: (nx + 2 (pnx/2)) (ny + 2 (pny/2))
+    int img_nx = 0, img_ny = 0;     // image and PSF sizes (the PSF-to-X band layout)
+    int psf_nx = 0, psf_ny = 0;
     bool fp64_mats = false;         // F and R in FP64 allocated
     cudaEvent_t done = nullptr;
     // second stream of the slot: R's factorisation runs beside F's
