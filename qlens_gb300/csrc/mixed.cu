@@ -436,10 +436,9 @@ __device__ __forceinline__ bool store_x8(void* Xh, void* Xl, size_t idx, const f
 
 // The band schedule's per-item set-up, one warp per (source cell s, band):
 // the range [e0, e1) of s's entries whose footprints reach the band's image
-// rows [j0, j1), their bounding box, the window's image rows [wr0, wr1) and
-// the active rows [r0, r1) lying in them (active rows are ordered by image
-// row).  meta[2 i] = (e0, e1, imin, imax), meta[2 i + 1] = (wr0, wr1, r0, r1)
-// for item i = s * nband + band; an item without entries gets e0 = e1.
+// rows [j0, j1), their bounding box and the window's image rows [wr0, wr1).
+// meta[2 i] = (e0, e1, imin, imax), meta[2 i + 1] = (wr0, wr1, -, -) for
+// item i = s * nband + band; an item without entries gets e0 = e1.
 __global__ void __launch_bounds__(256) k_psfx_meta(StaticData sd, const GridState* __restrict__ gs,
                                                    const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                    const int* __restrict__ rowpix, int H, int nband,
@@ -447,11 +446,11 @@ __global__ void __launch_bounds__(256) k_psfx_meta(StaticData sd, const GridStat
 {
     const int lane = threadIdx.x & 31;
     const int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int N = gs->N, M = gs->M;
+    const int M = gs->M;
     const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
     const int s = item / nband, band = item - s * nband;
     if (s >= Mp) return;
-    const int nxh = sd.pnx / 2, nyh = sd.pny / 2;
+    const int nyh = sd.pny / 2;
     const int j0 = band * H, j1 = min(j0 + H, sd.ny);
     const int b = (s < M) ? colptr[s] : 0, n = (s < M) ? colptr[s + 1] - b : 0;
     const int e0 = warp_lower_bound_row(rowpix, colrow + b, n, sd.ny, j0 - nyh);
@@ -471,11 +470,8 @@ __global__ void __launch_bounds__(256) k_psfx_meta(StaticData sd, const GridStat
             jmx = max(jmx, __shfl_xor_sync(0xffffffffu, jmx, o));
         }
         const int wr0 = max(j0, jmn - nyh), wr1 = min(j1, jmx - nyh + sd.pny);
-        const int r0 = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, wr0);
-        const int r1 = warp_lower_bound_row(rowpix, nullptr, N, sd.ny, wr1);
         m0 = make_int4(e0, e1, imn, imx);
-        m1 = make_int4(wr0, wr1, r0, r1);
-        (void)nxh;
+        m1 = make_int4(wr0, wr1, 0, 0);
     }
     if (lane == 0) {
         meta[2 * (size_t)item] = m0;
@@ -507,7 +503,7 @@ template <bool REGPSF>
 __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
-                                               const float* __restrict__ sqc, int nband,
+                                               const int2* __restrict__ pixT, int nband,
                                                const int4* __restrict__ meta, void* __restrict__ Xh,
                                                void* __restrict__ Xl, float xs, int half, int K_cap,
                                                unsigned char* __restrict__ nz, int nkb_cap)
@@ -523,7 +519,7 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     const int4 m0 = meta[2 * item], m1 = meta[2 * item + 1];
     const int e0 = m0.x, e1 = m0.y, imin = m0.z;
     if (e1 <= e0) return;                                // nothing reaches the band: X stays zero
-    const int wr0 = m1.x, wr1 = m1.y, ra = m1.z, rb = m1.w;
+    const int wr0 = m1.x, wr1 = m1.y;
     const int Wb = m0.w - imin + pnx;                    // window columns imin - nxh .. imin - nxh + Wb - 1
     long long* acc = reinterpret_cast<long long*>(psfx_smem);
     float* tpsf = reinterpret_cast<float*>(acc + (size_t)(wr1 - wr0) * Wb);
@@ -579,31 +575,22 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
         }
     }
     __syncthreads();
-    // X[s][r] for the active rows r of the window's image rows: v =
-    // sqrt(C^-1)_r * sum (0 outside the window's columns) split into hi + lo;
-    // eight rows per thread where the range is aligned to eight, single rows
-    // at its two ends.  Every other entry of X's row s is zero (k_zero_x).
+    // X[s][r] for the active pixels r of the window: v = sqrt(C^-1)_r * sum,
+    // split into hi + lo; the window's pixels are visited x fastest through
+    // the padded image's (active row, sqrt(C^-1)) table.  Every other entry
+    // of X's row s is zero (k_zero_x).
     {
-        const int ha = min(rb, (ra + 7) & ~7), tb = max(ha, rb & ~7);
-        auto xval = [&](int r) -> float {
-            const int pix = rowpix[r];
-            const int i = pix / sd.ny, j = pix - i * sd.ny;
-            const int wc = i - imin + nxh;
-            float v = 0.0f;
-            if (j >= wr0 && j < wr1 && wc >= 0 && wc < Wb) v = (ll2f_rn_int(acc[(j - wr0) * Wb + wc]) * inv) * sqc[r];
-            return v;
-        };
-        for (int r = threadIdx.x; r < (ha - ra) + (rb - tb); r += blockDim.x) {
-            const int rr = (r < ha - ra) ? ra + r : tb + (r - (ha - ra));
-            if (store_x(Xh, Xl, (size_t)s * K_cap + rr, xval(rr), xs, half))
-                nz[(size_t)(s / TC_TILE) * nkb_cap + rr / TC_KB] = 1;
-        }
-        for (int g = ha + 8 * threadIdx.x; g < tb; g += 8 * blockDim.x) {
-            float v[8];
-            #pragma unroll
-            for (int u = 0; u < 8; u++) v[u] = xval(g + u);
-            if (store_x8(Xh, Xl, (size_t)s * K_cap + g, v, xs, half))
-                nz[(size_t)(s / TC_TILE) * nkb_cap + g / TC_KB] = 1;
+        const int nxp = sd.nx + 2 * nxh;
+        const int area = (wr1 - wr0) * Wb;
+        for (int e = threadIdx.x; e < area; e += blockDim.x) {
+            const int jr = e / Wb, wc = e - jr * Wb;
+            const int i = imin - nxh + wc, j = wr0 + jr;
+            if (i < 0 || i >= sd.nx) continue;
+            const int2 pt = pixT[(size_t)(j + nyh) * nxp + i + nxh];
+            if (pt.x < 0) continue;
+            const float v = (ll2f_rn_int(acc[e]) * inv) * __int_as_float(pt.y);
+            if (store_x(Xh, Xl, (size_t)s * K_cap + pt.x, v, xs, half))
+                nz[(size_t)(s / TC_TILE) * nkb_cap + pt.x / TC_KB] = 1;
         }
     }
 }
@@ -633,7 +620,7 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
     if (s >= Mp || r0 >= Np) return;
     const int nT = sd.pnx * sd.pny;
     const float inv = ldexpf(1.0f, -sd.fix_exp_x);
-    const int pnx = sd.pnx, pny = sd.pny;
+    const int pnx = sd.pnx;
     const int nxp = sd.nx + 2 * (pnx / 2);                    // padded width of pixT
     int* toff = reinterpret_cast<int*>(tpsf + nT);
     for (int i = threadIdx.x; i < r1 - r0; i += blockDim.x) acc[i] = 0;
@@ -1023,11 +1010,11 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
                                                                   nband, m->psfx_meta);
             if (sd.pnx <= 32 && sd.pny <= 32)
                 k_psf_x_band<true><<<dim3(m->M_cap, nband), pt, smem, st>>>(
-                    sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->sqc, nband, m->psfx_meta, m->X_hi,
+                    sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->pixT, nband, m->psfx_meta, m->X_hi,
                     m->X_lo, xs, m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
             else
                 k_psf_x_band<false><<<dim3(m->M_cap, nband), pt, smem, st>>>(
-                    sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->sqc, nband, m->psfx_meta, m->X_hi,
+                    sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->pixT, nband, m->psfx_meta, m->X_hi,
                     m->X_lo, xs, m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
             n += 2;
         } else {
