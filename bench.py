@@ -50,9 +50,10 @@ METRIC = "pixel-likelihood evals/s on 1 GB300: batched+surrogate vs plain FP64 a
 # Useful FLOP of the surrogate network per ray on the tensor cores: its three
 # 128 x 128 layers, each product counted once (the hi/lo split is not work).
 MLP_FLOP_PER_RAY = 2 * 3 * 128 * 128
-# DRAM bytes (read + written) of one launch, from one ncu capture of that
-# kernel on the workload (dram__bytes_read.sum + dram__bytes_write.sum)
-RAYSUR_TRAFFIC = {"cfg5": 589824 + 512}
+# DRAM bytes (read + written) of one evaluation's ray-shooting stage on the
+# workload, from one ncu capture of its kernels (dram__bytes_read.sum +
+# dram__bytes_write.sum of k_ray_pre and k_raytrace_sur<true>)
+RAYSUR_TRAFFIC = {"cfg5": (255488 + 2560) + (22348032 + 24320)}
 SYRK_TRAFFIC = {}
 UNIT = "evals/s"
 
@@ -289,6 +290,8 @@ def plain_fp64_arm(wl, params, inst, n, slots):
     (graph capture), then the n vectors as one batch; returns (evaluations per
     second of device time, results)."""
     pl = make_context(wl, "fp64")
+    if wl.instance_masks is not None:
+        pl.set_instance_masks(wl.instance_masks)
     pl.set_batch_slots(slots)
     pl.set_graphs(True)
     ids, sizes, lam = inst
@@ -323,8 +326,11 @@ def main():
                     help="choose lambda per evaluation by Brent's method (QLens 'optimize_regparam on')")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch schedule instead of tuning it on a sample batch first")
-    ap.add_argument("--nfw", default="surrogate", choices=["surrogate", "quadrature"],
-                    help="NFW deflection: trained MLP surrogate (quadrature fallback) or quadrature only")
+    ap.add_argument("--nfw", default="auto", choices=["auto", "surrogate", "quadrature"],
+                    help="NFW deflection: trained MLP surrogate (quadrature fallback) or quadrature only; auto = "
+                         "the surrogate, except on cfg4, where most rays' deflections are too large for its gate "
+                         "(it saves nothing) and its prior-box draws on a sigma = 0.01 mock put the accepted rays' "
+                         "errors far above the |delta log L| bound")
     ap.add_argument("--profile-step", action="store_true",
                     help="after the measurement, run one more step between cudaProfilerStart and cudaProfilerStop "
                          "(for ncu --profile-from-start off); untimed")
@@ -364,7 +370,8 @@ def main():
     has_nfw = any(l["type"] in abi.NFW_TYPES for l in wl.lenses)
     if has_nfw:
         nfw = {"mode": "quadrature"}
-        if args.nfw == "surrogate":
+        nfw_mode = args.nfw if args.nfw != "auto" else ("quadrature" if args.config == "cfg4" else "surrogate")
+        if nfw_mode == "surrogate":
             from qlens_gb300 import pixlike
             rep = pixlike.train_nfw_surrogate(device=local_rank,
                                               **({"steps": args.train_steps} if args.train_steps > 0 else {}))
@@ -482,13 +489,14 @@ def main():
         n_rays = wl.n_mask * wl.nsplit ** 2
         mlp = n_rays * MLP_FLOP_PER_RAY
         ach = mlp / (ray_ms / 1e3) / 1e12 if ray_ms > 0 else None
-        roofline = {"bound": "tensor", "kernel": "k_raytrace_sur (ray shooting with the NFW surrogate)",
+        roofline = {"bound": "tensor", "kernel": "ray shooting with the NFW surrogate (k_ray_pre + k_raytrace_sur)",
                     "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if ach else None,
                     "traffic": RAYSUR_TRAFFIC.get(args.config), "peak_source": peak_note,
                     "algorithmic_flops_per_launch": mlp,
                     "work": "the network's three 128x128 layers per ray (2 x 3 x 128^2 FLOP), %d rays" % n_rays,
-                    "limiter": "the FP64 pipe (SIE deflection, lens equation and the NFW baseline per ray in FP64): "
-                               "34% active, tensor pipe 6%, 8 warps per SM (one ncu capture)",
+                    "limiter": "the network's SIMT epilogues (SFU tanh, F16 hi/lo split, TMEM loads and stores) at "
+                               "16 warps per SM: tensor pipe 20%, FP64 pipe 30% in k_raytrace_sur; the FP64 lenses "
+                               "in k_ray_pre at 85% of the FP64 pipe (one ncu capture)",
                     "timing": "CUDA events around the ray-shooting stage of single evaluations after the timed "
                               "region"}
     elif precision == "mixed":
