@@ -456,6 +456,7 @@ __global__ void __launch_bounds__(128, 3) k_chol_upd16(const __grid_constant__ C
     const uint32_t tmem = tmem_slot;
     bool ok = true;
     int issued = 0, landed = 0;      // K halves whose loads were issued / seen complete (thread 0)
+    float4 cpre[8];                  // the next 32 columns of this thread's row of the target tile
     for (int h = 0; h < 2; h++) {
         if (threadIdx.x == 0 && !abort_flag) {
             mbar_expect_tx(&full_bar, 4 * TC_TILE_BYTES);
@@ -483,6 +484,13 @@ __global__ void __launch_bounds__(128, 3) k_chol_upd16(const __grid_constant__ C
             mma_commit(&done_bar);
         }
         __syncthreads();
+        // (before the last half's MMAs are waited for, each thread's first
+        // 32 columns of the target tile are loaded: their latency overlaps the MMAs)
+        if (h == 1) {
+            const float* src = A + (size_t)(r0 + warp * 32 + lane) * ld + c0;
+            #pragma unroll
+            for (int i = 0; i < 8; i++) cpre[i] = *reinterpret_cast<const float4*>(src + 4 * i);
+        }
         // the MMAs read shared memory asynchronously: wait before the next half's loads reuse it
         if (!mbar_wait_bounded(&done_bar, (uint32_t)(h & 1), &abort_flag, false)) ok = false;
         tc_fence_after();
@@ -499,9 +507,16 @@ __global__ void __launch_bounds__(128, 3) k_chol_upd16(const __grid_constant__ C
             tmem_ld_32cols(trow + (uint32_t)c, v);
             const int sj = pexp[J * C2 + c + lane];      // column c + lane's row scale, shared through the warp
             float* dst = A + (size_t)row * ld + c0 + c;
+            float4 cur[8];
+            #pragma unroll
+            for (int i = 0; i < 8; i++) cur[i] = cpre[i];
+            if (c + 32 < TC_TILE) {                       // the next 32 columns' loads in flight meanwhile
+                #pragma unroll
+                for (int i = 0; i < 8; i++) cpre[i] = *reinterpret_cast<const float4*>(dst + 32 + 4 * i);
+            }
             #pragma unroll
             for (int i = 0; i < 32; i += 4) {
-                float4 a = *reinterpret_cast<float4*>(dst + i);
+                float4 a = cur[i / 4];
                 // 2^-(s_i + s_j), exact (|s_i + s_j| <= 120)
                 a.x -= v[i] * __int_as_float((127 - si - __shfl_sync(0xffffffffu, sj, i)) << 23);
                 a.y -= v[i + 1] * __int_as_float((127 - si - __shfl_sync(0xffffffffu, sj, i + 1)) << 23);

@@ -86,6 +86,13 @@ __device__ __forceinline__ float sur_tanh(float x)
     return 1.0f - __fdividef(2.0f, 1.0f + __expf(2.0f * x));
 }
 
+// s tanh(x) for a power of two s, as one FMA after the quotient: the same
+// bits as sur_tanh(x) * s (scaling by s commutes with the rounding)
+__device__ __forceinline__ float sur_tanh_scaled(float x, float s)
+{
+    return __fmaf_rn(-s, __fdividef(2.0f, 1.0f + __expf(2.0f * x)), s);
+}
+
 struct SurIn {
     float f0, f1, f2;   // normalised inputs
     int bin;            // error-bound cell, -1 outside the domain
@@ -530,12 +537,16 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
         uint32_t hi[16], lo[16];
         #pragma unroll
         for (int j = 0; j < 16; j++) {
-            const int u = c + 2 * j;
-            const float h0 = sur_tanh(
-                __fmaf_rn(W0[2 * SUR_H + u], f2, __fmaf_rn(W0[SUR_H + u], f1, __fmaf_rn(W0[u], f0, bb[u]))));
-            const float h1 = sur_tanh(__fmaf_rn(W0[2 * SUR_H + u + 1], f2,
-                                                __fmaf_rn(W0[SUR_H + u + 1], f1, __fmaf_rn(W0[u + 1], f0, bb[u + 1]))));
-            f16_split2(h0 * ascale, h1 * ascale, hi[j], lo[j]);
+            const int u = c + 2 * j;          // a pair of units: 8-byte loads of their weights and biases
+            const float2 w0 = *reinterpret_cast<const float2*>(W0 + u);
+            const float2 w1 = *reinterpret_cast<const float2*>(W0 + SUR_H + u);
+            const float2 w2 = *reinterpret_cast<const float2*>(W0 + 2 * SUR_H + u);
+            const float2 b0 = *reinterpret_cast<const float2*>(bb + u);
+            const float h0 = sur_tanh_scaled(__fmaf_rn(w2.x, f2, __fmaf_rn(w1.x, f1, __fmaf_rn(w0.x, f0, b0.x))),
+                                             ascale);
+            const float h1 = sur_tanh_scaled(__fmaf_rn(w2.y, f2, __fmaf_rn(w1.y, f1, __fmaf_rn(w0.y, f0, b0.y))),
+                                             ascale);
+            f16_split2(h0, h1, hi[j], lo[j]);
         }
         tmem_st_16cols_u(row + 128 + c / 2, hi);
         tmem_st_16cols_u(row + 192 + c / 2, lo);
@@ -577,19 +588,27 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
         for (int c = u0; c < u0 + 64; c += 32) {
             float v[32];
             tmem_ld_32cols(row + c, v);
+            const float sc = (l < 3) ? ascale : 1.0f;      // layers 1-2 feed the next MMA, scaled
             #pragma unroll
-            for (int j = 0; j < 32; j++) v[j] = sur_tanh(__fmaf_rn(v[j], us, bl[c + j]));
+            for (int j = 0; j < 32; j += 4) {
+                const float4 b4v = *reinterpret_cast<const float4*>(bl + c + j);
+                v[j] = sur_tanh_scaled(__fmaf_rn(v[j], us, b4v.x), sc);
+                v[j + 1] = sur_tanh_scaled(__fmaf_rn(v[j + 1], us, b4v.y), sc);
+                v[j + 2] = sur_tanh_scaled(__fmaf_rn(v[j + 2], us, b4v.z), sc);
+                v[j + 3] = sur_tanh_scaled(__fmaf_rn(v[j + 3], us, b4v.w), sc);
+            }
             if (l < 3) {
                 uint32_t hi[16], lo[16];
                 #pragma unroll
-                for (int j = 0; j < 16; j++) f16_split2(v[2 * j] * ascale, v[2 * j + 1] * ascale, hi[j], lo[j]);
+                for (int j = 0; j < 16; j++) f16_split2(v[2 * j], v[2 * j + 1], hi[j], lo[j]);
                 tmem_st_16cols_u(row + 128 + c / 2, hi);
                 tmem_st_16cols_u(row + 192 + c / 2, lo);
             } else {
                 #pragma unroll
                 for (int j = 0; j < 32; j++) {
-                    o0 = __fmaf_rn(v[j], W4[2 * (c + j)], o0);
-                    o1 = __fmaf_rn(v[j], W4[2 * (c + j) + 1], o1);
+                    const float2 w = *reinterpret_cast<const float2*>(W4 + 2 * (c + j));
+                    o0 = __fmaf_rn(v[j], w.x, o0);
+                    o1 = __fmaf_rn(v[j], w.y, o1);
                 }
             }
         }

@@ -10,9 +10,10 @@ the paths are compared on many draws of the benchmarked workloads themselves:
   workload: identical L indices, -2 log(evidence) within 1e-6 relative;
 * the mixed path against the plain FP64 path on 16 draws of that workload;
 * mixed precision with the NFW surrogate against the plain FP64 path with the
-  NFW quadrature on 8 draws of the two-plane subhalo workload (subhalo mass
-  1e8-1e10 M_sun, per-vector source grids 32x32-64x64), batched as the
-  benchmark runs it;
+  NFW quadrature on 16 draws of the two-plane subhalo workload (the posterior
+  region around the mock's subhalo of 1e9 M_sun, per-vector source grids
+  32x32-64x64), batched as the benchmark runs it, and the surrogate path's L
+  indices against the plain path's;
 
 each with the stated bound |delta log L| < 0.1, i.e. |delta(-2 log ev)| < 0.2,
 and the largest difference printed.
