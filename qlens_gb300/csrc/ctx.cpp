@@ -208,15 +208,18 @@ int ctx_init(qlp_ctx* c, const qlp_image* im, const qlp_psf* psf, const qlp_srcg
         for (int t = 0; t < npx; t++) cmax = std::max(cmax, covinv[t]);
         const double xmax = 4.0 * std::max(psum, 1e-30) * std::max(sqrt(cmax), 1e-30);
         sd.x_exp = std::max(-60, std::min(60, (int)floor(log2(16384.0 / xmax))));
-        sd.fix_exp_x = std::max(0, std::min(100, 61 - (int)ceil(log2(4.0 * std::max(psum, 1e-30)))));
+        // the taps on the grid 2^-T with sum |tap| <= 2^30 (each rounded tap
+        // then stays below 2^31)
+        const int T = std::max(0, std::min(70, 30 - (int)ceil(log2(std::max(psum, 1e-30)))));
+        sd.fix_exp_x = T + PSFX_LEXP;
         const int pnx = psf->nx, pny = psf->ny;
-        std::vector<float> pf((size_t)pnx * pny);
+        std::vector<int> pi((size_t)pnx * pny);
         for (int pl = 0; pl < pny; pl++)
             for (int pk = 0; pk < pnx; pk++)
-                pf[(size_t)pl * pnx + pk] = (float)psf->matrix[(size_t)pk * pny + pl] * ldexpf(1.0f, sd.fix_exp_x);
-        CK(dalloc(&c->d_psf_fix, pf.size()), "alloc");
-        CK(cudaMemcpy(c->d_psf_fix, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice), "h2d");
-        sd.psf_fix = c->d_psf_fix;
+                pi[(size_t)pl * pnx + pk] = (int)llrint(ldexp(psf->matrix[(size_t)pk * pny + pl], T));
+        CK(dalloc(&c->d_psf_int, pi.size()), "alloc");
+        CK(cudaMemcpy(c->d_psf_int, pi.data(), sizeof(int) * pi.size(), cudaMemcpyHostToDevice), "h2d");
+        sd.psf_int = c->d_psf_int;
     }
 
     SrcOpts& so = c->so;
@@ -248,7 +251,7 @@ void ctx_free(qlp_ctx* c)
         if (s.side_join) cudaEventDestroy(s.side_join);
     }
     c->slots.clear();
-    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_psf_fix, c->d_mpix, c->d_inst_mpix,
+    void* ptrs[] = {c->d_xvals, c->d_yvals, c->d_data, c->d_covinv, c->d_psf, c->d_psf_int, c->d_mpix, c->d_inst_mpix,
                     c->d_emask, c->d_inmask, c->d_epix, c->d_eoff};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->h_out) cudaFreeHost(c->h_out);

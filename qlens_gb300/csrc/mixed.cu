@@ -121,9 +121,10 @@ static int make_map(CUtensorMap* map, void* base, int rows, int cols, bool half)
 // pixelgrid.cpp:14126-14168); the sum at p is then scaled by sqrt(C^-1) of p.
 // The sums are accumulated as 64-bit fixed point in shared memory, so they
 // are exact and independent of the order the atomics land in (the result is
-// the same bits every run); each product is formed in FP32 and rounded once
-// to the fixed-point grid 2^-fix_exp_x, far below FP32 resolution.  No dense
-// L' is stored; each CTA covers one cell and one band of image rows.
+// the same bits every run): each product is the exact product of two 32-bit
+// integers, the tap on its grid (StaticData::psf_int) and the L entry on the
+// grid 2^-PSFX_LEXP (2^-28: 4e-9 absolute, far below FP32 resolution of the
+// entries) -- one wide multiply per tap.  No dense L' is stored.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float to_tf32(float f)
 {
@@ -310,23 +311,6 @@ __global__ void __launch_bounds__(256) k_LTw_csc(const GridState* __restrict__ g
 // band's active rows; for each entry only the PSF rows that land in the band
 // are visited, lanes along x (consecutive accumulators: the 64-bit shared
 // atomics of one instruction do not collide).
-// float -> int64, rounded to nearest even, without the 64-bit conversion
-// instruction (on GB300 it issues to the FP64 pipe, 1/64 of the FP32 rate,
-// and the PSF-to-X kernels convert one product per tap).  A float of
-// magnitude >= 2^23 is an integer: its value is the 24-bit significand
-// shifted left by the exponent.  Smaller ones (products below 2^-36 of the
-// grid's range) round through the 32-bit conversion.  Same result as
-// __float2ll_rn for |x| < 2^63, which the fixed-point scale guarantees
-// (4 sum|psf| 2^fix_exp_x <= 2^61, |L| <= 1).
-__device__ __forceinline__ long long f2ll_rn_int(float x)
-{
-    const unsigned u = __float_as_uint(x);
-    const int e = (int)((u >> 23) & 0xffu) - 150;
-    if (e < 0) return (long long)__float2int_rn(x);
-    const long long m = (long long)((u & 0x7fffffu) | 0x800000u) << e;
-    return (u >> 31) ? -m : m;
-}
-
 __device__ __forceinline__ int lower_bound_row(const int* __restrict__ rowpix, const int* __restrict__ idx, int n,
                                                int ny, int jmin)
 {
@@ -434,6 +418,9 @@ __device__ __forceinline__ bool store_x8(void* Xh, void* Xl, size_t idx, const f
     return any;
 }
 
+// Entries of a column staged in shared memory at a time by the band kernel
+#define PSFX_ECHUNK 512
+
 // The band schedule's per-item set-up, one warp per (source cell s, band):
 // the range [e0, e1) of s's entries whose footprints reach the band's image
 // rows [j0, j1), their bounding box and the window's image rows [wr0, wr1).
@@ -522,56 +509,63 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     const int wr0 = m1.x, wr1 = m1.y;
     const int Wb = m0.w - imin + pnx;                    // window columns imin - nxh .. imin - nxh + Wb - 1
     long long* acc = reinterpret_cast<long long*>(psfx_smem);
-    float* tpsf = reinterpret_cast<float*>(acc + (size_t)(wr1 - wr0) * Wb);
-    int* toff = reinterpret_cast<int*>(tpsf + nT);
+    int* tpsf = reinterpret_cast<int*>(acc + (size_t)(wr1 - wr0) * Wb);
+    int* toff = tpsf + nT;
+    int2* ent = reinterpret_cast<int2*>(toff + nT);      // staged entries (iq << 16 | jq, L): 8 nT bytes on, aligned
     const float inv = ldexpf(1.0f, -sd.fix_exp_x);
+    const float lscale = ldexpf(1.0f, PSFX_LEXP);
     const int b = colptr[s];
     for (int i = threadIdx.x; i < (wr1 - wr0) * Wb; i += blockDim.x) acc[i] = 0;
-    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on the
-    // fixed-point grid, and the tap's offset in the window from the
-    // footprint's corner (the register path reads the taps directly)
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on its grid,
+    // and the tap's offset in the window from the footprint's corner (the
+    // register path reads the taps directly)
     if (!REGPSF) {
         for (int t = threadIdx.x; t < nT; t += blockDim.x) {
             const int pl = t / pnx, pk = t - pl * pnx;
-            tpsf[t] = sd.psf_fix[t];
+            tpsf[t] = sd.psf_int[t];
             toff[t] = pl * Wb + pk;
         }
     }
-    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int col[32];
     if (REGPSF) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        float col[32];
         #pragma unroll
-        for (int pl = 0; pl < 32; pl++) col[pl] = (lane < pnx && pl < pny) ? sd.psf_fix[pl * pnx + lane] : 0.0f;
-        for (int e = e0 + warp; e < e1; e += nw) {
-            const int q = colrow[b + e];
-            const float v = colval[b + e];
-            const int pix = rowpix[q];
+        for (int pl = 0; pl < 32; pl++) col[pl] = (lane < pnx && pl < pny) ? sd.psf_int[pl * pnx + lane] : 0;
+    }
+    // the entries, PSFX_ECHUNK at a time: their pixel and L value staged in
+    // shared memory by all threads (independent loads), then spread
+    for (int c0 = e0; c0 < e1; c0 += PSFX_ECHUNK) {
+        const int cn = min(PSFX_ECHUNK, e1 - c0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cn; e += blockDim.x) {
+            const int pix = rowpix[colrow[b + c0 + e]];
             const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
-            const int pl0 = max(0, wr0 - (jq - nyh)), pl1 = min(pny, wr1 - (jq - nyh));
-            unsigned long long* cl = reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb +
-                                     (iq - imin) + lane;
-            if (lane < pnx) {
-                #pragma unroll
-                for (int pl = 0; pl < 32; pl++)
-                    if (pl >= pl0 && pl < pl1)
-                        atomicAdd(cl + pl * Wb, (unsigned long long)f2ll_rn_int(col[pl] * v));
-            }
+            ent[e] = make_int2((iq << 16) | jq, __float2int_rn(colval[b + c0 + e] * lscale));
         }
-    } else {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int e = e0 + warp; e < e1; e += nw) {
-            const int q = colrow[b + e];
-            const float v = colval[b + e];
-            const int pix = rowpix[q];
-            const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
+        __syncthreads();
+        for (int e = warp; e < cn; e += nw) {
+            const int2 en = ent[e];
+            const int iq = en.x >> 16, jq = en.x & 0xffff;
+            const int v = en.y;
             // PSF rows pl land on image row jq - nyh + pl; keep those in [wr0, wr1)
             const int pl0 = max(0, wr0 - (jq - nyh)), pl1 = min(pny, wr1 - (jq - nyh));
-            // the footprint's corner (iq - nxh, jq - nyh) in window coordinates
-            unsigned long long* corner = reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb + (iq - imin);
-            const int t1 = pl1 * pnx;
-            for (int t = pl0 * pnx + lane; t < t1; t += 32)
-                atomicAdd(corner + toff[t], (unsigned long long)f2ll_rn_int(tpsf[t] * v));
+            if (REGPSF) {
+                unsigned long long* cl = reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb +
+                                         (iq - imin) + lane;
+                if (lane < pnx) {
+                    #pragma unroll
+                    for (int pl = 0; pl < 32; pl++)
+                        if (pl >= pl0 && pl < pl1)
+                            atomicAdd(cl + pl * Wb, (unsigned long long)((long long)col[pl] * (long long)v));
+                }
+            } else {
+                // the footprint's corner (iq - nxh, jq - nyh) in window coordinates
+                unsigned long long* corner =
+                    reinterpret_cast<unsigned long long*>(acc) + (jq - nyh - wr0) * Wb + (iq - imin);
+                const int t1 = pl1 * pnx;
+                for (int t = pl0 * pnx + lane; t < t1; t += 32)
+                    atomicAdd(corner + toff[t], (unsigned long long)((long long)tpsf[t] * (long long)v));
+            }
         }
     }
     __syncthreads();
@@ -598,9 +592,9 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
 // Schedule "rows": grid (M_cap cells, chunks of active rows); one CTA holds
 // the 64-bit accumulators of a chunk of active rows and scatters each entry
 // of column s over its PSF footprint through the active-row table of the
-// padded image (pixT).  Each product psf x v is rounded once to the grid
-// 2^-fix_exp_x and sqrt(C^-1) applied to the sum, exactly as the "bands"
-// schedule does, so both give the same bits.
+// padded image (pixT).  Each product psf x L is the same exact integer
+// product and sqrt(C^-1) is applied to the sum as in the "bands" schedule, so
+// both give the same bits.
 __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridState* __restrict__ gs,
                                                const int* __restrict__ colptr, const int* __restrict__ colrow,
                                                const float* __restrict__ colval, const int* __restrict__ rowpix,
@@ -611,7 +605,7 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
 {
     extern __shared__ __align__(16) unsigned char psfx_smem[];
     long long* acc = reinterpret_cast<long long*>(psfx_smem);
-    float* tpsf = reinterpret_cast<float*>(acc + chunk);
+    int* tpsf = reinterpret_cast<int*>(acc + chunk);
     const int N = gs->N, M = gs->M;
     const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
     const int Np = (N + 63) & ~63;                           // whole 64-pixel stages for the F16 SYRK
@@ -624,21 +618,22 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
     const int nxp = sd.nx + 2 * (pnx / 2);                    // padded width of pixT
     int* toff = reinterpret_cast<int*>(tpsf + nT);
     for (int i = threadIdx.x; i < r1 - r0; i += blockDim.x) acc[i] = 0;
-    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on the
-    // fixed-point grid (StaticData::psf_fix), and the tap's offset in pixT
-    // from the footprint's corner
+    // taps in x-fastest order: tpsf[pl * pnx + pk] = psf[pk][pl] on its grid
+    // (StaticData::psf_int), and the tap's offset in pixT from the
+    // footprint's corner
     for (int t = threadIdx.x; t < nT; t += blockDim.x) {
         const int pl = t / pnx, pk = t - pl * pnx;
-        tpsf[t] = sd.psf_fix[t];
+        tpsf[t] = sd.psf_int[t];
         toff[t] = pl * nxp + pk;
     }
+    const float lscale = ldexpf(1.0f, PSFX_LEXP);
     __syncthreads();
     if (s < M) {
         const int b = colptr[s], n = colptr[s + 1] - b;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         for (int e = warp; e < n; e += nw) {
             const int q = colrow[b + e];
-            const float v = colval[b + e];
+            const long long v = __float2int_rn(colval[b + e] * lscale);     // L on its grid
             const int pix = rowpix[q];
             const int iq = pix / sd.ny, jq = pix - iq * sd.ny;
             // the footprint's corner (iq - pnx/2, jq - pny/2) sits at (iq, jq) of
@@ -649,12 +644,12 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
             // four taps per lane in flight: their table loads are independent
             for (int t0 = lane; t0 < nT; t0 += 128) {
                 int2 P[4];
-                float w[4];
+                int w[4];
                 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const int t = t0 + 32 * u;
                     P[u] = make_int2(-1, 0);
-                    w[u] = 0.0f;
+                    w[u] = 0;
                     if (t < nT) {
                         P[u] = corner[toff[t]];
                         w[u] = tpsf[t];
@@ -664,7 +659,7 @@ __global__ void __launch_bounds__(512) k_psf_x_rows(StaticData sd, const GridSta
                 for (int u = 0; u < 4; u++) {
                     if (P[u].x >= r0 && P[u].x < r1)                // inactive (-1) or another chunk
                         atomicAdd(reinterpret_cast<unsigned long long*>(&acc[P[u].x - r0]),
-                                  (unsigned long long)f2ll_rn_int(w[u] * v));
+                                  (unsigned long long)((long long)w[u] * v));
                 }
             }
         }
@@ -810,7 +805,7 @@ static void psfx_band_geom(int nx, int ny, int pnx, int pny, int split, int& H, 
 {
     const int nT = pnx * pny;
     const int W = nx + pnx - 1;
-    const size_t tap_bytes = (sizeof(float) + sizeof(int)) * (size_t)nT + 8 * sizeof(int);
+    const size_t tap_bytes = 2 * sizeof(int) * (size_t)nT + 8 * sizeof(int) + 2 * sizeof(int) * PSFX_ECHUNK;
     const size_t avail = (110 * 1024 > tap_bytes) ? 110 * 1024 - tap_bytes : 0;
     const int fit = std::max(1, (int)(avail / (sizeof(long long) * W)));
     H = std::max(1, std::min(ny, fit) / split);

@@ -77,7 +77,7 @@ struct qlp_ctx {
     double* d_data = nullptr;
     double* d_covinv = nullptr;
     double* d_psf = nullptr;
-    float* d_psf_fix = nullptr;    // the PSF on the PSF-to-X fixed-point grid (StaticData::psf_fix)
+    int* d_psf_int = nullptr;      // the PSF on the PSF-to-X fixed-point grid (StaticData::psf_int)
     int* d_mpix = nullptr;
 
     // extra masks for batched evaluation (device mpix lists, concatenated)

@@ -93,6 +93,8 @@ struct OsbWork {
     double* model;  int* act;  double* sb;   // nx*ny
 };
 
+#define PSFX_LEXP 28               // grid of the L entries in the PSF-to-X products: 2^-28
+
 struct StaticData {            // per-context, uploaded once
     int nx, ny;                // image pixels
     int n_mask;                // masked pixels
@@ -108,13 +110,15 @@ struct StaticData {            // per-context, uploaded once
     const double* covinv;      // nx*ny (filled with cov_inverse when uniform)
     const int* mpix;           // n_mask: i*ny+j, j-outer / i-inner order
     const double* psf;         // pnx*pny
-    // fixed-point scale of the mixed path's PSF-to-X sums of psf x L
-    // (sqrt(C^-1) is applied to the sum): 2^fix_exp_x keeps 4 sum|psf| below
-    // 2^61 (|L entries| <= 4)
+    // fixed-point PSF-to-X sums of the mixed path (sqrt(C^-1) is applied to
+    // the sum): every product psf x L is the exact integer product of the tap
+    // on the grid 2^-(fix_exp_x - PSFX_LEXP) (psf_int, |psf_int| summing to at
+    // most 2^30) and the L entry on the grid 2^-PSFX_LEXP (|L| <= 4: at most
+    // 2^30), so a sum -- one entry per tap at most -- stays below 2^61
     int fix_exp_x;
-    // the PSF as floats scaled by 2^fix_exp_x, x fastest: psf_fix[pl * pnx + pk]
-    // = (float)psf[pk * pny + pl] * 2^fix_exp_x (a power of two: exact)
-    const float* psf_fix;
+    // the PSF on its grid, x fastest: psf_int[pl * pnx + pk] =
+    // round(psf[pk * pny + pl] * 2^(fix_exp_x - PSFX_LEXP))
+    const int* psf_int;
     // F16 operands of the mixed path's SYRK: X scaled by 2^x_exp puts its
     // largest possible entry (4 sum|psf| max sqrt(C^-1)) at or below 2^14
     int x_exp;
