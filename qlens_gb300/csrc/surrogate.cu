@@ -158,34 +158,6 @@ __device__ __forceinline__ SurIn sur_inputs(double X, double Y, double q)
     return s;
 }
 
-// The same inputs for the ray shooting, with the network's features (log R,
-// the polar angle) in FP32 -- the network reads them in FP32 anyway -- and
-// the baseline B in FP32 where that is accurate (sur_B32), else FP64.
-// inv_q = 1 / q.
-__device__ __forceinline__ SurIn sur_inputs_ray(double X, double Y, double q, double inv_q)
-{
-    SurIn s;
-    const double ax = fabs(X), ay = fabs(Y);
-    const float axf = (float)ax, ayf = (float)ay;
-    const float rho = 0.5f * __logf(__fmaf_rn(axf, axf, ayf * ayf));
-    const float phi = atan2f(ayf, axf);
-    const float hr = (float)(0.5 * (SUR_RHO_HI - SUR_RHO_LO)), mr = (float)(0.5 * (SUR_RHO_HI + SUR_RHO_LO));
-    const double hq = 0.5 * (1.0 - SUR_Q_LO), mq = 0.5 * (1.0 + SUR_Q_LO);
-    s.f0 = fminf(fmaxf((rho - mr) / hr, -2.0f), 2.0f);
-    s.f1 = phi * (float)(4.0 / M_PI) - 1.0f;
-    s.f2 = (float)fmin(fmax((q - mq) * (1.0 / hq), -2.0), 2.0);
-    s.bin = sur_cell((double)rho, (double)phi, q);
-    const double xi2 = q * ax * ax + ay * ay * inv_q;
-    if (xi2 >= SUR_B32_MIN) {
-        s.B = (double)sur_B32((float)xi2);
-        s.B_rel = SUR_B32_REL;
-    } else {
-        s.B = nfw_kapavg_spherical_rsq(1.0, 1.0, xi2);
-        s.B_rel = 0.0;
-    }
-    return s;
-}
-
 __device__ __forceinline__ uint64_t sur_hash(uint64_t x)
 {
     x += 0x9E3779B97F4A7C15ull;
@@ -725,7 +697,26 @@ struct SurTabs {
     double inv_rs[QLP_MAX_LENSES], inv_q[QLP_MAX_LENSES];
     double sie_u[QLP_MAX_LENSES], sie_pre[QLP_MAX_LENSES];
     double frac_u[SUBPIX_TAB], frac_1mu[SUBPIX_TAB];
+    // an NFW lens's constants in FP32 for the surrogate's per-ray arithmetic:
+    // 1/rs, q, 1/q, ks, cos and sin of its angle, and the network's q feature
+    float f_inv_rs[QLP_MAX_LENSES], f_q[QLP_MAX_LENSES], f_inv_q[QLP_MAX_LENSES], f_ks[QLP_MAX_LENSES];
+    float f_cos[QLP_MAX_LENSES], f_sin[QLP_MAX_LENSES], f_feat_q[QLP_MAX_LENSES];
+    int qbin[QLP_MAX_LENSES];    // the error cell's q index (sur_cell's), -1 outside the trained q range
 };
+
+// sur_cell from the network's FP32 inputs and the lens's q index (the cell
+// indices in log R and phi by the same multiplications in FP32: a ray within
+// rounding of a cell boundary may take the neighbouring cell's bound, both
+// estimated from points on either side of it)
+__device__ __forceinline__ int sur_cell_f(float rho, float phi, int qbin)
+{
+    if (qbin < 0 || !(rho >= (float)SUR_RHO_LO && rho < (float)SUR_RHO_HI)) return -1;
+    int ir = (int)((rho - (float)SUR_RHO_LO) * (float)(SUR_NB_RHO / (SUR_RHO_HI - SUR_RHO_LO)));
+    int ip = (int)(phi * (float)(SUR_NB_PHI / (0.5 * M_PI)));
+    ir = ir < 0 ? 0 : (ir >= SUR_NB_RHO ? SUR_NB_RHO - 1 : ir);
+    ip = ip < 0 ? 0 : (ip >= SUR_NB_PHI ? SUR_NB_PHI - 1 : ip);
+    return (ir * SUR_NB_PHI + ip) * SUR_NB_Q + qbin;
+}
 
 __device__ __forceinline__ void sur_tabs_fill(const EvalParams* __restrict__ ep, int nsplit, SurTabs& T)
 {
@@ -737,6 +728,21 @@ __device__ __forceinline__ void sur_tabs_fill(const EvalParams* __restrict__ ep,
         const bool sie0 = L.type == QLP_LENS_SPLE && L.kind == 1 && L.sprime == 0.0 && L.ssq == 0.0;
         T.sie_u[threadIdx.x] = sie0 ? sqrt(1 - L.qsq) : 0.0;
         T.sie_pre[threadIdx.x] = sie0 ? L.bprime * L.q / sqrt(1 - L.qsq) : 0.0;
+        const bool nfw = L.type == QLP_LENS_NFW;
+        T.f_inv_rs[threadIdx.x] = nfw ? (float)(1.0 / L.rs) : 0.f;
+        T.f_q[threadIdx.x] = (float)L.q;
+        T.f_inv_q[threadIdx.x] = nfw ? (float)(1.0 / L.q) : 0.f;
+        T.f_ks[threadIdx.x] = (float)L.ks;
+        T.f_cos[threadIdx.x] = (float)L.costheta;
+        T.f_sin[threadIdx.x] = (float)L.sintheta;
+        const double hq = 0.5 * (1.0 - SUR_Q_LO), mq = 0.5 * (1.0 + SUR_Q_LO);
+        T.f_feat_q[threadIdx.x] = (float)fmin(fmax((L.q - mq) * (1.0 / hq), -2.0), 2.0);
+        int iq = -1;
+        if (L.q >= SUR_Q_LO && L.q < 1.0) {
+            iq = (int)((L.q - SUR_Q_LO) * (SUR_NB_Q / (1.0 - SUR_Q_LO)));
+            iq = iq < 0 ? 0 : (iq >= SUR_NB_Q ? SUR_NB_Q - 1 : iq);
+        }
+        T.qbin[threadIdx.x] = iq;
     }
     subpix_table(nsplit, T.frac_u, T.frac_1mu);
 }
@@ -785,18 +791,29 @@ struct SurRayOut {
     int* fb_count; int* fb_ray; double* fb_xy;
 };
 
+// Relative error allowance of the FP32 arithmetic around the network
+// (inputs, B, G, alpha and its rotation, each within a few ulp: well below
+// 1e-6), added to every surrogate ray's bound
+#define SUR_F32_REL 2e-6f
+
 __device__ __forceinline__ void sur_nfw(SurWG& S, bool& ok, const LensRec& L, int k, const SurTabs& T,
                                         const float* __restrict__ bound, double thresh, double zabs, bool valid,
                                         int t, int defer_lens, const SurRayOut& q, int& fb, double& eps,
                                         double xi, double yi, double& ax, double& ay)
 {
-    // the FP64 work is the first half's; the second half takes the network's
-    // inputs from shared memory (after the group's reduction below)
+    // the per-ray work is the first half's; the second half takes the
+    // network's inputs from shared memory (after the group's reduction
+    // below).  The lens-frame position is formed in FP64 (a difference of
+    // nearby coordinates), everything after it in FP32: the network's own
+    // error, bounded per cell at 1e-5 and more, dwarfs FP32 rounding, and
+    // SUR_F32_REL covers it in the bound.
     const int tid = threadIdx.x & 127;
     const bool first = S.half == 0;
-    double x = 0, y = 0, bnd = 0, B = 0;
+    double x = 0, y = 0;
+    float xf = 0.f, yf = 0.f, bnd = 0.f, B = 0.f;
     bool rot = false, centre = false, inb = false, maybe = false;
     float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+    const float thr = (float)thresh;
     if (first) {
         x = xi - L.xc; y = yi - L.yc;
         rot = (L.sintheta != 0);
@@ -805,22 +822,38 @@ __device__ __forceinline__ void sur_nfw(SurWG& S, bool& ok, const LensRec& L, in
             y = -x * L.sintheta + y * L.costheta;
             x = xp;
         }
-        const SurIn in = sur_inputs_ray(x * T.inv_rs[k], y * T.inv_rs[k], L.q, T.inv_q[k]);
-        centre = (fabs(x) < 1e-14) && (fabs(y) < 1e-14);
-        inb = in.bin >= 0;
-        B = in.B;
-        // the cell's bound on the relative error of G, plus B's
-        bnd = inb ? (double)bound[in.bin] + in.B_rel : 0.0;
+        xf = (float)x; yf = (float)y;
+        centre = (fabsf(xf) < 1e-14f) && (fabsf(yf) < 1e-14f);
+        // the network's inputs (log R, polar angle, q), its error cell, and
+        // the baseline B at xi^2 = q X^2 + Y^2 / q
+        const float Xa = fabsf(xf * T.f_inv_rs[k]), Ya = fabsf(yf * T.f_inv_rs[k]);
+        const float rho = 0.5f * __logf(__fmaf_rn(Xa, Xa, Ya * Ya));
+        const float phi = atan2f(Ya, Xa);
+        const float hr = (float)(0.5 * (SUR_RHO_HI - SUR_RHO_LO)), mr = (float)(0.5 * (SUR_RHO_HI + SUR_RHO_LO));
+        f0 = fminf(fmaxf((rho - mr) / hr, -2.0f), 2.0f);
+        f1 = phi * (float)(4.0 / M_PI) - 1.0f;
+        f2 = T.f_feat_q[k];
+        const int bin = sur_cell_f(rho, phi, T.qbin[k]);
+        inb = bin >= 0;
+        const float xi2 = T.f_q[k] * Xa * Xa + Ya * Ya * T.f_inv_q[k];
+        float brel = 0.f;
+        if (xi2 >= (float)SUR_B32_MIN) {
+            B = sur_B32(xi2);
+            brel = (float)SUR_B32_REL;
+        } else {                                   // small radius: the FP64 form (its series cancels)
+            const double Xd = x * T.inv_rs[k], Yd = y * T.inv_rs[k];
+            B = (float)nfw_kapavg_spherical_rsq(1.0, 1.0, L.q * Xd * Xd + Yd * Yd * T.inv_q[k]);
+        }
+        // the cell's bound on the relative error of G, plus B's and the FP32 arithmetic's
+        bnd = inb ? bound[bin] + brel + SUR_F32_REL : 0.f;
         // before the network: |alpha| ~ ks B |(x, y)| (G is within a few tens of
         // percent of B), so a group none of whose rays can pass the gate skips
-        // the network and sends every ray to the quadrature (the gates compare
-        // squares: no FP64 square root)
-        const double gb = L.ks * in.B * bnd;
-        maybe = valid && !centre && inb && gb * gb * (x * x + y * y) <= 2.25 * thresh * thresh;
-        f0 = in.f0; f1 = in.f1; f2 = in.f2;
+        // the network and sends every ray to the quadrature (squares compared)
+        const float gb = T.f_ks[k] * B * bnd;
+        maybe = valid && !centre && inb && gb * gb * (xf * xf + yf * yf) <= 2.25f * thr * thr;
         S.xin[tid] = make_float4(f0, f1, f2, 0.f);
     }
-    double bx = 0, by = 0;
+    float bxf = 0.f, byf = 0.f;
     bool use = false;
     if (wg_any(S.wg, maybe)) {
         if (!first) {
@@ -830,33 +863,42 @@ __device__ __forceinline__ void sur_nfw(SurWG& S, bool& ok, const LensRec& L, in
         float t0, t1;
         sur_mlp_wg(S, f0, f1, f2, t0, t1, ok);
         if (first) {
-            const float oq = (float)(1.0 - L.q);
-            const double G0 = B * (double)expf(oq * t0), G1 = B * (double)expf(oq * t1);
-            bx = x * L.ks * G0;
-            by = y * L.ks * G1;
-            const double m2 = bx * bx + by * by;
-            use = ok && !centre && inb && m2 * bnd * bnd <= thresh * thresh;
-            // |alpha| in FP32, rounded up by far more than its error
-            if (use) eps += 2.0 * zabs * (double)(sqrtf((float)m2) * 1.000001f) * bnd;
+            const float oq = 1.0f - T.f_q[k];
+            const float kb = T.f_ks[k] * B;
+            bxf = xf * (kb * expf(oq * t0));
+            byf = yf * (kb * expf(oq * t1));
+            const float m2 = bxf * bxf + byf * byf;
+            use = ok && !centre && inb && m2 * bnd * bnd <= thr * thr;
+            // |alpha| rounded up by far more than its error
+            if (use) eps += 2.0 * zabs * (double)(sqrtf(m2) * 1.000001f * bnd);
         }
     }
     if (!first) { ax = 0; ay = 0; return; }
-    if (!use && valid) {
+    if (use) {
+        if (rot) {
+            const float xp = bxf * T.f_cos[k] - byf * T.f_sin[k];
+            byf = bxf * T.f_sin[k] + byf * T.f_cos[k];
+            bxf = xp;
+        }
+        ax = (double)bxf; ay = (double)byf;
+        return;
+    }
+    double bx = 0, by = 0;
+    if (valid) {
         fb++;
         if (k == defer_lens) {
             const int e = atomicAdd(q.fb_count, 1);
             q.fb_ray[e] = t;
             q.fb_xy[2 * (size_t)e] = x;
             q.fb_xy[2 * (size_t)e + 1] = y;
-            bx = 0; by = 0;
         } else {
             nfw_deflection(L, x, y, bx, by);
+            if (rot) {
+                const double xp = bx * L.costheta - by * L.sintheta;
+                by = bx * L.sintheta + by * L.costheta;
+                bx = xp;
+            }
         }
-    }
-    if (rot) {
-        const double xp = bx * L.costheta - by * L.sintheta;
-        by = bx * L.sintheta + by * L.costheta;
-        bx = xp;
     }
     ax = bx; ay = by;
 }
