@@ -86,11 +86,15 @@ __device__ __forceinline__ float sur_tanh(float x)
     return 1.0f - __fdividef(2.0f, 1.0f + __expf(2.0f * x));
 }
 
-// s tanh(x) for a power of two s, as one FMA after the quotient: the same
-// bits as sur_tanh(x) * s (scaling by s commutes with the rounding)
-__device__ __forceinline__ float sur_tanh_scaled(float x, float s)
+// s tanh(x) from a = 2 log2(e) x (the inference's parameters carry the
+// factor): s - 2 s / (1 + 2^a) with the SFU's base-2 exponential and
+// reciprocal, one FMA for the rest
+__device__ __forceinline__ float sur_tanh_a(float a, float s)
 {
-    return __fmaf_rn(-s, __fdividef(2.0f, 1.0f + __expf(2.0f * x)), s);
+    float e, r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(a));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+    return __fmaf_rn(-2.0f * s, r, s);
 }
 
 struct SurIn {
@@ -390,7 +394,8 @@ __global__ void k_sur_adam(int n, float* __restrict__ p, const float* __restrict
 // bits, as 3xTF32, at the F16 tensor rate).  The activations (tanh, |h| <= 1)
 // enter scaled by 2^SUR_ACT_EXP and each layer's weights by 2^s_l (largest
 // entry near 2^14), so both parts stay in F16's normal range; the epilogue
-// multiplies the accumulator by 2^-(SUR_ACT_EXP + s_l), which is exact.
+// multiplies the accumulator by 2^-(SUR_ACT_EXP + s_l) (exact), times the
+// factor 2 log2(e) of tanh's base-2 form.
 //   B (weights): resident in shared memory for the kernel's life -- the F16
 //     image [3 layers][hi, lo][2 K blocks][128 output rows][64 inputs] in the
 //     128-byte swizzled K-major layout the MMA descriptor reads (192 KB),
@@ -514,10 +519,8 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
             const float2 w1 = *reinterpret_cast<const float2*>(W0 + SUR_H + u);
             const float2 w2 = *reinterpret_cast<const float2*>(W0 + 2 * SUR_H + u);
             const float2 b0 = *reinterpret_cast<const float2*>(bb + u);
-            const float h0 = sur_tanh_scaled(__fmaf_rn(w2.x, f2, __fmaf_rn(w1.x, f1, __fmaf_rn(w0.x, f0, b0.x))),
-                                             ascale);
-            const float h1 = sur_tanh_scaled(__fmaf_rn(w2.y, f2, __fmaf_rn(w1.y, f1, __fmaf_rn(w0.y, f0, b0.y))),
-                                             ascale);
+            const float h0 = sur_tanh_a(__fmaf_rn(w2.x, f2, __fmaf_rn(w1.x, f1, __fmaf_rn(w0.x, f0, b0.x))), ascale);
+            const float h1 = sur_tanh_a(__fmaf_rn(w2.y, f2, __fmaf_rn(w1.y, f1, __fmaf_rn(w0.y, f0, b0.y))), ascale);
             f16_split2(h0, h1, hi[j], lo[j]);
         }
         tmem_st_16cols_u(row + 128 + c / 2, hi);
@@ -564,10 +567,10 @@ __device__ void sur_mlp_wg(SurWG& S, float f0, float f1, float f2, float& t0, fl
             #pragma unroll
             for (int j = 0; j < 32; j += 4) {
                 const float4 b4v = *reinterpret_cast<const float4*>(bl + c + j);
-                v[j] = sur_tanh_scaled(__fmaf_rn(v[j], us, b4v.x), sc);
-                v[j + 1] = sur_tanh_scaled(__fmaf_rn(v[j + 1], us, b4v.y), sc);
-                v[j + 2] = sur_tanh_scaled(__fmaf_rn(v[j + 2], us, b4v.z), sc);
-                v[j + 3] = sur_tanh_scaled(__fmaf_rn(v[j + 3], us, b4v.w), sc);
+                v[j] = sur_tanh_a(__fmaf_rn(v[j], us, b4v.x), sc);
+                v[j + 1] = sur_tanh_a(__fmaf_rn(v[j + 1], us, b4v.y), sc);
+                v[j + 2] = sur_tanh_a(__fmaf_rn(v[j + 2], us, b4v.z), sc);
+                v[j + 3] = sur_tanh_a(__fmaf_rn(v[j + 3], us, b4v.w), sc);
             }
             if (l < 3) {
                 uint32_t hi[16], lo[16];
@@ -1121,7 +1124,9 @@ static SurState g_sur[64];
 // (2 l + h) SUR_OPB + (k / 64) (SUR_OPB / 2) + 128 n + 16 ((k % 64) / 8 XOR n % 8)
 // + 2 (k % 8), the 128-byte swizzled K-major layout -- each layer scaled by
 // 2^sexp[l]; and the small parameters, with the target normalisation folded
-// into the output layer and the unscale factors 2^-(SUR_ACT_EXP + sexp[l]).
+// into the output layer, the unscale factors 2^-(SUR_ACT_EXP + sexp[l]), and
+// the factor 2 log2(e) of tanh's base-2 form on W0, the hidden biases and the
+// unscale factors.
 __global__ void k_sur_prep(const float* __restrict__ p, unsigned char* __restrict__ wimg, float* __restrict__ small,
                            float mu0, float mu1, float sg0, float sg1, int3 sexp)
 {
@@ -1138,17 +1143,21 @@ __global__ void k_sur_prep(const float* __restrict__ p, unsigned char* __restric
         *reinterpret_cast<__half*>(wimg + (size_t)(2 * l + 1) * SUR_OPB + off) = lo;
     }
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < SUR_SMALL; e += gridDim.x * blockDim.x) {
+        // (W0, the hidden biases and the unscale factors carry the factor
+        // 2 log2(e) of tanh(x) = 1 - 2 / (1 + 2^(2 log2(e) x)): the
+        // epilogues' FMA yields the exponent directly)
+        const float c2 = (float)(2.0 * 1.4426950408889634);
         float v;
-        if (e < 3 * SUR_H) v = p[SUR_W0 + e];
+        if (e < 3 * SUR_H) v = p[SUR_W0 + e] * c2;
         else if (e < 7 * SUR_H) {
             const int l = (e - 3 * SUR_H) / SUR_H, u = (e - 3 * SUR_H) % SUR_H;
-            v = p[SUR_B0 + l * (SUR_H * SUR_H + SUR_H) + u];
+            v = p[SUR_B0 + l * (SUR_H * SUR_H + SUR_H) + u] * c2;
         } else if (e < 9 * SUR_H) v = p[SUR_W4 + (e - 7 * SUR_H)] * (((e - 7 * SUR_H) & 1) ? sg1 : sg0);
         else if (e < 9 * SUR_H + 2)
             v = p[SUR_B4 + (e - 9 * SUR_H)] * ((e & 1) ? sg1 : sg0) + ((e & 1) ? mu1 : mu0);   // un-normalised s
         else {
             const int l = e - (9 * SUR_H + 2);
-            v = ldexpf(1.0f, -(SUR_ACT_EXP + ((l == 0) ? sexp.x : (l == 1) ? sexp.y : sexp.z)));
+            v = ldexpf(1.0f, -(SUR_ACT_EXP + ((l == 0) ? sexp.x : (l == 1) ? sexp.y : sexp.z))) * c2;
         }
         small[e] = v;
     }
