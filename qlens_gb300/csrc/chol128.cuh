@@ -599,19 +599,34 @@ __global__ void __launch_bounds__(256) k_trsv128_fwd(const float* __restrict__ L
     const int k = blockIdx.x;
     if (k >= nb) return;
     const int o = k * C2, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // the diagonal block's inverse rows (two threads per row) and, before each
+    // wait, this thread's part of the next block of L's strip are loaded
+    // first: their latency overlaps the wait for the block they multiply
+    const int irow = tid >> 1, ih = tid & 1;
+    float4 lv[16];
+    {
+        const float4* Lr =
+            reinterpret_cast<const float4*>(Linv + (size_t)k * 2 * C2 * C2 + (size_t)irow * C2 + ih * 64);
+        #pragma unroll
+        for (int u = 0; u < 16; u++) lv[u] = Lr[u];
+    }
     float part[16];
     #pragma unroll
     for (int i = 0; i < 16; i++) part[i] = 0.f;
     for (int j = 0; j < k;) {
+        float4 lp[16];
+        #pragma unroll
+        for (int i = 0; i < 16; i++)
+            lp[i] = *reinterpret_cast<const float4*>(L + (size_t)(o + warp * 16 + i) * ld + j * C2 + 4 * lane);
         const int n = wait_ready(flags, j, k, 1, gs, &sh);
         if (n == 0) return;
         for (int jj = j; jj < j + n; jj++) {
             const float4 yv = __ldcg(reinterpret_cast<const float4*>(y + (size_t)jj * C2) + lane);
             #pragma unroll
             for (int i = 0; i < 16; i++) {
-                const float4 lv =
-                    *reinterpret_cast<const float4*>(L + (size_t)(o + warp * 16 + i) * ld + jj * C2 + 4 * lane);
-                part[i] += lv.x * yv.x + lv.y * yv.y + lv.z * yv.z + lv.w * yv.w;
+                const float4 lw = (jj == j) ? lp[i]
+                    : *reinterpret_cast<const float4*>(L + (size_t)(o + warp * 16 + i) * ld + jj * C2 + 4 * lane);
+                part[i] += lw.x * yv.x + lw.y * yv.y + lw.z * yv.z + lw.w * yv.w;
             }
         }
         j += n;
@@ -625,20 +640,15 @@ __global__ void __launch_bounds__(256) k_trsv128_fwd(const float* __restrict__ L
     __syncthreads();
     if (tid < C2) t[tid] = ((o + tid < M) ? (float)r[o + tid] : 0.f) - red[tid >> 4][tid & 15];
     __syncthreads();
-    {   // y_k = Linv_k t: two threads per row, a half row each, all loads in flight
-        const int row = tid >> 1, h = tid & 1;
-        const float4* Lr = reinterpret_cast<const float4*>(Linv + (size_t)k * 2 * C2 * C2 + (size_t)row * C2 + h * 64);
-        float4 lv[16];
-        #pragma unroll
-        for (int u = 0; u < 16; u++) lv[u] = Lr[u];
+    {   // y_k = Linv_k t: two threads per row, a half row each
         float acc = 0.f;
         #pragma unroll
         for (int u = 0; u < 16; u++) {
-            const int m = h * 64 + 4 * u;
+            const int m = ih * 64 + 4 * u;
             acc += lv[u].x * t[m] + lv[u].y * t[m + 1] + lv[u].z * t[m + 2] + lv[u].w * t[m + 3];
         }
         acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        if (h == 0) y[o + row] = acc;
+        if (ih == 0) y[o + irow] = acc;
     }
     __threadfence();
     __syncthreads();
@@ -657,8 +667,22 @@ __global__ void __launch_bounds__(256) k_trsv128_bwd(const float* __restrict__ L
     const int b = blockIdx.x;
     if (b >= nb) return;
     const int kb = nb - 1 - b, o = kb * C2, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // as in the forward sweep: the inverse's rows and, before each wait, the
+    // next block of L's column strip are loaded first
+    const int ic = tid >> 1, ih = tid & 1;
+    float4 lv[16];
+    {
+        const float4* Lr =
+            reinterpret_cast<const float4*>(Linv + (size_t)kb * 2 * C2 * C2 + C2 * C2 + (size_t)ic * C2 + ih * 64);
+        #pragma unroll
+        for (int u = 0; u < 16; u++) lv[u] = Lr[u];
+    }
     float4 part = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int j = nb - 1; j > kb;) {
+        float4 lp[16];
+        #pragma unroll
+        for (int i = 0; i < 16; i++)
+            lp[i] = *reinterpret_cast<const float4*>(L + (size_t)(j * C2 + warp * 16 + i) * ld + o + 4 * lane);
         const int n = wait_ready(flags, j, kb, -1, gs, &sh);
         if (n == 0) return;
         for (int jj = j; jj > j - n; jj--) {
@@ -666,8 +690,8 @@ __global__ void __launch_bounds__(256) k_trsv128_bwd(const float* __restrict__ L
             for (int i = 0; i < 16; i++) {
                 const int row = jj * C2 + warp * 16 + i;
                 const float zv = __ldcg(zf + row);
-                const float4 lv = *reinterpret_cast<const float4*>(L + (size_t)row * ld + o + 4 * lane);
-                part.x += lv.x * zv; part.y += lv.y * zv; part.z += lv.z * zv; part.w += lv.w * zv;
+                const float4 lw = (jj == j) ? lp[i] : *reinterpret_cast<const float4*>(L + (size_t)row * ld + o + 4 * lane);
+                part.x += lw.x * zv; part.y += lw.y * zv; part.z += lw.z * zv; part.w += lw.w * zv;
             }
         }
         j -= n;
@@ -683,20 +707,14 @@ __global__ void __launch_bounds__(256) k_trsv128_bwd(const float* __restrict__ L
     }
     __syncthreads();
     {   // z_k = Linv_k^T t from the stored transpose: two threads per row of it
-        const int c = tid >> 1, h = tid & 1;
-        const float4* Lr =
-            reinterpret_cast<const float4*>(Linv + (size_t)kb * 2 * C2 * C2 + C2 * C2 + (size_t)c * C2 + h * 64);
-        float4 lv[16];
-        #pragma unroll
-        for (int u = 0; u < 16; u++) lv[u] = Lr[u];
         float acc = 0.f;
         #pragma unroll
         for (int u = 0; u < 16; u++) {
-            const int m = h * 64 + 4 * u;
+            const int m = ih * 64 + 4 * u;
             acc += lv[u].x * t[m] + lv[u].y * t[m + 1] + lv[u].z * t[m + 2] + lv[u].w * t[m + 3];
         }
         acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        if (h == 0) { zf[o + c] = acc; zout[o + c] = (double)acc; }
+        if (ih == 0) { zf[o + ic] = acc; zout[o + ic] = (double)acc; }
     }
     __threadfence();
     __syncthreads();

@@ -466,10 +466,10 @@ __global__ void __launch_bounds__(256) k_psfx_meta(StaticData sd, const GridStat
     }
 }
 
-// X's first Mp rows (cells) cleared before the band kernel, which then writes
-// only the active rows of its windows: 16-byte stores, every column of X
-// (K_cap, a multiple of 64) -- the tail beyond N included, which the SYRK
-// reads as whole 64-pixel stages.
+// X's first Mp rows (cells) cleared by 16-byte stores, every column of X
+// (K_cap, a multiple of 64): after the SYRK of the "rows" schedule, which
+// writes every entry of its rows, so that X is all zero again for a band
+// evaluation (whose own writes k_x_clean undoes).
 __global__ void k_zero_x(const GridState* __restrict__ gs, uint4* __restrict__ Xh, uint4* __restrict__ Xl,
                          size_t row_vec)
 {
@@ -479,6 +479,42 @@ __global__ void k_zero_x(const GridState* __restrict__ gs, uint4* __restrict__ X
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         Xh[i] = z;
         Xl[i] = z;
+    }
+}
+
+// After the SYRK has read X: the entries the band kernel wrote (the active
+// pixels of each item's window) set back to zero, so that X is all zero when
+// the next evaluation's band kernel starts -- instead of clearing all of it
+// (k_zero_x: ~480 MB per cfg5 evaluation) before.  The "rows" schedule
+// writes every entry of its rows and clears X with k_zero_x after the SYRK.
+__global__ void __launch_bounds__(256) k_x_clean(StaticData sd, const GridState* __restrict__ gs,
+                                                 const int2* __restrict__ pixT, int nband,
+                                                 const int4* __restrict__ meta, void* __restrict__ Xh,
+                                                 void* __restrict__ Xl, int half, int K_cap)
+{
+    const int M = gs->M;
+    const int Mp = (M + TC_TILE - 1) / TC_TILE * TC_TILE;
+    const int s = blockIdx.x;
+    if (s >= Mp) return;
+    const size_t item = (size_t)s * nband + blockIdx.y;
+    const int4 m0 = meta[2 * item], m1 = meta[2 * item + 1];
+    if (m0.y <= m0.x) return;
+    const int nxh = sd.pnx / 2, nyh = sd.pny / 2, nxp = sd.nx + 2 * nxh;
+    const int imin = m0.z, Wb = m0.w - imin + sd.pnx, wr0 = m1.x, area = (m1.y - m1.x) * Wb;
+    for (int e = threadIdx.x; e < area; e += blockDim.x) {
+        const int jr = e / Wb, wc = e - jr * Wb;
+        const int i = imin - nxh + wc, j = wr0 + jr;
+        if (i < 0 || i >= sd.nx) continue;
+        const int r = pixT[(size_t)(j + nyh) * nxp + i + nxh].x;
+        if (r < 0) continue;
+        const size_t idx = (size_t)s * K_cap + r;
+        if (half) {
+            reinterpret_cast<__half*>(Xh)[idx] = __float2half_rn(0.0f);
+            reinterpret_cast<__half*>(Xl)[idx] = __float2half_rn(0.0f);
+        } else {
+            reinterpret_cast<float*>(Xh)[idx] = 0.0f;
+            reinterpret_cast<float*>(Xl)[idx] = 0.0f;
+        }
     }
 }
 
@@ -572,7 +608,7 @@ __global__ void __launch_bounds__(512) k_psf_x_band(StaticData sd, const GridSta
     // X[s][r] for the active pixels r of the window: v = sqrt(C^-1)_r * sum,
     // split into hi + lo; the window's pixels are visited x fastest through
     // the padded image's (active row, sqrt(C^-1)) table.  Every other entry
-    // of X's row s is zero (k_zero_x).
+    // of X's row s is zero (X is all zero between evaluations: k_x_clean).
     {
         const int nxp = sd.nx + 2 * nxh;
         const int area = (wr1 - wr0) * Wb;
@@ -989,6 +1025,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
     n++;
     // X = (P L sqrt(C^-1))^T and its block flags, from L by source cell
     const float xs = m->half ? ldexpf(1.0f, sd.x_exp) : 1.0f;     // F16 scale of X
+    int band_nband = 0;                                               // bands of the band schedule (0: rows)
     {
         const int nT = sd.pnx * sd.pny;
         const int split = std::max(1, std::min(c->psfx_split, 4));
@@ -997,10 +1034,9 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
             int H = 1, nband = 1;
             size_t smem = 0;
             psfx_band_geom(sd.nx, sd.ny, sd.pnx, sd.pny, split, H, nband, smem);
-            // X's rows cleared, each item's set-up, then the windows
-            const size_t row_vec = (size_t)m->K_cap * (m->half ? 2 : 4) / 16;
-            k_zero_x<<<152 * 8, 256, 0, st>>>(w.gs, reinterpret_cast<uint4*>(m->X_hi),
-                                              reinterpret_cast<uint4*>(m->X_lo), row_vec);
+            // each item's set-up, then the windows (X is all zero here: the
+            // previous evaluation cleaned it after its SYRK, see below)
+            band_nband = nband;
             k_psfx_meta<<<(m->M_cap * nband + 7) / 8, 256, 0, st>>>(sd, w.gs, m->colcnt, m->colrow, w.rowpix, H,
                                                                   nband, m->psfx_meta);
             if (sd.pnx <= 32 && sd.pny <= 32)
@@ -1011,7 +1047,7 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
                 k_psf_x_band<false><<<dim3(m->M_cap, nband), pt, smem, st>>>(
                     sd, w.gs, m->colcnt, m->colrow, m->colval, w.rowpix, m->pixT, nband, m->psfx_meta, m->X_hi,
                     m->X_lo, xs, m->half ? 1 : 0, m->K_cap, m->nz, m->nkb_cap);
-            n += 2;
+            n += 1;
         } else {
             // accumulator rows per CTA: the active rows split into psfx_split
             // chunks (or more, if a chunk does not fit beside the PSF in 227 KB)
@@ -1037,6 +1073,16 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
         else
             k_syrk_tc<false><<<nt * (nt + 1) / 2, 128, TC_SMEM, st>>>(m->map_hi, m->map_lo, w.gs, m->nz,
                                                                        m->nkb_cap, m->F32, m->ld32, 1.0f);
+        n++;
+        // X back to all zero for the next evaluation
+        if (band_nband > 0) {
+            k_x_clean<<<dim3(m->M_cap, band_nband), 256, 0, st>>>(sd, w.gs, m->pixT, band_nband, m->psfx_meta,
+                                                                  m->X_hi, m->X_lo, m->half ? 1 : 0, m->K_cap);
+        } else {
+            const size_t row_vec = (size_t)m->K_cap * (m->half ? 2 : 4) / 16;
+            k_zero_x<<<152 * 8, 256, 0, st>>>(w.gs, reinterpret_cast<uint4*>(m->X_hi),
+                                              reinterpret_cast<uint4*>(m->X_lo), row_vec);
+        }
         n++;
     }
     if (ev) cudaEventRecord(ev[4], st);
