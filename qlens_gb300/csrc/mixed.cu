@@ -920,14 +920,28 @@ int mixed_init(Slot& c)
         set_error("%s (%d)", "cuTensorMapEncodeTiled unavailable or failed", 0);
         return QLP_ERR_CUDA;
     }
-    cudaFuncSetAttribute(k_psf_x_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_psf_x_band<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_psf_x_band<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, P128_SMEM);
-    cudaFuncSetAttribute(k_chol_tile128, cudaFuncAttributeMaxDynamicSharedMemorySize, T128_SMEM);
-    cudaFuncSetAttribute(k_chol_upd16, cudaFuncAttributeMaxDynamicSharedMemorySize, U16_SMEM);
-    cudaFuncSetAttribute(k_syrk_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    cudaFuncSetAttribute(k_syrk_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    // shared-memory opt-ins (a kernel's static and dynamic shared memory
+    // together may not pass 227 KB): a failed opt-in is reported here, not at
+    // the first launch that needs it
+    {
+        cudaError_t ea = cudaSuccess;
+        auto opt = [&](const void* f, int bytes) {
+            const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (ea == cudaSuccess) ea = r;
+        };
+        opt((const void*)k_psf_x_rows, 227 * 1024);
+        opt((const void*)k_psf_x_band<true>, 227 * 1024);
+        opt((const void*)k_psf_x_band<false>, 227 * 1024);
+        opt((const void*)k_potrf128, P128_SMEM);
+        opt((const void*)k_chol_tile128, T128_SMEM);
+        opt((const void*)k_chol_upd16, U16_SMEM);
+        opt((const void*)k_syrk_tc<false>, TC_SMEM);
+        opt((const void*)k_syrk_tc<true>, TC_SMEM);
+        if (ea != cudaSuccess) {
+            set_error("%s (%d)", "shared-memory opt-in failed", (int)ea);
+            return QLP_ERR_CUDA;
+        }
+    }
     m->ready = true;
     return QLP_OK;
 }
