@@ -481,6 +481,14 @@ def main():
                      "traffic": SYRK_TRAFFIC.get(args.config) if precision == "mixed" else None,
                      "peak_source": peak_note, "algorithmic_flops_per_launch": flops,
                      "timing": "CUDA events around the SYRK launch of single evaluations after the timed region"}
+    if precision != "mixed":
+        # k_syrk64 skips the 16-pixel steps where either tile of L' is zero
+        # (the products it leaves out are zeros): the dense N M^2 count over
+        # its time is a dense-equivalent rate, not a fraction of the pipe
+        roofline_syrk["frac"] = None
+        roofline_syrk["dense_equivalent_frac"] = (achieved / peak) if achieved else None
+        roofline_syrk["note"] = ("achieved = the dense contraction's FLOP over the time of a kernel that skips L''s "
+                                 "zero blocks: above the FP64 peak because most products are skipped")
     # the dominant kernel of the batch: the ray shooting on the NFW surrogate
     # workloads (k_raytrace_sur), else the factorisation of F
     roofline = roofline_syrk
@@ -494,10 +502,21 @@ def main():
                     "traffic": RAYSUR_TRAFFIC.get(args.config), "peak_source": peak_note,
                     "algorithmic_flops_per_launch": mlp,
                     "work": "the network's three 128x128 layers per ray (2 x 3 x 128^2 FLOP), %d rays" % n_rays,
-                    "limiter": "the network's SIMT epilogues (SFU tanh, F16 hi/lo split, TMEM loads and stores) at "
-                               "16 warps per SM: tensor pipe 20%, FP64 pipe 30% in k_raytrace_sur; the FP64 lenses "
-                               "in k_ray_pre at 85% of the FP64 pipe (one ncu capture)",
+                    "limiter": "the network's SIMT epilogues (tanh from the SFU's exp2 and reciprocal, F16 hi/lo "
+                               "split, TMEM loads and stores) at 16 warps per SM: tensor pipe 29%, SFU 26%, FMA 20%, "
+                               "FP64 7% in k_raytrace_sur, top stall the TMEM and ray loads; the FP64 lenses in "
+                               "k_ray_pre at 85% of the FP64 pipe (one ncu capture)",
                     "timing": "CUDA events around the ray-shooting stage of single evaluations after the timed "
+                              "region"}
+    elif precision != "mixed":
+        # the plain path's largest stage: the FP64 blocked Cholesky of F
+        ch_flop = float(np.mean([r["n_active_src"] ** 3 / 3.0 for r in iso_res]))
+        ach = ch_flop / (stage[4] / 1e3) / 1e12 if stage[4] > 0 else None
+        roofline = {"bound": "fp64", "kernel": "FP64 Cholesky of F (k_potrf_t, k_trsm_inv_t, k_chol_update_t)",
+                    "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": (ach / peak) if ach else None,
+                    "traffic": None, "peak_source": peak_note, "algorithmic_flops_per_launch": ch_flop,
+                    "work": "M^3/3 FLOP per factorisation",
+                    "timing": "CUDA events around the factorisation stage of single evaluations after the timed "
                               "region"}
     elif precision == "mixed":
         ch_flop = float(np.mean([r["n_active_src"] ** 3 / 3.0 for r in iso_res]))
