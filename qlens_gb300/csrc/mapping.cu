@@ -37,6 +37,10 @@ __global__ void __launch_bounds__(256) k_grid_partial(StaticData sd_, SrcOpts so
     if (so.auto_grid) {
         const int nsub = sd.nsub;
         const bool use_nt = so.noise_threshold > 0;
+        // a power-of-two count divides as a multiply by its exact reciprocal
+        // (the same correctly rounded quotient, without the FP64 divide)
+        const bool pow2 = (nsub & (nsub - 1)) == 0;
+        const double inv_nsub = 1.0 / nsub;
         for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < sd.n_mask; m += gridDim.x * blockDim.x) {
             if (use_nt) {
                 int pix = sd.mpix[m];
@@ -45,7 +49,7 @@ __global__ void __launch_bounds__(256) k_grid_partial(StaticData sd_, SrcOpts so
             }
             double xs = 0, ys = 0;
             for (int k = 0; k < nsub; k++) { xs += spx[m * nsub + k]; ys += spy[m * nsub + k]; }
-            xs /= nsub; ys /= nsub;
+            if (pow2) { xs *= inv_nsub; ys *= inv_nsub; } else { xs /= nsub; ys /= nsub; }
             // NaN means are skipped, like the reference's failed comparisons
             if (xs == xs) { xmn = fmin(xmn, xs); xmx = fmax(xmx, xs); }
             if (ys == ys) { ymn = fmin(ymn, ys); ymx = fmax(ymx, ys); }

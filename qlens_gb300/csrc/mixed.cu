@@ -222,10 +222,12 @@ __global__ void k_csc_fill(const GridState* __restrict__ gs, const int* __restri
 // Each column's entries in increasing row order, so that every sum over a
 // column runs in a fixed order (k_csc_fill places them in atomic order).
 // Rows are distinct within a column of the merged L, so the order is a
-// permutation: a bitonic sort of the (row, source position) pairs in shared
-// memory for columns of up to CSC_SORT_MAX entries, else each entry's rank
-// counted directly.  One CTA per column.
+// permutation: a bitonic sort of the (row, source position) pairs, a warp
+// per column in registers for columns of up to CSC_SORT_WARP entries
+// (k_csc_sort_w), else one CTA per column in shared memory for up to
+// CSC_SORT_MAX entries, and past that each entry's rank counted directly.
 #define CSC_SORT_MAX 4096
+#define CSC_SORT_WARP 64    // columns sorted a warp each (k_csc_sort_w)
 __global__ void __launch_bounds__(256) k_csc_sort(const GridState* __restrict__ gs, const int* __restrict__ colptr,
                                                   const int* __restrict__ col_u, const int* __restrict__ src_u,
                                                   const double* __restrict__ cval, int* __restrict__ colrow,
@@ -236,6 +238,7 @@ __global__ void __launch_bounds__(256) k_csc_sort(const GridState* __restrict__ 
     const int s = blockIdx.x;
     if (s >= gs->M) return;
     const int b = colptr[s], n = colptr[s + 1] - b;
+    if (n <= CSC_SORT_WARP) return;                       // k_csc_sort_w's
     if (n <= CSC_SORT_MAX) {
         int p2 = 1;
         while (p2 < n) p2 <<= 1;
@@ -277,6 +280,81 @@ __global__ void __launch_bounds__(256) k_csc_sort(const GridState* __restrict__ 
         colval[b + rank] = (float)v;
         colval64[b + rank] = v;
     }
+}
+
+// Columns of up to CSC_SORT_WARP entries, a warp each: the same permutation
+// by a bitonic network in registers (R = 1 or 2 entries a lane, entry
+// lane + 32 h in register h; partners 32 apart within the lane, the others
+// through lane shuffles; no barriers); k_csc_sort takes the longer columns
+// (with more entries a lane the network's cost passed the block sort's).
+// The rows are distinct, so any sort gives the same order.
+__device__ __forceinline__ void csc_bitonic_step(int& key, int& pos, int e, int j, int k)
+{
+    const int kp = __shfl_xor_sync(0xffffffffu, key, j), pp = __shfl_xor_sync(0xffffffffu, pos, j);
+    const bool up = ((e & ~j) & k) == 0;                  // the pair's direction, from its lower index
+    const bool take_min = ((e & j) == 0) == up;
+    if (take_min ? (kp < key) : (kp > key)) { key = kp; pos = pp; }
+}
+
+template <int R>
+__device__ __forceinline__ void csc_sort_warp(const int* __restrict__ col_u, const int* __restrict__ src_u,
+                                              const double* __restrict__ cval, int b, int n, int lane,
+                                              int* __restrict__ colrow, float* __restrict__ colval,
+                                              double* __restrict__ colval64)
+{
+    int key[R], pos[R];
+    #pragma unroll
+    for (int h = 0; h < R; h++) {
+        const int e = lane + 32 * h;
+        key[h] = (e < n) ? col_u[b + e] : INT_MAX;
+        pos[h] = (e < n) ? src_u[b + e] : 0;
+    }
+    #pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+        #pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                #pragma unroll
+                for (int h = 0; h < R; h++) {
+                    const int h2 = h ^ (j >> 5);
+                    if (h2 > h) {
+                        const bool up = ((lane + 32 * h) & k) == 0;
+                        if ((key[h] > key[h2]) == up) {
+                            const int tk = key[h]; key[h] = key[h2]; key[h2] = tk;
+                            const int tp = pos[h]; pos[h] = pos[h2]; pos[h2] = tp;
+                        }
+                    }
+                }
+            } else {
+                #pragma unroll
+                for (int h = 0; h < R; h++) csc_bitonic_step(key[h], pos[h], lane + 32 * h, j, k);
+            }
+        }
+    }
+    #pragma unroll
+    for (int h = 0; h < R; h++) {
+        const int e = lane + 32 * h;
+        if (e < n) {
+            const double v = cval[pos[h]];
+            colrow[b + e] = key[h];
+            colval[b + e] = (float)v;
+            colval64[b + e] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) k_csc_sort_w(const GridState* __restrict__ gs,
+                                                       const int* __restrict__ colptr,
+                                                       const int* __restrict__ col_u, const int* __restrict__ src_u,
+                                                       const double* __restrict__ cval, int* __restrict__ colrow,
+                                                       float* __restrict__ colval, double* __restrict__ colval64)
+{
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (s >= gs->M) return;                                // whole warps
+    const int b = colptr[s], n = colptr[s + 1] - b;
+    if (n <= 32) csc_sort_warp<1>(col_u, src_u, cval, b, n, lane, colrow, colval, colval64);
+    else if (n <= CSC_SORT_WARP) csc_sort_warp<2>(col_u, src_u, cval, b, n, lane, colrow, colval, colval64);
 }
 
 // out[s] = sum over column s of L of value * w[row]: one warp per column, lane
@@ -1029,9 +1107,11 @@ int run_inversion_mixed(const qlp_ctx* c, Slot& slot, const StaticData& sd, cons
                                                      m->sqc, m->pixT);
         k_csc_scan<<<1, 1024, 0, st>>>(w.gs, m->colcnt, m->cursor);
         k_csc_fill<<<std::max(rb, 1), 256, 0, st>>>(w.gs, w.rowptr, w.cidx, w.ccnt, m->cursor, m->col_u, m->src_u);
+        k_csc_sort_w<<<(m->M_cap + 7) / 8, 256, 0, st>>>(w.gs, m->colcnt, m->col_u, m->src_u, w.cval, m->colrow,
+                                                        m->colval, m->colval64);
         k_csc_sort<<<m->M_cap, 256, 0, st>>>(w.gs, m->colcnt, m->col_u, m->src_u, w.cval, m->colrow, m->colval,
                                             m->colval64);
-        n += 4;
+        n += 5;
     }
     // D = L^T P^T (C^-1 d), FP64
     op_conv(sd, w, N_cap, true, w.dvec, w.cvec, m->t, m->img, m->pixT, st);

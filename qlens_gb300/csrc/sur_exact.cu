@@ -100,7 +100,10 @@ __global__ void __launch_bounds__(256) k_sur_exact_extremes(StaticData sd_, SrcO
             emax = fmaxf(emax, sur_eps[m * nsub + k]);
         }
         if (emax == 0.f) continue;
-        xs /= nsub; ys /= nsub;
+        // the mean as k_grid_partial forms it (a multiply by the exact
+        // reciprocal for a power-of-two count: the same quotient)
+        if ((nsub & (nsub - 1)) == 0) { const double inv = 1.0 / nsub; xs *= inv; ys *= inv; }
+        else { xs /= nsub; ys /= nsub; }
         const double tol = 2.0 * eps_g;
         const bool near = fabs(xs - e0) <= tol || fabs(xs - e1) <= tol || fabs(ys - e2) <= tol || fabs(ys - e3) <= tol;
         if (!near) continue;
